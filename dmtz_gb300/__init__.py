@@ -1,0 +1,203 @@
+"""dmtz_gb300 — GB300 implementation of DMTz's topology-correction path.
+
+Python front end of libdmtz (include/dmtz.h) through ctypes.  The compute
+runs in the CUDA library; nothing here falls back to the CPU: every function
+raises if the library or a GPU is missing.
+
+    import dmtz_gb300 as dm
+    ctx = dm.Context()
+    fixed, report = ctx.correct(f, g, rel_eps=1e-4, flags=(1, 1, 1, 0, 0, 0, 0))
+
+Arrays are float64 with shape (D, H, W) or flat, x fastest (the reference's
+vertex order).  Pairing arrays use the reference's cell numbering.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+__all__ = ["Context", "DmtzError", "Opts", "Report", "cell_counts", "load_library"]
+
+_lib = None
+
+STATUS = {0: "OK", 1: "ERR_CUDA", 2: "ERR_ARG", 3: "ERR_IO", 4: "ERR_NONCONVERGED", 5: "ERR_CYCLE",
+          6: "ERR_BOUND", 7: "ERR_UNSUPPORTED", 8: "ERR_OOB"}
+
+
+class DmtzError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Opts(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in (
+        "preserve_saddles", "preserve_vpath", "preserve_geometry", "filtration", "preserve_connectors",
+        "preserve_type", "edit_type", "max_rounds", "use_graph")]
+
+
+class Report(ctypes.Structure):
+    _fields_ = [("outer_iterations", ctypes.c_int64), ("cp_rounds", ctypes.c_int64), ("path_rounds", ctypes.c_int64),
+                ("initial_mismatch", ctypes.c_int64 * 4), ("final_mismatch", ctypes.c_int64 * 4),
+                ("final_paths", ctypes.c_int64 * 2), ("edited_vertices", ctypes.c_int64),
+                ("converged", ctypes.c_int32), ("error_flags", ctypes.c_int32), ("seconds", ctypes.c_double)]
+
+    def as_dict(self):
+        return dict(outer_iterations=self.outer_iterations, cp_rounds=self.cp_rounds, path_rounds=self.path_rounds,
+                    initial_mismatch=list(self.initial_mismatch), final_mismatch=list(self.final_mismatch),
+                    final_paths=list(self.final_paths), converged=bool(self.converged),
+                    error_flags=self.error_flags, seconds=self.seconds)
+
+
+_i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_i64p = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
+_vp = ctypes.c_void_p
+_int = ctypes.c_int
+
+
+def load_library(build_if_missing: bool = True):
+    """Load libdmtz.so (compiling it first if needed)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build_if_missing:
+        _build.build()
+    if not os.path.exists(_build.LIB):
+        raise OSError(f"libdmtz not built: {_build.LIB}")
+    L = ctypes.CDLL(_build.LIB)
+    L.dmtz_ctx_create.argtypes = [ctypes.POINTER(_vp), _int]
+    L.dmtz_ctx_destroy.argtypes = [_vp]
+    L.dmtz_ctx_destroy.restype = None
+    L.dmtz_last_error.argtypes = [_vp]
+    L.dmtz_last_error.restype = ctypes.c_char_p
+    L.dmtz_cell_counts.argtypes = [_int, _int, _int, _i64p]
+    L.dmtz_extract.argtypes = [_vp, _int, _int, _int, _vp, _int, _i32p, _i32p, _i32p, _i32p]
+    L.dmtz_mismatch.argtypes = [_vp, _int, _int, _int, _f64p, _f64p, _i64p, _i32p, _i32p, _i32p, _i32p]
+    L.dmtz_fix_round.argtypes = [_vp, _int, _int, _int, _f64p, _f64p, _i32p, ctypes.c_double, _int, _int, _f64p]
+    L.dmtz_path_detect.argtypes = [_vp, _int, _int, _int, _f64p, _f64p, _i64p, _i32p, _i32p, _i32p, _i32p]
+    L.dmtz_correct.argtypes = [_vp, _int, _int, _int, _vp, _vp, _int, ctypes.c_double, ctypes.POINTER(Opts),
+                               ctypes.POINTER(Report), _vp]
+    for fn in ("dmtz_ctx_create", "dmtz_cell_counts", "dmtz_extract", "dmtz_mismatch", "dmtz_fix_round",
+               "dmtz_path_detect", "dmtz_correct"):
+        getattr(L, fn).restype = _int
+    _lib = L
+    return L
+
+
+def cell_counts(dims):
+    W, H, D = dims
+    out = np.zeros(4, np.int64)
+    rc = load_library().dmtz_cell_counts(W, H, D, out)
+    if rc:
+        raise DmtzError(rc, "bad dims")
+    return tuple(int(x) for x in out)
+
+
+def _flat(a):
+    return np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
+
+
+def _dims_of(a, dims):
+    if dims is not None:
+        return tuple(int(x) for x in dims)
+    if a.ndim != 3:
+        raise ValueError("pass dims=(W, H, D) for flat arrays")
+    D, H, W = a.shape
+    return (W, H, D)
+
+
+class Context:
+    """Owns a CUDA device, a stream and the device buffers (dmtz_ctx)."""
+
+    def __init__(self, device: int = 0):
+        self._L = load_library()
+        h = _vp()
+        rc = self._L.dmtz_ctx_create(ctypes.byref(h), device)
+        if rc:
+            raise DmtzError(rc, "cannot create a context (no CUDA device?)")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.dmtz_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc:
+            raise DmtzError(rc, self._L.dmtz_last_error(self._h).decode())
+
+    # ------------------------------------------------------------------ stages
+    def extract(self, data, dims=None):
+        """Gradient pairing of one field -> (PV, PE, PF, PT) in the reference's layout."""
+        dims = _dims_of(np.asarray(data), dims)
+        d = _flat(data)
+        V, E, F, T = cell_counts(dims)
+        out = [np.empty(n, np.int32) for n in (V, E, F, T)]
+        self._check(self._L.dmtz_extract(self._h, *dims, d.ctypes.data, 0, *out))
+        return tuple(out)
+
+    def mismatch(self, f, g, dims=None):
+        """Sorted critical-cell mismatch lists (min, 1-saddle, 2-saddle, max)."""
+        dims = _dims_of(np.asarray(f), dims)
+        V, E, F, T = cell_counts(dims)
+        c = np.zeros(4, np.int64)
+        lists = [np.empty(max(n, 1), np.int32) for n in (V, E, F, T)]
+        self._check(self._L.dmtz_mismatch(self._h, *dims, _flat(f), _flat(g), c, *lists))
+        return [lists[k][: int(c[k])].copy() for k in range(4)]
+
+    def fix_round(self, f, g, cnt, rel_eps, preserve_saddles, edit_type, dims=None):
+        """Delta buffer of one critical-point fix round (sentinel -2000*range where nothing is requested)."""
+        dims = _dims_of(np.asarray(f), dims)
+        V = cell_counts(dims)[0]
+        out = np.empty(V, np.float64)
+        self._check(self._L.dmtz_fix_round(self._h, *dims, _flat(f), _flat(g), np.ascontiguousarray(cnt, np.int32),
+                                           float(rel_eps), int(preserve_saddles), int(edit_type), out))
+        return out
+
+    def path_detect(self, f, g, dims=None):
+        """Geometry-mode separatrix records (as_tet, as_cur, ds_edge, ds_vert), sorted."""
+        dims = _dims_of(np.asarray(f), dims)
+        V, E, F, T = cell_counts(dims)
+        c = np.zeros(2, np.int64)
+        at, ac = np.empty(F, np.int32), np.empty(F, np.int32)
+        de, dv = np.empty(E, np.int32), np.empty(E, np.int32)
+        self._check(self._L.dmtz_path_detect(self._h, *dims, _flat(f), _flat(g), c, at, ac, de, dv))
+        na, nd = int(c[0]), int(c[1])
+        return at[:na].copy(), ac[:na].copy(), de[:nd].copy(), dv[:nd].copy()
+
+    def correct(self, f, g, rel_eps, flags=(1, 1, 1, 0, 0, 0, 0), dims=None, max_rounds=0, use_graph=0,
+                return_counter=False):
+        """Full correction of g against f.  Returns (corrected g, report dict[, edit counter])."""
+        dims = _dims_of(np.asarray(f), dims)
+        ff = _flat(f)
+        gg = np.array(_flat(g), copy=True)
+        V = ff.size
+        cnt = np.empty(V, np.int32)
+        o = Opts(*[int(x) for x in flags], int(max_rounds), int(use_graph))
+        r = Report()
+        rc = self._L.dmtz_correct(self._h, *dims, ff.ctypes.data, gg.ctypes.data, 0, float(rel_eps),
+                                  ctypes.byref(o), ctypes.byref(r), cnt.ctypes.data)
+        self._check(rc)
+        rep = r.as_dict()
+        rep["edited_vertices"] = int((gg != _flat(g)).sum())
+        return (gg, rep, cnt) if return_counter else (gg, rep)
+
+    def correct_device(self, f_ptr: int, g_ptr: int, dims, rel_eps, flags=(1, 1, 1, 0, 0, 0, 0), max_rounds=0,
+                       use_graph=0):
+        """Correction on device-resident float64 buffers (raw CUDA pointers); g is edited in place."""
+        o = Opts(*[int(x) for x in flags], int(max_rounds), int(use_graph))
+        r = Report()
+        self._check(self._L.dmtz_correct(self._h, *dims, _vp(f_ptr), _vp(g_ptr), 1, float(rel_eps),
+                                         ctypes.byref(o), ctypes.byref(r), None))
+        return r.as_dict()

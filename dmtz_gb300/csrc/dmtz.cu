@@ -1,0 +1,768 @@
+// dmtz.cu — kernels and host driver of libdmtz (see include/dmtz.h).
+//
+// Data layout in HBM, per field (original f, decompressed g), one entry per
+// anchor vertex, structure of arrays:
+//   key u64 | low u16 | pv u8 | ea2 u32 | fp3 u16 | fa3 u32 | eup u32 | fup u32 | crit u32
+// plus, shared: f, g (float64), delta_counter (int32), request bits (1 bit per
+// vertex), the request list and the four mismatch lists (cell ids, int64).
+//
+// One correction round (main_3d.cu:6789-6921) is: fix rules on the mismatch
+// lists -> request bits/list; apply (bounded update of g); five pairing passes
+// on g; criticality + mismatch compaction.  Counters live on the device; the
+// host reads four words per round (or none, in the CUDA-graph loop).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/dmtz.h"
+#include "dmtz_common.cuh"
+#include "pairing.cuh"
+#include "rules.cuh"
+
+using namespace dmtz;
+
+namespace dmtz {
+
+static const int kBlock = 256;
+static inline unsigned grid_for(i64 n) { return (unsigned)std::max<i64>(1, (n + kBlock - 1) / kBlock); }
+
+// --------------------------------------------------------------- mismatch compaction
+struct Lists {
+    i64 *l[4];                  // min, 1-saddle, 2-saddle, max (reference cell ids)
+    unsigned long long *n;      // 4 counters
+};
+
+__device__ __forceinline__ void push_list(const Lists &L, int k, i64 id) {
+    const unsigned long long at = atomicAdd(&L.n[k], 1ull);
+    L.l[k][at] = id;
+}
+
+// criticality of g's gradient; mismatch against the original's criticality
+// (get_false_minimum / saddle / 2_saddle / maximum, main_3d.cu:2492-2550)
+__global__ void k_crit(Grid g, FieldState s, const uint32_t *crit_o, Lists L, int want_saddles, i64 v0, i64 n) {
+    i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const i64 v = v0 + t;
+    int x, y, z;
+    decode_v(g, v, x, y, z);
+    const uint32_t m = crit_mask(g, s, v, x, y, z);
+    s.crit[v] = m;
+    if (!crit_o) return;
+    uint32_t d = m ^ crit_o[v];
+    if (!want_saddles) d &= 1u | (0x3Fu << 20);
+    while (d) {
+        const int b = __ffs(d) - 1;
+        d &= d - 1;
+        if (b == 0) push_list(L, 0, v);
+        else if (b < 8) push_list(L, 1, edge_ref(g, x, y, z, b - 1));
+        else if (b < 20) push_list(L, 2, face_ref(g, x, y, z, b - 8));
+        else push_list(L, 3, tet_ref(g, x, y, z, b - 20));
+    }
+}
+
+// --------------------------------------------------------------- export to the reference layout
+__global__ void k_export(Grid g, FieldState s, int32_t *PV, int32_t *PE, int32_t *PF, int32_t *PT) {
+    i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= g.V) return;
+    int x, y, z;
+    decode_v(g, v, x, y, z);
+    const int d = s.pv[v];
+    PV[v] = d == 15 ? -1 : (int32_t)edge_ref_pair(g, v, v + g.doff[d]);
+    const uint32_t eu = s.eup[v];
+    for (int k = 0; k < 7; k++) {
+        int mx, my, mz;
+        edge_extent(k, mx, my, mz);
+        if (!cell_ok(g, x, y, z, mx, my, mz)) continue;
+        i64 val = -1;
+        const int up = eup_get(eu, k);
+        if (up) {
+            const signed char *cf = TOPO_EDGE_COF[k][up - 1];
+            val = face_ref(g, x + cf[0], y + cf[1], z + cf[2], cf[3]);
+        } else {
+            const int cp = TOPO_EDGE_V[k][0], cq = TOPO_EDGE_V[k][1];
+            const i64 p = v + g.coff[cp], q = v + g.coff[cq];
+            if (s.pv[p] == TOPO_CORNER_DIR[cp][cq]) val = p;
+            else if (s.pv[q] == TOPO_CORNER_DIR[cq][cp]) val = q;
+        }
+        PE[edge_ref(g, x, y, z, k)] = (int32_t)val;
+    }
+    const uint32_t fu = s.fup[v];
+    for (int sl = 0; sl < 12; sl++) {
+        int mx, my, mz;
+        face_extent(sl, mx, my, mz);
+        if (!cell_ok(g, x, y, z, mx, my, mz)) continue;
+        i64 val = -1;
+        const int up = fup_get(fu, sl);
+        if (up) {
+            const signed char *tc = TOPO_FACE_COF[sl][up - 1];
+            val = tet_ref(g, x + tc[0], y + tc[1], z + tc[2], tc[3]);
+        } else {
+            for (int j = 0; j < 3; j++) {
+                const signed char *fe = TOPO_FACE_EDGE[sl][j];
+                const i64 ea = v + fe[0] + (i64)fe[1] * g.W + (i64)fe[2] * g.WH;
+                if (eup_get(s.eup[ea], fe[3]) == fe[4] + 1) val = edge_ref(g, x + fe[0], y + fe[1], z + fe[2], fe[3]);
+            }
+        }
+        PF[face_ref(g, x, y, z, sl)] = (int32_t)val;
+    }
+    if (cell_ok(g, x, y, z, 1, 1, 1)) {
+        for (int ts = 0; ts < 6; ts++) {
+            i64 val = -1;
+            for (int j = 0; j < 4; j++) {
+                const signed char *tf = TOPO_TET_FACE[ts][j];
+                const i64 fa = v + tf[0] + (i64)tf[1] * g.W + (i64)tf[2] * g.WH;
+                if (fup_get(s.fup[fa], tf[3]) == tf[4] + 1) val = face_ref(g, x + tf[0], y + tf[1], z + tf[2], tf[3]);
+            }
+            PT[tet_ref(g, x, y, z, ts)] = (int32_t)val;
+        }
+    }
+}
+
+// --------------------------------------------------------------- fix rules
+struct CpLists {
+    const i64 *l[4];
+    const unsigned long long *n;
+};
+
+// fix_minimum, [fix_saddle, fix_2saddle], fix_maximum over the current lists
+__global__ void k_fix_cp(RuleCtx c, CpLists L, int preserve_saddles) {
+    const i64 n0 = (i64)L.n[0], n1 = preserve_saddles ? (i64)L.n[1] : 0, n2 = preserve_saddles ? (i64)L.n[2] : 0,
+              n3 = (i64)L.n[3];
+    const i64 total = n0 + n1 + n2 + n3;
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (i64)gridDim.x * blockDim.x) {
+        if (i < n0) rule_min(c, L.l[0][i]);
+        else if (i < n0 + n1) rule_saddle(c, L.l[1][i - n0]);
+        else if (i < n0 + n1 + n2) rule_2saddle(c, L.l[2][i - n0 - n1]);
+        else rule_max(c, L.l[3][i - n0 - n1 - n2]);
+    }
+}
+
+// separatrix records
+struct PathRec {
+    i64 *as_tet, *as_cur, *ds_edge, *ds_vert;
+    unsigned long long *n;  // [0] ascending, [1] descending
+};
+
+// get_false_as_vpath (main_3d.cu:4540-4610): per original 2-saddle triangle,
+// the first coface (search order) whose ascending path meets a difference
+__global__ void k_path_as(RuleCtx c, PathRec R, i64 cap) {
+    const Grid &g = c.g;
+    for (i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x; v < g.V; v += (i64)gridDim.x * blockDim.x) {
+        uint32_t m = (c.P.crit[v] >> 8) & 0xFFFu;
+        if (!m) continue;
+        int x, y, z;
+        decode_v(g, v, x, y, z);
+        while (m) {
+            const int sl = __ffs(m) - 1;
+            m &= m - 1;
+            const i64 face = face_ref(g, x, y, z, sl);
+            i64 cof[2];
+            const int nc = face_cofaces(g, face, cof);
+            for (int j = 0; j < nc; j++) {
+                i64 rec;
+                if (walk_ascending(c, cof[j], rec, cap)) {
+                    const unsigned long long at = atomicAdd(&R.n[0], 1ull);
+                    R.as_tet[at] = cof[j];
+                    R.as_cur[at] = rec;
+                    break;
+                }
+            }
+        }
+    }
+}
+
+// get_false_ds_vpath (main_3d.cu:4837-4959): the reference's walk never
+// advances past the first vertex (dec_current_id stays at the start), so each
+// endpoint's steepest-descent pairing is compared once, v1 (higher id) first.
+__global__ void k_path_ds(RuleCtx c, PathRec R) {
+    const Grid &g = c.g;
+    for (i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x; v < g.V; v += (i64)gridDim.x * blockDim.x) {
+        uint32_t m = (c.P.crit[v] >> 1) & 0x7Fu;
+        if (!m) continue;
+        int x, y, z;
+        decode_v(g, v, x, y, z);
+        while (m) {
+            const int k = __ffs(m) - 1;
+            m &= m - 1;
+            const i64 ends[2] = {v + g.coff[TOPO_EDGE_V[k][0]], v + g.coff[TOPO_EDGE_V[k][1]]};
+            for (int j = 0; j < 2; j++) {
+                const i64 e = ends[j];
+                const int po = c.P.pv[e];
+                if (po == 15) continue;
+                if (po != c.Q.pv[e]) {
+                    const unsigned long long at = atomicAdd(&R.n[1], 1ull);
+                    R.ds_edge[at] = edge_ref(g, x, y, z, k);
+                    R.ds_vert[at] = e;
+                    break;
+                }
+            }
+        }
+    }
+}
+
+__global__ void k_fix_path(RuleCtx c, PathRec R) {
+    const i64 na = (i64)R.n[0], nd = (i64)R.n[1];
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < na + nd; i += (i64)gridDim.x * blockDim.x) {
+        if (i < na) rule_as_path(c, R.as_cur[i]);
+        else rule_ds_path(c, R.ds_vert[i - na]);
+    }
+}
+
+// --------------------------------------------------------------- value update
+// applyDeltaBuffer1 (main_3d.cu:1122-1164) on the requested vertices only.
+// The delta is what the reference's buffer holds: get_delta(v), with the
+// buffer's "no request" sentinel -2000*range (a request whose delta is not
+// above the sentinel leaves the buffer unchanged under edit_type 0).
+__global__ void k_apply(RuleCtx c, double range, int preserve_type, int update, uint8_t *changed, double *delta_out) {
+    const i64 n = (i64)*c.reqn;
+    const double sentinel = -2000.0 * range;
+    const double tiny = 1e-15 * range;
+    double *g = const_cast<double *>(c.gv);
+    int *cnt = const_cast<int *>(c.cnt);
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n && i < c.reqcap; i += (i64)gridDim.x * blockDim.x) {
+        const i64 v = c.reqlist[i];
+        c.reqbits[v >> 5] = 0;  // every bit of this word belongs to listed vertices
+        const double d = get_delta(c, v);
+        const bool req = c.edit_type == 0 ? (d > sentinel) : (d != sentinel);
+        if (delta_out) delta_out[v] = req ? d : sentinel;
+        if (!req || !update) continue;
+        const double f = c.f[v];
+        const double gv = g[v];
+        const double lowb = __dsub_rn(f, c.bound);
+        if (preserve_type == 0 && fabs(d) > tiny && cnt[v] < 5 && fabs(__dsub_rn(f, __dadd_rn(gv, d))) <= c.bound) {
+            g[v] = __dadd_rn(gv, d);
+            cnt[v] += 1;
+        } else {
+            cnt[v] = 6;
+            g[v] = lowb;
+        }
+        if (changed) changed[v] = 1;
+    }
+}
+
+// filter_vertices / _edges / _faces / _tetrahedras (main_3d.cu:2405-2490):
+// every vertex of every original critical cell goes to f - bound
+__global__ void k_filter(Grid g, const uint32_t *crit_o, const double *f, double *gv, double bound) {
+    i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= g.V) return;
+    uint32_t m = crit_o[v];
+    if (!m) return;
+    int x, y, z;
+    decode_v(g, v, x, y, z);
+    uint32_t corners = 0;
+    if (m & 1u) corners |= 1u;
+    for (int k = 0; k < 7; k++)
+        if (m & (1u << (1 + k))) corners |= (1u << TOPO_EDGE_V[k][0]) | (1u << TOPO_EDGE_V[k][1]);
+    for (int s = 0; s < 12; s++)
+        if (m & (1u << (8 + s)))
+            corners |= (1u << TOPO_FACE_V[s][0]) | (1u << TOPO_FACE_V[s][1]) | (1u << TOPO_FACE_V[s][2]);
+    for (int s = 0; s < 6; s++)
+        if (m & (1u << (20 + s)))
+            corners |= (1u << TOPO_TET_V[s][0]) | (1u << TOPO_TET_V[s][1]) | (1u << TOPO_TET_V[s][2]) |
+                       (1u << TOPO_TET_V[s][3]);
+    while (corners) {
+        const int c8 = __ffs(corners) - 1;
+        corners &= corners - 1;
+        const i64 u = v + g.coff[c8];
+        gv[u] = __dsub_rn(f[u], bound);  // same value from every writer
+    }
+}
+
+__global__ void k_fill_i32(int *p, int val, i64 n) {
+    i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = val;
+}
+__global__ void k_check_finite(const double *a, i64 n, int *bad) {
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x)
+        if (!isfinite(a[i])) atomicOr(bad, 1);
+}
+
+}  // namespace dmtz
+
+// =============================================================================
+// host side
+// =============================================================================
+struct DevField {
+    uint64_t *key = nullptr;
+    uint16_t *low = nullptr;
+    uint8_t *pv = nullptr;
+    uint32_t *ea2 = nullptr;
+    uint16_t *fp3 = nullptr;
+    uint32_t *fa3 = nullptr;
+    uint32_t *eup = nullptr;
+    uint32_t *fup = nullptr;
+    uint32_t *crit = nullptr;
+};
+
+struct dmtz_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    // sized buffers
+    i64 capV = 0, capE = 0, capF = 0, capT = 0;
+    double *f = nullptr, *g = nullptr;
+    DevField P, Q;
+    int *cnt = nullptr;
+    uint32_t *reqbits = nullptr;
+    i64 *reqlist = nullptr;
+    i64 *lists[4] = {nullptr, nullptr, nullptr, nullptr};
+    i64 *as_tet = nullptr, *as_cur = nullptr, *ds_edge = nullptr, *ds_vert = nullptr;
+    unsigned long long *counters = nullptr;  // [0..3] cp lists, [4] requests, [5,6] paths
+    int *errword = nullptr;
+    uint8_t *changed = nullptr;
+    void *scratch = nullptr;
+    size_t scratch_bytes = 0;
+};
+
+namespace {
+
+dmtz_status fail(dmtz_ctx *c, dmtz_status s, const std::string &m) {
+    if (c) c->err = m;
+    return s;
+}
+#define CK(call)                                                                                   \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess) return fail(ctx, DMTZ_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+template <class T>
+cudaError_t dalloc(T **p, i64 n) {
+    return cudaMalloc((void **)p, sizeof(T) * (size_t)std::max<i64>(n, 1));
+}
+
+void free_field(DevField &d) {
+    cudaFree(d.key); cudaFree(d.low); cudaFree(d.pv); cudaFree(d.ea2); cudaFree(d.fp3);
+    cudaFree(d.fa3); cudaFree(d.eup); cudaFree(d.fup); cudaFree(d.crit);
+    d = DevField();
+}
+void free_all(dmtz_ctx *c) {
+    cudaFree(c->f); cudaFree(c->g); free_field(c->P); free_field(c->Q);
+    cudaFree(c->cnt); cudaFree(c->reqbits); cudaFree(c->reqlist);
+    for (auto &l : c->lists) { cudaFree(l); l = nullptr; }
+    cudaFree(c->as_tet); cudaFree(c->as_cur); cudaFree(c->ds_edge); cudaFree(c->ds_vert);
+    cudaFree(c->counters); cudaFree(c->errword); cudaFree(c->changed);
+    c->f = c->g = nullptr; c->cnt = nullptr; c->reqbits = nullptr; c->reqlist = nullptr;
+    c->as_tet = c->as_cur = c->ds_edge = c->ds_vert = nullptr; c->counters = nullptr;
+    c->errword = nullptr; c->changed = nullptr;
+    c->capV = c->capE = c->capF = c->capT = 0;
+}
+
+dmtz_status alloc_field(dmtz_ctx *ctx, DevField &d, i64 V) {
+    CK(dalloc(&d.key, V)); CK(dalloc(&d.low, V)); CK(dalloc(&d.pv, V)); CK(dalloc(&d.ea2, V));
+    CK(dalloc(&d.fp3, V)); CK(dalloc(&d.fa3, V)); CK(dalloc(&d.eup, V)); CK(dalloc(&d.fup, V));
+    CK(dalloc(&d.crit, V));
+    return DMTZ_OK;
+}
+
+dmtz_status ensure(dmtz_ctx *ctx, const Grid &g) {
+    if (g.V <= ctx->capV && g.E <= ctx->capE && g.F <= ctx->capF && g.T <= ctx->capT) return DMTZ_OK;
+    free_all(ctx);
+    const i64 V = g.V;
+    CK(dalloc(&ctx->f, V)); CK(dalloc(&ctx->g, V));
+    dmtz_status s;
+    if ((s = alloc_field(ctx, ctx->P, V)) != DMTZ_OK) return s;
+    if ((s = alloc_field(ctx, ctx->Q, V)) != DMTZ_OK) return s;
+    CK(dalloc(&ctx->cnt, V));
+    CK(dalloc(&ctx->reqbits, (V + 31) / 32 + 1));
+    CK(cudaMemset(ctx->reqbits, 0, sizeof(uint32_t) * (size_t)((V + 31) / 32 + 1)));
+    CK(dalloc(&ctx->reqlist, V));
+    CK(dalloc(&ctx->lists[0], g.V)); CK(dalloc(&ctx->lists[1], g.E));
+    CK(dalloc(&ctx->lists[2], g.F)); CK(dalloc(&ctx->lists[3], g.T));
+    CK(dalloc(&ctx->as_tet, g.F)); CK(dalloc(&ctx->as_cur, g.F));
+    CK(dalloc(&ctx->ds_edge, g.E)); CK(dalloc(&ctx->ds_vert, g.E));
+    CK(dalloc(&ctx->counters, 8)); CK(dalloc(&ctx->errword, 1)); CK(dalloc(&ctx->changed, V));
+    ctx->capV = g.V; ctx->capE = g.E; ctx->capF = g.F; ctx->capT = g.T;
+    return DMTZ_OK;
+}
+
+FieldState view(const DevField &d, const double *val) {
+    FieldState s;
+    s.val = val; s.key = d.key; s.low = d.low; s.pv = d.pv; s.ea2 = d.ea2; s.fp3 = d.fp3;
+    s.fa3 = d.fa3; s.eup = d.eup; s.fup = d.fup; s.crit = d.crit;
+    return s;
+}
+
+// five passes + criticality (and mismatch lists when crit_o is given)
+void run_pairing(dmtz_ctx *ctx, const Grid &g, const FieldState &s, const uint32_t *crit_o, int want_saddles) {
+    const unsigned gr = grid_for(g.V);
+    cudaStream_t st = ctx->stream;
+    k_pass_vertex<<<gr, kBlock, 0, st>>>(g, s, 0, g.V);
+    k_pass_edge_a2<<<gr, kBlock, 0, st>>>(g, s, 0, g.V);
+    k_pass_face_a3<<<gr, kBlock, 0, st>>>(g, s, 0, g.V);
+    k_pass_edge_a4<<<gr, kBlock, 0, st>>>(g, s, 0, g.V);
+    k_pass_face_a5<<<gr, kBlock, 0, st>>>(g, s, 0, g.V);
+    Lists L;
+    for (int k = 0; k < 4; k++) L.l[k] = ctx->lists[k];
+    L.n = ctx->counters;
+    if (crit_o) cudaMemsetAsync(ctx->counters, 0, 4 * sizeof(unsigned long long), st);
+    k_crit<<<gr, kBlock, 0, st>>>(g, s, crit_o, L, want_saddles, 0, g.V);
+}
+
+RuleCtx rule_ctx(dmtz_ctx *ctx, const Grid &g, double bound, int edit_type) {
+    RuleCtx c;
+    c.g = g;
+    c.P = view(ctx->P, ctx->f);
+    c.Q = view(ctx->Q, ctx->g);
+    c.f = ctx->f;
+    c.gv = ctx->g;
+    c.cnt = ctx->cnt;
+    c.bound = bound;
+    c.edit_type = edit_type;
+    c.reqbits = ctx->reqbits;
+    c.reqlist = ctx->reqlist;
+    c.reqn = ctx->counters + 4;
+    c.reqcap = g.V;
+    c.err = ctx->errword;
+    return c;
+}
+
+unsigned persistent_grid() {
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return (unsigned)sms * 8;
+}
+
+dmtz_status check_dims(dmtz_ctx *ctx, int W, int H, int D, Grid &g) {
+    if (!ctx) return DMTZ_ERR_ARG;
+    if (W < 2 || H < 2 || D < 2) return fail(ctx, DMTZ_ERR_ARG, "dims must be >= 2");
+    g = make_grid(W, H, D);
+    return DMTZ_OK;
+}
+
+dmtz_status upload(dmtz_ctx *ctx, double *dst, const double *src, i64 n, int on_device) {
+    CK(cudaMemcpyAsync(dst, src, sizeof(double) * (size_t)n, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaMemsetAsync(ctx->errword, 0, sizeof(int), ctx->stream));
+    k_check_finite<<<persistent_grid(), kBlock, 0, ctx->stream>>>(dst, n, ctx->errword);
+    int bad = 0;
+    CK(cudaMemcpyAsync(&bad, ctx->errword, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (bad) return fail(ctx, DMTZ_ERR_ARG, "input contains NaN or Inf");
+    return DMTZ_OK;
+}
+
+}  // namespace
+
+// =============================================================================
+// C ABI
+// =============================================================================
+extern "C" {
+
+dmtz_status dmtz_ctx_create(dmtz_ctx **out, int device) {
+    if (!out) return DMTZ_ERR_ARG;
+    *out = nullptr;
+    dmtz_ctx *ctx = new dmtz_ctx();
+    ctx->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete ctx;
+        return DMTZ_ERR_CUDA;
+    }
+    *out = ctx;
+    return DMTZ_OK;
+}
+
+void dmtz_ctx_destroy(dmtz_ctx *ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    free_all(ctx);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char *dmtz_last_error(const dmtz_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+dmtz_status dmtz_cell_counts(int W, int H, int D, int64_t out[4]) {
+    if (W < 2 || H < 2 || D < 2 || !out) return DMTZ_ERR_ARG;
+    Grid g = make_grid(W, H, D);
+    out[0] = g.V; out[1] = g.E; out[2] = g.F; out[3] = g.T;
+    return DMTZ_OK;
+}
+
+dmtz_status dmtz_extract(dmtz_ctx *ctx, int W, int H, int D, const double *data, int on_device, int32_t *PV,
+                         int32_t *PE, int32_t *PF, int32_t *PT) {
+    Grid g;
+    dmtz_status s = check_dims(ctx, W, H, D, g);
+    if (s != DMTZ_OK) return s;
+    if (g.F >= INT32_MAX) return fail(ctx, DMTZ_ERR_ARG, "grid too large for 32-bit reference ids");
+    CK(cudaSetDevice(ctx->device));
+    if ((s = ensure(ctx, g)) != DMTZ_OK) return s;
+    if ((s = upload(ctx, ctx->f, data, g.V, on_device)) != DMTZ_OK) return s;
+    FieldState fs = view(ctx->P, ctx->f);
+    run_pairing(ctx, g, fs, nullptr, 1);
+    int32_t *d[4];
+    const i64 n[4] = {g.V, g.E, g.F, g.T};
+    for (int k = 0; k < 4; k++) CK(dalloc(&d[k], n[k]));
+    k_export<<<grid_for(g.V), kBlock, 0, ctx->stream>>>(g, fs, d[0], d[1], d[2], d[3]);
+    int32_t *h[4] = {PV, PE, PF, PT};
+    for (int k = 0; k < 4; k++)
+        CK(cudaMemcpyAsync(h[k], d[k], sizeof(int32_t) * (size_t)n[k], cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (int k = 0; k < 4; k++) cudaFree(d[k]);
+    CK(cudaGetLastError());
+    return DMTZ_OK;
+}
+
+// shared set-up of the two complexes for the parity entry points
+static dmtz_status setup_pair(dmtz_ctx *ctx, const Grid &g, const double *orig, const double *decp) {
+    dmtz_status s;
+    if ((s = ensure(ctx, g)) != DMTZ_OK) return s;
+    if ((s = upload(ctx, ctx->f, orig, g.V, 0)) != DMTZ_OK) return s;
+    if ((s = upload(ctx, ctx->g, decp, g.V, 0)) != DMTZ_OK) return s;
+    run_pairing(ctx, g, view(ctx->P, ctx->f), nullptr, 1);
+    run_pairing(ctx, g, view(ctx->Q, ctx->g), ctx->P.crit, 1);
+    CK(cudaGetLastError());
+    return DMTZ_OK;
+}
+
+dmtz_status dmtz_mismatch(dmtz_ctx *ctx, int W, int H, int D, const double *orig, const double *decp,
+                          int64_t counts[4], int32_t *lmin, int32_t *lsad, int32_t *l2sad, int32_t *lmax) {
+    Grid g;
+    dmtz_status s = check_dims(ctx, W, H, D, g);
+    if (s != DMTZ_OK) return s;
+    CK(cudaSetDevice(ctx->device));
+    if ((s = setup_pair(ctx, g, orig, decp)) != DMTZ_OK) return s;
+    unsigned long long hc[4];
+    CK(cudaMemcpyAsync(hc, ctx->counters, sizeof(hc), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    int32_t *outs[4] = {lmin, lsad, l2sad, lmax};
+    for (int k = 0; k < 4; k++) {
+        counts[k] = (int64_t)hc[k];
+        if (!outs[k] || !hc[k]) continue;
+        std::vector<i64> tmp(hc[k]);
+        CK(cudaMemcpy(tmp.data(), ctx->lists[k], sizeof(i64) * hc[k], cudaMemcpyDeviceToHost));
+        std::sort(tmp.begin(), tmp.end());
+        for (size_t i = 0; i < tmp.size(); i++) outs[k][i] = (int32_t)tmp[i];
+    }
+    return DMTZ_OK;
+}
+
+static void host_minmax(const double *f, i64 n, double &mn, double &mx) {
+    mn = f[0]; mx = f[0];
+    for (i64 i = 1; i < n; i++) {
+        if (f[i] < mn) mn = f[i];
+        if (f[i] > mx) mx = f[i];
+    }
+}
+
+dmtz_status dmtz_fix_round(dmtz_ctx *ctx, int W, int H, int D, const double *orig, const double *decp,
+                           const int32_t *edit_counter, double rel_eps, int preserve_saddles, int edit_type,
+                           double *delta_out) {
+    Grid g;
+    dmtz_status s = check_dims(ctx, W, H, D, g);
+    if (s != DMTZ_OK) return s;
+    CK(cudaSetDevice(ctx->device));
+    if ((s = setup_pair(ctx, g, orig, decp)) != DMTZ_OK) return s;
+    double mn, mx;
+    host_minmax(orig, g.V, mn, mx);
+    const double range = mx - mn, bound = (mx - mn) * rel_eps;
+    CK(cudaMemcpyAsync(ctx->cnt, edit_counter, sizeof(int) * (size_t)g.V, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemsetAsync(ctx->counters + 4, 0, sizeof(unsigned long long), ctx->stream));
+    CK(cudaMemsetAsync(ctx->errword, 0, sizeof(int), ctx->stream));
+    RuleCtx rc = rule_ctx(ctx, g, bound, edit_type);
+    CpLists L;
+    for (int k = 0; k < 4; k++) L.l[k] = ctx->lists[k];
+    L.n = ctx->counters;
+    k_fix_cp<<<persistent_grid(), kBlock, 0, ctx->stream>>>(rc, L, preserve_saddles);
+    double *dd = nullptr;
+    CK(dalloc(&dd, g.V));
+    const double sentinel = -2000.0 * range;
+    std::vector<double> fill((size_t)g.V, sentinel);
+    CK(cudaMemcpyAsync(dd, fill.data(), sizeof(double) * (size_t)g.V, cudaMemcpyHostToDevice, ctx->stream));
+    // report the deltas the rules requested, without updating the field
+    k_apply<<<persistent_grid(), kBlock, 0, ctx->stream>>>(rc, range, 0, 0, nullptr, dd);
+    CK(cudaMemcpyAsync(delta_out, dd, sizeof(double) * (size_t)g.V, cudaMemcpyDeviceToHost, ctx->stream));
+    int err = 0;
+    CK(cudaMemcpyAsync(&err, ctx->errword, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    cudaFree(dd);
+    CK(cudaGetLastError());
+    if (err & ERR_OOB) return fail(ctx, DMTZ_ERR_OOB, "a fix rule indexed out of range");
+    return DMTZ_OK;
+}
+
+dmtz_status dmtz_path_detect(dmtz_ctx *ctx, int W, int H, int D, const double *orig, const double *decp,
+                             int64_t counts[2], int32_t *as_tet, int32_t *as_cur, int32_t *ds_edge,
+                             int32_t *ds_vert) {
+    Grid g;
+    dmtz_status s = check_dims(ctx, W, H, D, g);
+    if (s != DMTZ_OK) return s;
+    CK(cudaSetDevice(ctx->device));
+    if ((s = setup_pair(ctx, g, orig, decp)) != DMTZ_OK) return s;
+    CK(cudaMemsetAsync(ctx->counters + 5, 0, 2 * sizeof(unsigned long long), ctx->stream));
+    CK(cudaMemsetAsync(ctx->errword, 0, sizeof(int), ctx->stream));
+    RuleCtx rc = rule_ctx(ctx, g, 0.0, 0);
+    PathRec R{ctx->as_tet, ctx->as_cur, ctx->ds_edge, ctx->ds_vert, ctx->counters + 5};
+    k_path_as<<<persistent_grid(), kBlock, 0, ctx->stream>>>(rc, R, g.T + 16);
+    k_path_ds<<<persistent_grid(), kBlock, 0, ctx->stream>>>(rc, R);
+    unsigned long long hc[2];
+    CK(cudaMemcpyAsync(hc, ctx->counters + 5, sizeof(hc), cudaMemcpyDeviceToHost, ctx->stream));
+    int err = 0;
+    CK(cudaMemcpyAsync(&err, ctx->errword, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    counts[0] = (int64_t)hc[0];
+    counts[1] = (int64_t)hc[1];
+    auto fetch = [&](i64 *da, i64 *db, unsigned long long n, int32_t *oa, int32_t *ob) -> dmtz_status {
+        if (!n || !oa) return DMTZ_OK;
+        std::vector<i64> a(n), b(n);
+        CK(cudaMemcpy(a.data(), da, sizeof(i64) * n, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(b.data(), db, sizeof(i64) * n, cudaMemcpyDeviceToHost));
+        std::vector<std::pair<i64, i64>> p(n);
+        for (size_t i = 0; i < n; i++) p[i] = {a[i], b[i]};
+        std::sort(p.begin(), p.end());
+        for (size_t i = 0; i < n; i++) {
+            oa[i] = (int32_t)p[i].first;
+            if (ob) ob[i] = (int32_t)p[i].second;
+        }
+        return DMTZ_OK;
+    };
+    if ((s = fetch(ctx->as_tet, ctx->as_cur, hc[0], as_tet, as_cur)) != DMTZ_OK) return s;
+    if ((s = fetch(ctx->ds_edge, ctx->ds_vert, hc[1], ds_edge, ds_vert)) != DMTZ_OK) return s;
+    if (err & ERR_WALK) return fail(ctx, DMTZ_ERR_CYCLE, "ascending path walk exceeded its step cap");
+    if (err & ERR_OOB) return fail(ctx, DMTZ_ERR_OOB, "a path rule indexed out of range");
+    return DMTZ_OK;
+}
+
+// ----------------------------------------------------------------------------- the correction loop
+dmtz_status dmtz_correct(dmtz_ctx *ctx, int W, int H, int D, const double *orig, double *decp, int on_device,
+                         double rel_eps, const dmtz_opts *opts, dmtz_report *rep, int32_t *edit_counter_out) {
+    Grid g;
+    dmtz_status s = check_dims(ctx, W, H, D, g);
+    if (s != DMTZ_OK) return s;
+    if (!opts) return fail(ctx, DMTZ_ERR_ARG, "null options");
+    const int ps = opts->preserve_saddles, pvp = opts->preserve_vpath, pg = opts->preserve_geometry,
+              filt = opts->filtration, pc = opts->preserve_connectors, pt = opts->preserve_type,
+              et = opts->edit_type;
+    if (pc == 1) return fail(ctx, DMTZ_ERR_UNSUPPORTED, "preserve_connectors=1 is not supported");
+    if (pvp == 1 && pg == 0) return fail(ctx, DMTZ_ERR_UNSUPPORTED, "connectivity-mode separatrices are not supported");
+    if (!(rel_eps >= 0.0) || !std::isfinite(rel_eps)) return fail(ctx, DMTZ_ERR_ARG, "rel_eps must be finite and >= 0");
+    const i64 max_rounds = opts->max_rounds > 0 ? opts->max_rounds : 100000;
+    CK(cudaSetDevice(ctx->device));
+    if ((s = ensure(ctx, g)) != DMTZ_OK) return s;
+    cudaStream_t st = ctx->stream;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    if ((s = upload(ctx, ctx->f, orig, g.V, on_device)) != DMTZ_OK) return s;
+    if ((s = upload(ctx, ctx->g, decp, g.V, on_device)) != DMTZ_OK) return s;
+    // range and bound exactly as the reference computes them (main_3d.cu:6303-6323)
+    double mn, mx;
+    if (on_device) {
+        std::vector<double> hf((size_t)g.V);
+        CK(cudaMemcpy(hf.data(), orig, sizeof(double) * (size_t)g.V, cudaMemcpyDeviceToHost));
+        host_minmax(hf.data(), g.V, mn, mx);
+    } else {
+        host_minmax(orig, g.V, mn, mx);
+    }
+    const double bound = (mx - mn) * rel_eps;
+    const double range = mx - mn;
+    CK(cudaEventRecord(e0, st));
+    CK(cudaMemsetAsync(ctx->errword, 0, sizeof(int), st));
+    CK(cudaMemsetAsync(ctx->changed, 0, (size_t)g.V, st));
+    CK(cudaMemsetAsync(ctx->counters, 0, 8 * sizeof(unsigned long long), st));
+    const FieldState Ps = view(ctx->P, ctx->f), Qs = view(ctx->Q, ctx->g);
+    run_pairing(ctx, g, Ps, nullptr, 1);
+    if (filt == 1) k_filter<<<grid_for(g.V), kBlock, 0, st>>>(g, ctx->P.crit, ctx->f, ctx->g, bound);
+    run_pairing(ctx, g, Qs, ctx->P.crit, 1);
+    k_fill_i32<<<grid_for(g.V), kBlock, 0, st>>>(ctx->cnt, 1, g.V);
+    unsigned long long hc[8];
+    auto read_counts = [&]() -> dmtz_status {
+        CK(cudaMemcpyAsync(hc, ctx->counters, sizeof(hc), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        return DMTZ_OK;
+    };
+    if ((s = read_counts()) != DMTZ_OK) return s;
+    dmtz_report R;
+    memset(&R, 0, sizeof(R));
+    for (int k = 0; k < 4; k++) R.initial_mismatch[k] = (int64_t)hc[k];
+    i64 cc[4] = {(i64)hc[0], (i64)hc[1], (i64)hc[2], (i64)hc[3]};
+    i64 n_as = 1, n_ds = 1, n_wall = 1;
+    i64 rounds = 0;
+    int converged = 1;
+    const unsigned pgrid = persistent_grid();
+    RuleCtx rc = rule_ctx(ctx, g, bound, et);
+    CpLists L;
+    for (int k = 0; k < 4; k++) L.l[k] = ctx->lists[k];
+    L.n = ctx->counters;
+    PathRec PR{ctx->as_tet, ctx->as_cur, ctx->ds_edge, ctx->ds_vert, ctx->counters + 5};
+    auto cp_any = [&]() { return cc[0] > 0 || cc[1] > 0 || cc[2] > 0 || cc[3] > 0; };
+    while (n_as > 0 || n_ds > 0 || n_wall > 0 || cp_any()) {
+        if (rounds >= max_rounds) {
+            converged = 0;
+            break;
+        }
+        R.outer_iterations++;
+        while (cp_any()) {
+            if (rounds >= max_rounds) break;
+            rounds++;
+            R.cp_rounds++;
+            CK(cudaMemsetAsync(ctx->counters + 4, 0, sizeof(unsigned long long), st));
+            k_fix_cp<<<pgrid, kBlock, 0, st>>>(rc, L, ps);
+            k_apply<<<pgrid, kBlock, 0, st>>>(rc, range, pt, 1, ctx->changed, nullptr);
+            run_pairing(ctx, g, Qs, ctx->P.crit, ps == 1);
+            if ((s = read_counts()) != DMTZ_OK) return s;
+            for (int k = 0; k < 4; k++) cc[k] = (i64)hc[k];
+        }
+        if (rounds >= max_rounds) {
+            converged = 0;
+            break;
+        }
+        if (pvp == 0) break;
+        // separatrix phase (main_3d.cu:6943-7148)
+        rounds++;
+        R.path_rounds++;
+        CK(cudaMemsetAsync(ctx->counters + 5, 0, 2 * sizeof(unsigned long long), st));
+        k_path_as<<<pgrid, kBlock, 0, st>>>(rc, PR, g.T + 16);
+        k_path_ds<<<pgrid, kBlock, 0, st>>>(rc, PR);
+        CK(cudaMemsetAsync(ctx->counters + 4, 0, sizeof(unsigned long long), st));
+        k_fix_path<<<pgrid, kBlock, 0, st>>>(rc, PR);
+        k_apply<<<pgrid, kBlock, 0, st>>>(rc, range, pt, 1, ctx->changed, nullptr);
+        run_pairing(ctx, g, Qs, ctx->P.crit, 1);
+        if ((s = read_counts()) != DMTZ_OK) return s;
+        for (int k = 0; k < 4; k++) cc[k] = (i64)hc[k];
+        n_as = n_ds = n_wall = 0;
+        if (!cp_any()) {
+            CK(cudaMemsetAsync(ctx->counters + 5, 0, 2 * sizeof(unsigned long long), st));
+            k_path_as<<<pgrid, kBlock, 0, st>>>(rc, PR, g.T + 16);
+            k_path_ds<<<pgrid, kBlock, 0, st>>>(rc, PR);
+            if ((s = read_counts()) != DMTZ_OK) return s;
+            n_as = (i64)hc[5];
+            n_ds = (i64)hc[6];
+        }
+    }
+    CK(cudaEventRecord(e1, st));
+    CK(cudaMemcpyAsync(decp, ctx->g, sizeof(double) * (size_t)g.V,
+                       on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+    if (edit_counter_out)
+        CK(cudaMemcpyAsync(edit_counter_out, ctx->cnt, sizeof(int) * (size_t)g.V, cudaMemcpyDeviceToHost, st));
+    int err = 0;
+    CK(cudaMemcpyAsync(&err, ctx->errword, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    CK(cudaGetLastError());
+    for (int k = 0; k < 4; k++) R.final_mismatch[k] = cc[k];
+    R.final_paths[0] = n_as;
+    R.final_paths[1] = n_ds;
+    R.converged = converged;
+    R.error_flags = err;
+    R.seconds = ms * 1e-3;
+    if (rep) *rep = R;
+    if (err & ERR_OOB) return fail(ctx, DMTZ_ERR_OOB, "a fix rule indexed out of range");
+    if (err & ERR_WALK) return fail(ctx, DMTZ_ERR_CYCLE, "ascending path walk exceeded its step cap");
+    if (!converged) return fail(ctx, DMTZ_ERR_NONCONVERGED, "round cap reached before the complexes agree");
+    return DMTZ_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,99 @@
+"""Seeded synthetic scalar fields and decompression-error models.
+
+The reference ships no data and names no public dataset, so every workload is
+generated here from a seed:
+
+* ``gaussian_mix``: a sum of isotropic Gaussians with uniform centres, widths
+  and amplitudes plus white noise (the 64^3 extrema-only workload).
+* ``power_law``: a Gaussian random field with spectrum P(k) ~ k^-3, normalised
+  to [0, 1] (the 256^3 full-MSC workload).
+* ``decompress_uniform``: original + U[-eps, eps] (an error-bounded lossy
+  compressor's error model).
+* ``decompress_sz``: SZ-style pre-quantisation with bin 2*eps, 5 % of voxels
+  with extra U[-eps, eps] noise, clamped to [f - eps, f + eps].
+
+Arrays are shaped (D, H, W) in C order, so the flat index is x + y*W + z*W*H,
+the vertex numbering of the reference.  Original fields are float32 values
+widened to float64 (the reference reads float64 only); decompressed fields are
+float64.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def _rng(seed: int) -> np.random.Generator:
+    return np.random.Generator(np.random.PCG64(seed))
+
+
+def gaussian_mix(dims, seed: int, n_gauss: int = 32, sigma=(2.0, 8.0), noise: float = 1e-3) -> np.ndarray:
+    """Sum of n_gauss isotropic Gaussians + N(0, noise) as float32 widened to float64."""
+    W, H, D = dims
+    r = _rng(seed)
+    c = r.uniform(0.0, 1.0, size=(n_gauss, 3)) * np.array([W, H, D], np.float64)
+    s = r.uniform(sigma[0], sigma[1], size=n_gauss)
+    a = r.uniform(-1.0, 1.0, size=n_gauss)
+    z, y, x = np.meshgrid(np.arange(D, dtype=np.float64), np.arange(H, dtype=np.float64),
+                          np.arange(W, dtype=np.float64), indexing="ij")
+    f = np.zeros((D, H, W), np.float64)
+    for k in range(n_gauss):
+        d2 = (x - c[k, 0]) ** 2 + (y - c[k, 1]) ** 2 + (z - c[k, 2]) ** 2
+        f += a[k] * np.exp(-d2 / (2.0 * s[k] ** 2))
+    f += r.normal(0.0, noise, size=f.shape)
+    return f.astype(np.float32).astype(np.float64)
+
+
+def power_law(dims, seed: int, slope: float = -3.0) -> np.ndarray:
+    """Gaussian random field with P(k) ~ k^slope, min-max normalised to [0, 1]."""
+    W, H, D = dims
+    r = _rng(seed)
+    white = r.standard_normal((D, H, W))
+    spec = np.fft.rfftn(white)
+    kz = np.fft.fftfreq(D)[:, None, None]
+    ky = np.fft.fftfreq(H)[None, :, None]
+    kx = np.fft.rfftfreq(W)[None, None, :]
+    k = np.sqrt(kx * kx + ky * ky + kz * kz)
+    amp = np.zeros_like(k)
+    nz = k > 0
+    amp[nz] = k[nz] ** (slope / 2.0)
+    f = np.fft.irfftn(spec * amp, s=(D, H, W), axes=(0, 1, 2))
+    f = (f - f.min()) / (f.max() - f.min())
+    return f.astype(np.float32).astype(np.float64)
+
+
+def value_range(f: np.ndarray) -> float:
+    return float(f.max() - f.min())
+
+
+def decompress_uniform(f: np.ndarray, eps: float, seed: int) -> np.ndarray:
+    """g = f + U[-eps, eps] (float64)."""
+    r = _rng(seed + 7919)
+    return f + r.uniform(-eps, eps, size=f.shape)
+
+
+def decompress_sz(f: np.ndarray, eps: float, seed: int, frac: float = 0.05) -> np.ndarray:
+    """SZ-style pre-quantisation (bin 2 eps) + frac of voxels with U[-eps, eps], clamped to f +- eps."""
+    r = _rng(seed + 104729)
+    fmin = float(f.min())
+    g = fmin + 2.0 * eps * np.round((f - fmin) / (2.0 * eps))
+    sel = r.random(f.shape) < frac
+    g = g + sel * r.uniform(-eps, eps, size=f.shape)
+    return np.clip(g, f - eps, f + eps)
+
+
+def make_case(kind: str, dims, seed: int, rel_eps: float, decomp: str = "uniform", **kw):
+    """Return (f, g) float64 arrays of shape (D, H, W) for a named field kind."""
+    if kind == "gauss":
+        f = gaussian_mix(dims, seed, **kw)
+    elif kind == "powerlaw":
+        f = power_law(dims, seed, **kw)
+    else:
+        raise ValueError(kind)
+    eps = rel_eps * value_range(f)
+    if decomp == "uniform":
+        g = decompress_uniform(f, eps, seed)
+    elif decomp == "sz":
+        g = decompress_sz(f, eps, seed)
+    else:
+        raise ValueError(decomp)
+    return f, g

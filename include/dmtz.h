@@ -1,0 +1,129 @@
+/*
+ * dmtz.h — C ABI of libdmtz, the GB300 (sm_103a) implementation of DMTz's
+ * topology-correction path for lossy-compressed 3-D scalar fields.
+ *
+ * The reference (main_3d.cu) has no library interface: its boundary is the
+ * process (argv + files, main_3d.cu:6255-6393) and a set of device-global
+ * kernels driven by a host loop.  Each entry point below replaces one stage
+ * of that program; the comment on each names the reference code it stands
+ * in for.  Plain pointers and sizes only; no CUDA or torch types.
+ *
+ * Conventions
+ *   - Fields are float64, x fastest: value of vertex (x,y,z) at x + y*W + z*W*H
+ *     (main_3d.cu:1945-1947).  W, H, D >= 2.
+ *   - Pairing arrays use the reference's cell numbering (getEdgeID,
+ *     getTriangleID, getTetrahedraID) and its union encoding: -1 = unpaired,
+ *     otherwise the id of the partner cell of the next lower or higher
+ *     dimension.  Cell counts: dmtz_cell_counts().
+ *   - Pointers are host pointers unless on_device != 0, in which case they are
+ *     device pointers on the context's device.
+ *   - Every call returns a dmtz_status; dmtz_last_error() gives a message.
+ *     The library never exits the process.  One context per host thread.
+ */
+#ifndef DMTZ_H
+#define DMTZ_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    DMTZ_OK = 0,
+    DMTZ_ERR_CUDA = 1,          /* a CUDA runtime call failed */
+    DMTZ_ERR_ARG = 2,           /* invalid argument (dims, NaN/Inf input, bad flags) */
+    DMTZ_ERR_IO = 3,            /* file read/write failed (CLI helpers) */
+    DMTZ_ERR_NONCONVERGED = 4,  /* iteration cap reached before the complexes agree */
+    DMTZ_ERR_CYCLE = 5,         /* a gradient path walk exceeded its step cap */
+    DMTZ_ERR_BOUND = 6,         /* an output value violates the error bound */
+    DMTZ_ERR_UNSUPPORTED = 7,   /* flag combination not implemented */
+    DMTZ_ERR_OOB = 8            /* the reference rules would index out of range here */
+} dmtz_status;
+
+typedef struct dmtz_ctx dmtz_ctx;
+
+/* The reference's seven command-line flags (main_3d.cu:6265-6272) plus
+ * controls of this implementation. */
+typedef struct {
+    int preserve_saddles;     /* argv[4] */
+    int preserve_vpath;       /* argv[5] */
+    int preserve_geometry;    /* argv[6] */
+    int filtration;           /* argv[7] */
+    int preserve_connectors;  /* argv[8]; 1 is rejected (DMTZ_ERR_UNSUPPORTED) */
+    int preserve_type;        /* argv[9] */
+    int edit_type;            /* argv[10] */
+    int max_rounds;           /* cap on fix/apply rounds; 0 = 100000 */
+    int use_graph;            /* 1: run the loop as a CUDA graph with a device-side
+                                 convergence flag; 0: host-driven loop */
+} dmtz_opts;
+
+typedef struct {
+    int64_t outer_iterations;   /* total_ite of the reference (main_3d.cu:6786) */
+    int64_t cp_rounds;          /* rounds of the critical-point loop */
+    int64_t path_rounds;        /* rounds of the separatrix phase */
+    int64_t initial_mismatch[4];/* min, 1-saddle, 2-saddle, max before correction */
+    int64_t final_mismatch[4];
+    int64_t final_paths[2];     /* ascending, descending separatrix records */
+    int64_t edited_vertices;    /* vertices whose value changed */
+    int32_t converged;
+    int32_t error_flags;        /* bit 0: out-of-range index met by a fix rule,
+                                   bit 1: path-walk step cap reached */
+    double seconds;             /* device time of the whole correction */
+} dmtz_report;
+
+/* Context: owns the device, a stream and all scratch memory.
+ * Replaces the device globals and cudaMalloc calls of main_3d.cu:43-129,
+ * 6466-6714. */
+dmtz_status dmtz_ctx_create(dmtz_ctx **out, int device);
+void dmtz_ctx_destroy(dmtz_ctx *ctx);
+const char *dmtz_last_error(const dmtz_ctx *ctx);
+
+/* Cell counts V, E, F, T of a W x H x D grid (main_3d.cu:6401-6415). */
+dmtz_status dmtz_cell_counts(int W, int H, int D, int64_t out[4]);
+
+/* Discrete gradient of one field: the five pairing passes processVertices,
+ * edgePairingKernel(a2=0), trianglePairingKernel(a2=0), edgePairingKernel(a2=1),
+ * trianglePairingKernel(a2=1) (main_3d.cu:1930-2316), exported in the
+ * reference's layout (paired_vertices / _edges / _faces / _tetrahedras). */
+dmtz_status dmtz_extract(dmtz_ctx *ctx, int W, int H, int D, const double *data, int on_device,
+                         int32_t *PV, int32_t *PE, int32_t *PF, int32_t *PT);
+
+/* Critical-cell mismatch between the gradients of `orig` and `decp`
+ * (get_false_minimum/saddle/2_saddle/maximum, main_3d.cu:2492-2550).
+ * counts[4] = {min, 1-saddle, 2-saddle, max}; each list (capacity = the
+ * number of cells of that dimension, may be NULL) receives the mismatched cell
+ * ids in increasing order. */
+dmtz_status dmtz_mismatch(dmtz_ctx *ctx, int W, int H, int D, const double *orig, const double *decp,
+                          int64_t counts[4], int32_t *lmin, int32_t *lsad, int32_t *l2sad, int32_t *lmax);
+
+/* One critical-point fix round (fix_minimum, fix_saddle, fix_2saddle,
+ * fix_maximum; main_3d.cu:2554-4303) on the current mismatch: writes the
+ * per-vertex delta that the reference's d_deltaBuffer would hold, or
+ * -2000*range (the reference's "no request" sentinel) where nothing was
+ * requested.  edit_counter: per-vertex delta_counter (host, V ints). */
+dmtz_status dmtz_fix_round(dmtz_ctx *ctx, int W, int H, int D, const double *orig, const double *decp,
+                           const int32_t *edit_counter, double rel_eps, int preserve_saddles, int edit_type,
+                           double *delta_out);
+
+/* Geometry-mode separatrix check (get_false_as_vpath + is_false,
+ * get_false_ds_vpath; main_3d.cu:4437-4610, 4837-4959).  counts[2] =
+ * {ascending, descending}; as_tet/as_cur: starting coface tet and the tet
+ * where the pairing first differs; ds_edge/ds_vert: 1-saddle and vertex.
+ * Lists are sorted by (first, second); capacities F (ascending), E
+ * (descending). */
+dmtz_status dmtz_path_detect(dmtz_ctx *ctx, int W, int H, int D, const double *orig, const double *decp,
+                             int64_t counts[2], int32_t *as_tet, int32_t *as_cur, int32_t *ds_edge,
+                             int32_t *ds_vert);
+
+/* The whole correction (main_3d.cu:6255-7149): extracts both complexes and
+ * edits `decp` in place until they agree.  bound = (max(orig) - min(orig)) *
+ * rel_eps, as in the reference.  edit_counter_out (optional, V ints) receives
+ * delta_counter.  Returns DMTZ_ERR_NONCONVERGED if opts->max_rounds is hit. */
+dmtz_status dmtz_correct(dmtz_ctx *ctx, int W, int H, int D, const double *orig, double *decp, int on_device,
+                         double rel_eps, const dmtz_opts *opts, dmtz_report *report, int32_t *edit_counter_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DMTZ_H */

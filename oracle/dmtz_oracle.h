@@ -1,0 +1,88 @@
+/*
+ * dmtz_oracle.h — CPU oracle for the DMTz topology-correction path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a serial C restatement of the
+ * reference's CUDA kernels (main_3d.cu), used by tests/, by the smoke check
+ * and by bench.py's CPU-baseline leg to check and to time the product.  The
+ * product library (dmtz_gb300/) never links, loads or calls it.
+ *
+ * Pinning: the oracle is checked against outputs of the reference program
+ * itself (built from main_3d.cu with its one-character compile fix and run
+ * on a GB300); the fixtures live in tests/golden/ together with the script
+ * that produced them (oracle/ref_harness.py).
+ *
+ * Conventions follow the reference exactly: vertex id = x + y*W + z*W*H,
+ * edge/face/tet ids as produced by getEdgeID / getTriangleID /
+ * getTetrahedraID, pairing arrays hold -1 for "unpaired" and otherwise the
+ * id of the partner cell (a union of lower/higher dimension, disambiguated by
+ * back-pointer checks), all ids are 32-bit ints.
+ */
+#ifndef DMTZ_ORACLE_H
+#define DMTZ_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* counts of cells of the implicit Freudenthal complex (main_3d.cu:6401-6415) */
+void orc_counts(int W, int H, int D, long long out[4]);
+
+/* Five-pass discrete-gradient pairing of one field (main_3d.cu:1930-2316).
+ * Arrays are overwritten (all -1 first, as init_* do).  Returns number of
+ * out-of-bounds index events (0 for any valid grid). */
+int orc_pair(int W, int H, int D, const double *data,
+             int *PV, int *PE, int *PF, int *PT, int nthreads);
+
+/* Critical-cell mismatch counts between two pairings (get_false_*,
+ * main_3d.cu:2492-2550).  Lists (optional, may be NULL) receive the cell ids
+ * in increasing id order. counts = {min, saddle, 2saddle, max}. */
+void orc_cp_mismatch(int W, int H, int D,
+                     const int *PV, const int *PE, const int *PF, const int *PT,
+                     const int *QV, const int *QE, const int *QF, const int *QT,
+                     int counts[4], int *lmin, int *lsad, int *l2sad, int *lmax);
+
+/* One critical-point fix round (fix_minimum / fix_saddle / fix_2saddle /
+ * fix_maximum, main_3d.cu:2554-4303) on the given mismatch lists.  buf is the
+ * per-vertex delta buffer (V doubles) initialised by the caller to the
+ * sentinel -2000*range; cnt the per-vertex edit counter.  Returns the number
+ * of out-of-bounds events. */
+int orc_fix_cp(int W, int H, int D, const double *f, const double *g,
+               const int *cnt, double bound, double range, int edit_type,
+               int preserve_saddles,
+               const int *PV, const int *PE, const int *PF, const int *PT,
+               const int *QV, const int *QE, const int *QF, const int *QT,
+               const int counts[4], const int *lmin, const int *lsad,
+               const int *l2sad, const int *lmax, double *buf);
+
+/* Geometry-mode separatrix detection (get_false_as_vpath + is_false,
+ * get_false_ds_vpath; main_3d.cu:4437-4610, 4837-4959).  Outputs the record
+ * lists in increasing saddle-id order: as_tet[k] = starting coface tet,
+ * as_cur[k] = tet where the pairing first differs; ds_edge[k] = 1-saddle,
+ * ds_vert[k] = vertex where the pairing differs.  counts = {as, ds}.
+ * Returns number of out-of-bounds/cycle events. */
+int orc_path_detect(int W, int H, int D,
+                    const int *PV, const int *PE, const int *PF, const int *PT,
+                    const int *QV, const int *QE, const int *QF, const int *QT,
+                    int counts[2], int *as_tet, int *as_cur,
+                    int *ds_edge, int *ds_vert);
+
+/* Full correction run (host loop main_3d.cu:6255-7149).
+ *   f, g       : original / decompressed field (g is corrected in place)
+ *   rel_eps    : the relative error bound argument
+ *   flags[7]   : preserve_saddles, preserve_vpath, preserve_geometry,
+ *                filtration, preserve_connectors, preserve_type, edit_type
+ *   max_outer  : cap on outer iterations (0 = 100000)
+ *   stats[8]   : out: outer iterations (total_ite), CP inner iterations,
+ *                out-of-bounds events, converged(1/0), initial mismatch
+ *                counts min, saddle, 2saddle, max
+ *   cnt_out    : out (optional): final per-vertex edit counter
+ * preserve_connectors=1 is not supported (the reference path is racy);
+ * returns -1 for it, else 0. */
+int orc_correct(int W, int H, int D, const double *f, double *g,
+                double rel_eps, const int flags[7], int max_outer,
+                int nthreads, long long stats[8], int *cnt_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

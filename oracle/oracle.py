@@ -1,0 +1,131 @@
+"""ctypes front end of the CPU oracle (test infrastructure only).
+
+Only tests/, the smoke check and bench.py's CPU-baseline leg import this
+module; the product package never does.  The oracle restates the reference
+kernels of main_3d.cu serially in C (oracle/dmtz_oracle.c); arrays use the
+reference's cell numbering and its -1 = "unpaired" convention.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libdmtz_oracle.so")
+_lib = None
+
+_i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_i64p = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
+
+
+def build() -> str:
+    """Compile the oracle with its Makefile (idempotent)."""
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        src = os.path.join(_HERE, "dmtz_oracle.c")
+        if not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
+            build()
+        L = ctypes.CDLL(_LIB_PATH)
+        L.orc_counts.argtypes = [ctypes.c_int] * 3 + [_i64p]
+        L.orc_pair.argtypes = [ctypes.c_int] * 3 + [_f64p, _i32p, _i32p, _i32p, _i32p, ctypes.c_int]
+        L.orc_pair.restype = ctypes.c_int
+        L.orc_cp_mismatch.argtypes = [ctypes.c_int] * 3 + [_i32p] * 8 + [_i32p] + [_i32p] * 4
+        L.orc_fix_cp.argtypes = (
+            [ctypes.c_int] * 3 + [_f64p, _f64p, _i32p, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int]
+            + [_i32p] * 8 + [_i32p] + [_i32p] * 4 + [_f64p]
+        )
+        L.orc_fix_cp.restype = ctypes.c_int
+        L.orc_path_detect.argtypes = [ctypes.c_int] * 3 + [_i32p] * 8 + [_i32p] + [_i32p] * 4
+        L.orc_path_detect.restype = ctypes.c_int
+        L.orc_correct.argtypes = [ctypes.c_int] * 3 + [_f64p, _f64p, ctypes.c_double, _i32p, ctypes.c_int,
+                                                        ctypes.c_int, _i64p, _i32p]
+        L.orc_correct.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def counts(dims):
+    W, H, D = dims
+    out = np.zeros(4, np.int64)
+    lib().orc_counts(W, H, D, out)
+    return tuple(int(v) for v in out)
+
+
+def pair(data: np.ndarray, dims, threads: int = 1):
+    """Five-pass gradient pairing -> (PV, PE, PF, PT) int32 arrays."""
+    W, H, D = dims
+    V, E, F, T = counts(dims)
+    d = np.ascontiguousarray(data, dtype=np.float64).reshape(-1)
+    assert d.size == V
+    PV = np.empty(V, np.int32)
+    PE = np.empty(E, np.int32)
+    PF = np.empty(F, np.int32)
+    PT = np.empty(T, np.int32)
+    oob = lib().orc_pair(W, H, D, d, PV, PE, PF, PT, threads)
+    if oob:
+        raise RuntimeError(f"oracle pairing touched {oob} out-of-range ids")
+    return PV, PE, PF, PT
+
+
+def cp_mismatch(P, Q, dims):
+    """Critical-cell mismatch lists (min, 1-saddle, 2-saddle, max)."""
+    W, H, D = dims
+    V, E, F, T = counts(dims)
+    c = np.zeros(4, np.int32)
+    lists = [np.empty(max(n, 1), np.int32) for n in (V, E, F, T)]
+    lib().orc_cp_mismatch(W, H, D, *P, *Q, c, *lists)
+    return [lists[k][: int(c[k])].copy() for k in range(4)]
+
+
+def fix_cp(f, g, cnt, bound, rng, edit_type, preserve_saddles, P, Q, lists, dims):
+    """One critical-point fix round -> per-vertex delta buffer (sentinel = -2000*range)."""
+    W, H, D = dims
+    V = counts(dims)[0]
+    buf = np.full(V, -2000.0 * rng, np.float64)
+    c = np.array([len(x) for x in lists], np.int32)
+    ls = [np.ascontiguousarray(x, np.int32) if len(x) else np.zeros(1, np.int32) for x in lists]
+    oob = lib().orc_fix_cp(W, H, D, np.ascontiguousarray(f, np.float64).reshape(-1),
+                           np.ascontiguousarray(g, np.float64).reshape(-1), np.ascontiguousarray(cnt, np.int32),
+                           float(bound), float(rng), int(edit_type), int(preserve_saddles), *P, *Q, c, *ls, buf)
+    return buf, oob
+
+
+def path_detect(P, Q, dims):
+    """Geometry-mode separatrix records: (as_tet, as_cur, ds_edge, ds_vert)."""
+    W, H, D = dims
+    V, E, F, T = counts(dims)
+    c = np.zeros(2, np.int32)
+    a_t = np.empty(F, np.int32)
+    a_c = np.empty(F, np.int32)
+    d_e = np.empty(E, np.int32)
+    d_v = np.empty(E, np.int32)
+    oob = lib().orc_path_detect(W, H, D, *P, *Q, c, a_t, a_c, d_e, d_v)
+    na, nd = int(c[0]), int(c[1])
+    return a_t[:na].copy(), a_c[:na].copy(), d_e[:nd].copy(), d_v[:nd].copy(), oob
+
+
+def correct(f, g, dims, rel_eps, flags, max_outer=0, threads=1):
+    """Run the full correction loop.  Returns (corrected g, stats dict, cnt)."""
+    W, H, D = dims
+    V = counts(dims)[0]
+    ff = np.ascontiguousarray(f, np.float64).reshape(-1)
+    gg = np.array(g, np.float64).reshape(-1)
+    assert ff.size == V and gg.size == V
+    fl = np.ascontiguousarray(flags, np.int32)
+    st = np.zeros(8, np.int64)
+    cnt = np.empty(V, np.int32)
+    rc = lib().orc_correct(W, H, D, ff, gg, float(rel_eps), fl, int(max_outer), int(threads), st, cnt)
+    if rc != 0:
+        raise ValueError("flag combination not supported by the oracle")
+    stats = dict(outer_iterations=int(st[0]), cp_iterations=int(st[1]), oob=int(st[2]), converged=bool(st[3]),
+                 initial_mismatch=[int(x) for x in st[4:8]])
+    return gg, stats, cnt

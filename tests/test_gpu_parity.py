@@ -1,0 +1,163 @@
+"""Parity of the CUDA path (through the C ABI) with the oracle and with the
+reference's own outputs.  Integer/index results must match exactly; the
+corrected float64 field must match bit for bit."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import fixture_files, load_fixture, reference_cnt, reference_fixed, sha
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+FIXTURES = fixture_files()
+
+
+def _id(p):
+    return os.path.basename(p)[4:-4]
+
+
+def _assert_pairing_equal(got, want):
+    for a, b, k in zip(got, want, ("PV", "PE", "PF", "PT")):
+        bad = np.nonzero(a != b)[0]
+        assert bad.size == 0, f"{k}: {bad.size} differ, first ids {bad[:5]} got {a[bad[:5]]} want {b[bad[:5]]}"
+
+
+@pytest.mark.parametrize("path", FIXTURES, ids=_id)
+def test_extract_matches_reference(gpu_ctx, path):
+    meta, z, f, g = load_fixture(path)
+    dims = tuple(meta["dims"])
+    P = gpu_ctx.extract(f, dims)
+    for a, k in zip(P, ("PV", "PE", "PF", "PT")):
+        assert sha(a) == meta[k + "_sha256"], k
+    if meta["flags"][3] == 0:
+        Q = gpu_ctx.extract(g, dims)
+        for a, k in zip(Q, ("QV", "QE", "QF", "QT")):
+            assert sha(a) == meta[k + "_sha256"], k
+
+
+@pytest.mark.parametrize("path", FIXTURES, ids=_id)
+def test_mismatch_lists_match_oracle(gpu_ctx, path):
+    meta, z, f, g = load_fixture(path)
+    dims = tuple(meta["dims"])
+    got = gpu_ctx.mismatch(f, g, dims)
+    want = O.cp_mismatch(O.pair(f, dims, 4), O.pair(g, dims, 4), dims)
+    for a, b in zip(got, want):
+        assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("path", [p for p in FIXTURES if "1001000" not in p], ids=_id)
+def test_first_fix_round_matches_reference(gpu_ctx, path):
+    meta, z, f, g = load_fixture(path)
+    dims = tuple(meta["dims"])
+    cnt = np.ones(f.size, np.int32)
+    buf = gpu_ctx.fix_round(f, g, cnt, meta["rel"], meta["flags"][0], meta["flags"][6], dims)
+    rng = float(f.max() - f.min())
+    idx = np.nonzero(buf != -2000.0 * rng)[0]
+    assert np.array_equal(idx, z["r0_idx"])
+    assert np.array_equal(buf[idx], z["r0_buf"])
+
+
+@pytest.mark.parametrize("path", FIXTURES, ids=_id)
+def test_path_detect_matches_oracle(gpu_ctx, path):
+    meta, z, f, g = load_fixture(path)
+    dims = tuple(meta["dims"])
+    got = gpu_ctx.path_detect(f, g, dims)
+    a_t, a_c, d_e, d_v, oob = O.path_detect(O.pair(f, dims, 4), O.pair(g, dims, 4), dims)
+    want_as = sorted(set(zip(a_t.tolist(), a_c.tolist())))
+    got_as = sorted(set(zip(got[0].tolist(), got[1].tolist())))
+    assert got_as == want_as
+    assert sorted(zip(got[2].tolist(), got[3].tolist())) == sorted(zip(d_e.tolist(), d_v.tolist()))
+
+
+@pytest.mark.parametrize("path", FIXTURES, ids=_id)
+def test_correction_matches_reference(gpu_ctx, path):
+    meta, z, f, g = load_fixture(path)
+    dims = tuple(meta["dims"])
+    out, rep, cnt = gpu_ctx.correct(f, g, meta["rel"], meta["flags"], dims=dims, return_counter=True)
+    ref = reference_fixed(z, g)
+    assert rep["converged"]
+    bad = np.nonzero(out != ref)[0]
+    assert bad.size == 0, f"{bad.size} values differ, first {bad[:5]}"
+    assert np.array_equal(cnt, reference_cnt(z, f.size))
+    assert rep["outer_iterations"] + 1 == meta["iteration_number"]
+
+
+EDGE_CASES = [
+    ("tiny2", (2, 2, 2), "gauss", 0),
+    ("tiny3", (3, 3, 3), "powerlaw", 1),
+    ("noncubic", (5, 6, 7), "powerlaw", 2),
+    ("flat", (7, 5, 6), "const", 0),
+    ("ties", (11, 9, 8), "ties", 4),
+    ("thin", (40, 3, 2), "powerlaw", 5),
+]
+
+
+def _edge_field(kind, dims, seed):
+    from dmtz_gb300 import synth
+
+    if kind == "gauss":
+        return synth.gaussian_mix(dims, seed, n_gauss=4).reshape(-1)
+    if kind == "powerlaw":
+        return synth.power_law(dims, seed).reshape(-1)
+    if kind == "const":
+        return np.full(int(np.prod(dims)), 0.25)
+    r = np.random.Generator(np.random.PCG64(seed))
+    return r.integers(0, 4, size=int(np.prod(dims))).astype(np.float64)
+
+
+@pytest.mark.parametrize("name,dims,kind,seed", EDGE_CASES, ids=[c[0] for c in EDGE_CASES])
+def test_extract_edge_cases(gpu_ctx, name, dims, kind, seed):
+    f = _edge_field(kind, dims, seed)
+    _assert_pairing_equal(gpu_ctx.extract(f, dims), O.pair(f, dims))
+
+
+@pytest.mark.parametrize("name,dims,kind,seed", EDGE_CASES, ids=[c[0] for c in EDGE_CASES])
+def test_correction_edge_cases(gpu_ctx, name, dims, kind, seed):
+    f = _edge_field(kind, dims, seed)
+    rng = float(f.max() - f.min()) or 1.0
+    r = np.random.Generator(np.random.PCG64(seed + 99))
+    g = f + r.uniform(-0.05 * rng, 0.05 * rng, size=f.size)
+    rel = 0.05
+    want, st, wcnt = O.correct(f, g, dims, rel, [1, 1, 1, 0, 0, 0, 0], max_outer=300)
+    if not st["converged"]:
+        pytest.skip("the reference rules do not converge on this input")
+    out, rep, cnt = gpu_ctx.correct(f, g, rel, (1, 1, 1, 0, 0, 0, 0), dims=dims, return_counter=True)
+    assert np.array_equal(out, want)
+    assert np.array_equal(cnt, wcnt)
+
+
+def test_pairing_parity_128(gpu_ctx):
+    from dmtz_gb300 import synth
+
+    dims = (128, 96, 80)
+    f = synth.power_law(dims, 21).reshape(-1)
+    _assert_pairing_equal(gpu_ctx.extract(f, dims), O.pair(f, dims, threads=8))
+
+
+def test_correction_is_deterministic_and_bounded(gpu_ctx):
+    meta, z, f, g = load_fixture([p for p in fixture_files() if "p64_1110000" in p][0])
+    dims = tuple(meta["dims"])
+    a, ra = gpu_ctx.correct(f, g, meta["rel"], meta["flags"], dims=dims)
+    b, rb = gpu_ctx.correct(f, g, meta["rel"], meta["flags"], dims=dims)
+    assert np.array_equal(a, b) and ra["outer_iterations"] == rb["outer_iterations"]
+    bound = float(f.max() - f.min()) * meta["rel"]
+    assert np.all(a - (f - bound) >= -1e-9 * bound) and np.all(a <= np.maximum(g, f + bound))
+    # the corrected field's critical cells agree with the original's
+    assert all(len(x) == 0 for x in gpu_ctx.mismatch(f, a, dims))
+
+
+def test_rejects_bad_input(gpu_ctx):
+    import dmtz_gb300 as dm
+
+    f = np.zeros(27)
+    g = f.copy()
+    g[3] = np.nan
+    with pytest.raises(dm.DmtzError) as e:
+        gpu_ctx.correct(f, g, 0.1, dims=(3, 3, 3))
+    assert e.value.status == 2
+    with pytest.raises(dm.DmtzError) as e:
+        gpu_ctx.correct(f, f, 0.1, flags=(1, 1, 1, 0, 1, 0, 0), dims=(3, 3, 3))
+    assert e.value.status == 7
+    with pytest.raises(dm.DmtzError):
+        gpu_ctx.extract(np.zeros(4), dims=(1, 2, 2))
