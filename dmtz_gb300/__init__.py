@@ -44,13 +44,14 @@ class Report(ctypes.Structure):
     _fields_ = [("outer_iterations", ctypes.c_int64), ("cp_rounds", ctypes.c_int64), ("path_rounds", ctypes.c_int64),
                 ("initial_mismatch", ctypes.c_int64 * 4), ("final_mismatch", ctypes.c_int64 * 4),
                 ("final_paths", ctypes.c_int64 * 2), ("edited_vertices", ctypes.c_int64),
-                ("converged", ctypes.c_int32), ("error_flags", ctypes.c_int32), ("seconds", ctypes.c_double)]
+                ("converged", ctypes.c_int32), ("error_flags", ctypes.c_int32), ("seconds", ctypes.c_double),
+                ("kernel_launches", ctypes.c_int64)]
 
     def as_dict(self):
         return dict(outer_iterations=self.outer_iterations, cp_rounds=self.cp_rounds, path_rounds=self.path_rounds,
                     initial_mismatch=list(self.initial_mismatch), final_mismatch=list(self.final_mismatch),
                     final_paths=list(self.final_paths), converged=bool(self.converged),
-                    error_flags=self.error_flags, seconds=self.seconds)
+                    error_flags=self.error_flags, seconds=self.seconds, kernel_launches=self.kernel_launches)
 
 
 _i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
@@ -82,8 +83,9 @@ def load_library(build_if_missing: bool = True):
     L.dmtz_path_detect.argtypes = [_vp, _int, _int, _int, _f64p, _f64p, _i64p, _i32p, _i32p, _i32p, _i32p]
     L.dmtz_correct.argtypes = [_vp, _int, _int, _int, _vp, _vp, _int, ctypes.c_double, ctypes.POINTER(Opts),
                                ctypes.POINTER(Report), _vp]
+    L.dmtz_profile_sweep.argtypes = [_vp, _int, _int, _int, _vp, _vp, _int, _int, _f64p]
     for fn in ("dmtz_ctx_create", "dmtz_cell_counts", "dmtz_extract", "dmtz_mismatch", "dmtz_fix_round",
-               "dmtz_path_detect", "dmtz_correct"):
+               "dmtz_path_detect", "dmtz_correct", "dmtz_profile_sweep"):
         getattr(L, fn).restype = _int
     _lib = L
     return L
@@ -193,11 +195,19 @@ class Context:
         rep["edited_vertices"] = int((gg != _flat(g)).sum())
         return (gg, rep, cnt) if return_counter else (gg, rep)
 
-    def correct_device(self, f_ptr: int, g_ptr: int, dims, rel_eps, flags=(1, 1, 1, 0, 0, 0, 0), max_rounds=0,
-                       use_graph=0):
-        """Correction on device-resident float64 buffers (raw CUDA pointers); g is edited in place."""
+    def correct_ptr(self, f_ptr: int, g_ptr: int, dims, rel_eps, flags=(1, 1, 1, 0, 0, 0, 0), on_device=True,
+                    max_rounds=0, use_graph=0):
+        """Correction on raw float64 buffers (device pointers when on_device, else host
+        pointers, e.g. pinned memory); g is edited in place."""
         o = Opts(*[int(x) for x in flags], int(max_rounds), int(use_graph))
         r = Report()
-        self._check(self._L.dmtz_correct(self._h, *dims, _vp(f_ptr), _vp(g_ptr), 1, float(rel_eps),
-                                         ctypes.byref(o), ctypes.byref(r), None))
+        self._check(self._L.dmtz_correct(self._h, *dims, _vp(f_ptr), _vp(g_ptr), int(bool(on_device)),
+                                         float(rel_eps), ctypes.byref(o), ctypes.byref(r), None))
         return r.as_dict()
+
+    def profile_sweep(self, f_ptr: int, g_ptr: int, dims, reps=10, on_device=True):
+        """Mean per-launch ms of the six gradient-sweep kernels and of the whole sweep."""
+        ms = np.zeros(7, np.float64)
+        self._check(self._L.dmtz_profile_sweep(self._h, *dims, _vp(f_ptr), _vp(g_ptr), int(bool(on_device)),
+                                               int(reps), ms))
+        return ms

@@ -274,6 +274,25 @@ __global__ void k_filter(Grid g, const uint32_t *crit_o, const double *f, double
     }
 }
 
+// exact min / max of a field through its order keys
+__global__ void k_minmax(const double *a, i64 n, unsigned long long *kmin, unsigned long long *kmax) {
+    unsigned long long lo = ~0ull, hi = 0ull;
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+        const unsigned long long k = okey(a[i]);
+        lo = k < lo ? k : lo;
+        hi = k > hi ? k : hi;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long l2 = __shfl_xor_sync(0xffffffffu, lo, o), h2 = __shfl_xor_sync(0xffffffffu, hi, o);
+        lo = l2 < lo ? l2 : lo;
+        hi = h2 > hi ? h2 : hi;
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(kmin, lo);
+        atomicMax(kmax, hi);
+    }
+}
+
 __global__ void k_fill_i32(int *p, int val, i64 n) {
     i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) p[i] = val;
@@ -313,11 +332,10 @@ struct dmtz_ctx {
     i64 *reqlist = nullptr;
     i64 *lists[4] = {nullptr, nullptr, nullptr, nullptr};
     i64 *as_tet = nullptr, *as_cur = nullptr, *ds_edge = nullptr, *ds_vert = nullptr;
-    unsigned long long *counters = nullptr;  // [0..3] cp lists, [4] requests, [5,6] paths
+    unsigned long long *counters = nullptr;  // [0..3] cp lists, [4] requests, [5,6] paths, [8,9] min/max keys
     int *errword = nullptr;
     uint8_t *changed = nullptr;
-    void *scratch = nullptr;
-    size_t scratch_bytes = 0;
+    int64_t launches = 0;  // kernels launched by the current call
 };
 
 namespace {
@@ -377,7 +395,7 @@ dmtz_status ensure(dmtz_ctx *ctx, const Grid &g) {
     CK(dalloc(&ctx->lists[2], g.F)); CK(dalloc(&ctx->lists[3], g.T));
     CK(dalloc(&ctx->as_tet, g.F)); CK(dalloc(&ctx->as_cur, g.F));
     CK(dalloc(&ctx->ds_edge, g.E)); CK(dalloc(&ctx->ds_vert, g.E));
-    CK(dalloc(&ctx->counters, 8)); CK(dalloc(&ctx->errword, 1)); CK(dalloc(&ctx->changed, V));
+    CK(dalloc(&ctx->counters, 16)); CK(dalloc(&ctx->errword, 1)); CK(dalloc(&ctx->changed, V));
     ctx->capV = g.V; ctx->capE = g.E; ctx->capF = g.F; ctx->capT = g.T;
     return DMTZ_OK;
 }
@@ -388,6 +406,8 @@ FieldState view(const DevField &d, const double *val) {
     s.fa3 = d.fa3; s.eup = d.eup; s.fup = d.fup; s.crit = d.crit;
     return s;
 }
+
+unsigned persistent_grid();
 
 // five passes + criticality (and mismatch lists when crit_o is given)
 void run_pairing(dmtz_ctx *ctx, const Grid &g, const FieldState &s, const uint32_t *crit_o, int want_saddles) {
@@ -403,6 +423,27 @@ void run_pairing(dmtz_ctx *ctx, const Grid &g, const FieldState &s, const uint32
     L.n = ctx->counters;
     if (crit_o) cudaMemsetAsync(ctx->counters, 0, 4 * sizeof(unsigned long long), st);
     k_crit<<<gr, kBlock, 0, st>>>(g, s, crit_o, L, want_saddles, 0, g.V);
+    ctx->launches += 6;
+}
+
+double key_to_double(unsigned long long k) {
+    uint64_t b = (k & 0x8000000000000000ull) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k;
+    double d;
+    memcpy(&d, &b, 8);
+    return d;
+}
+
+// min and max of a device field (exact)
+dmtz_status device_minmax(dmtz_ctx *ctx, const double *a, i64 n, double &mn, double &mx) {
+    unsigned long long init[2] = {~0ull, 0ull}, out[2];
+    CK(cudaMemcpyAsync(ctx->counters + 8, init, sizeof(init), cudaMemcpyHostToDevice, ctx->stream));
+    k_minmax<<<persistent_grid(), kBlock, 0, ctx->stream>>>(a, n, ctx->counters + 8, ctx->counters + 9);
+    ctx->launches++;
+    CK(cudaMemcpyAsync(out, ctx->counters + 8, sizeof(out), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    mn = key_to_double(out[0]);
+    mx = key_to_double(out[1]);
+    return DMTZ_OK;
 }
 
 RuleCtx rule_ctx(dmtz_ctx *ctx, const Grid &g, double bound, int edit_type) {
@@ -442,6 +483,7 @@ dmtz_status upload(dmtz_ctx *ctx, double *dst, const double *src, i64 n, int on_
                        ctx->stream));
     CK(cudaMemsetAsync(ctx->errword, 0, sizeof(int), ctx->stream));
     k_check_finite<<<persistent_grid(), kBlock, 0, ctx->stream>>>(dst, n, ctx->errword);
+    ctx->launches++;
     int bad = 0;
     CK(cudaMemcpyAsync(&bad, ctx->errword, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
@@ -656,24 +698,23 @@ dmtz_status dmtz_correct(dmtz_ctx *ctx, int W, int H, int D, const double *orig,
     if ((s = upload(ctx, ctx->g, decp, g.V, on_device)) != DMTZ_OK) return s;
     // range and bound exactly as the reference computes them (main_3d.cu:6303-6323)
     double mn, mx;
-    if (on_device) {
-        std::vector<double> hf((size_t)g.V);
-        CK(cudaMemcpy(hf.data(), orig, sizeof(double) * (size_t)g.V, cudaMemcpyDeviceToHost));
-        host_minmax(hf.data(), g.V, mn, mx);
-    } else {
-        host_minmax(orig, g.V, mn, mx);
-    }
+    ctx->launches = 0;
+    CK(cudaEventRecord(e0, st));
+    if ((s = device_minmax(ctx, ctx->f, g.V, mn, mx)) != DMTZ_OK) return s;
     const double bound = (mx - mn) * rel_eps;
     const double range = mx - mn;
-    CK(cudaEventRecord(e0, st));
     CK(cudaMemsetAsync(ctx->errword, 0, sizeof(int), st));
     CK(cudaMemsetAsync(ctx->changed, 0, (size_t)g.V, st));
     CK(cudaMemsetAsync(ctx->counters, 0, 8 * sizeof(unsigned long long), st));
     const FieldState Ps = view(ctx->P, ctx->f), Qs = view(ctx->Q, ctx->g);
     run_pairing(ctx, g, Ps, nullptr, 1);
-    if (filt == 1) k_filter<<<grid_for(g.V), kBlock, 0, st>>>(g, ctx->P.crit, ctx->f, ctx->g, bound);
+    if (filt == 1) {
+        k_filter<<<grid_for(g.V), kBlock, 0, st>>>(g, ctx->P.crit, ctx->f, ctx->g, bound);
+        ctx->launches++;
+    }
     run_pairing(ctx, g, Qs, ctx->P.crit, 1);
     k_fill_i32<<<grid_for(g.V), kBlock, 0, st>>>(ctx->cnt, 1, g.V);
+    ctx->launches++;
     unsigned long long hc[8];
     auto read_counts = [&]() -> dmtz_status {
         CK(cudaMemcpyAsync(hc, ctx->counters, sizeof(hc), cudaMemcpyDeviceToHost, st));
@@ -708,6 +749,7 @@ dmtz_status dmtz_correct(dmtz_ctx *ctx, int W, int H, int D, const double *orig,
             CK(cudaMemsetAsync(ctx->counters + 4, 0, sizeof(unsigned long long), st));
             k_fix_cp<<<pgrid, kBlock, 0, st>>>(rc, L, ps);
             k_apply<<<pgrid, kBlock, 0, st>>>(rc, range, pt, 1, ctx->changed, nullptr);
+            ctx->launches += 2;
             run_pairing(ctx, g, Qs, ctx->P.crit, ps == 1);
             if ((s = read_counts()) != DMTZ_OK) return s;
             for (int k = 0; k < 4; k++) cc[k] = (i64)hc[k];
@@ -726,6 +768,7 @@ dmtz_status dmtz_correct(dmtz_ctx *ctx, int W, int H, int D, const double *orig,
         CK(cudaMemsetAsync(ctx->counters + 4, 0, sizeof(unsigned long long), st));
         k_fix_path<<<pgrid, kBlock, 0, st>>>(rc, PR);
         k_apply<<<pgrid, kBlock, 0, st>>>(rc, range, pt, 1, ctx->changed, nullptr);
+        ctx->launches += 4;
         run_pairing(ctx, g, Qs, ctx->P.crit, 1);
         if ((s = read_counts()) != DMTZ_OK) return s;
         for (int k = 0; k < 4; k++) cc[k] = (i64)hc[k];
@@ -734,6 +777,7 @@ dmtz_status dmtz_correct(dmtz_ctx *ctx, int W, int H, int D, const double *orig,
             CK(cudaMemsetAsync(ctx->counters + 5, 0, 2 * sizeof(unsigned long long), st));
             k_path_as<<<pgrid, kBlock, 0, st>>>(rc, PR, g.T + 16);
             k_path_ds<<<pgrid, kBlock, 0, st>>>(rc, PR);
+            ctx->launches += 2;
             if ((s = read_counts()) != DMTZ_OK) return s;
             n_as = (i64)hc[5];
             n_ds = (i64)hc[6];
@@ -758,10 +802,65 @@ dmtz_status dmtz_correct(dmtz_ctx *ctx, int W, int H, int D, const double *orig,
     R.converged = converged;
     R.error_flags = err;
     R.seconds = ms * 1e-3;
+    R.kernel_launches = ctx->launches;
     if (rep) *rep = R;
     if (err & ERR_OOB) return fail(ctx, DMTZ_ERR_OOB, "a fix rule indexed out of range");
     if (err & ERR_WALK) return fail(ctx, DMTZ_ERR_CYCLE, "ascending path walk exceeded its step cap");
     if (!converged) return fail(ctx, DMTZ_ERR_NONCONVERGED, "round cap reached before the complexes agree");
+    return DMTZ_OK;
+}
+
+dmtz_status dmtz_profile_sweep(dmtz_ctx *ctx, int W, int H, int D, const double *orig, const double *decp,
+                               int on_device, int reps, double ms[7]) {
+    Grid g;
+    dmtz_status s = check_dims(ctx, W, H, D, g);
+    if (s != DMTZ_OK) return s;
+    if (reps < 1) return fail(ctx, DMTZ_ERR_ARG, "reps must be >= 1");
+    CK(cudaSetDevice(ctx->device));
+    if ((s = ensure(ctx, g)) != DMTZ_OK) return s;
+    if ((s = upload(ctx, ctx->f, orig, g.V, on_device)) != DMTZ_OK) return s;
+    if ((s = upload(ctx, ctx->g, decp, g.V, on_device)) != DMTZ_OK) return s;
+    cudaStream_t st = ctx->stream;
+    const FieldState Ps = view(ctx->P, ctx->f), Qs = view(ctx->Q, ctx->g);
+    run_pairing(ctx, g, Ps, nullptr, 1);
+    run_pairing(ctx, g, Qs, ctx->P.crit, 1);  // warm-up
+    cudaEvent_t ev[7];
+    for (auto &e : ev) CK(cudaEventCreate(&e));
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    float total = 0;
+    Lists L;
+    for (int k = 0; k < 4; k++) L.l[k] = ctx->lists[k];
+    L.n = ctx->counters;
+    const unsigned gr = grid_for(g.V);
+    for (int r = 0; r < reps; r++) {
+        CK(cudaMemsetAsync(ctx->counters, 0, 4 * sizeof(unsigned long long), st));
+        CK(cudaEventRecord(ev[0], st));
+        k_pass_vertex<<<gr, kBlock, 0, st>>>(g, Qs, 0, g.V);
+        CK(cudaEventRecord(ev[1], st));
+        k_pass_edge_a2<<<gr, kBlock, 0, st>>>(g, Qs, 0, g.V);
+        CK(cudaEventRecord(ev[2], st));
+        k_pass_face_a3<<<gr, kBlock, 0, st>>>(g, Qs, 0, g.V);
+        CK(cudaEventRecord(ev[3], st));
+        k_pass_edge_a4<<<gr, kBlock, 0, st>>>(g, Qs, 0, g.V);
+        CK(cudaEventRecord(ev[4], st));
+        k_pass_face_a5<<<gr, kBlock, 0, st>>>(g, Qs, 0, g.V);
+        CK(cudaEventRecord(ev[5], st));
+        k_crit<<<gr, kBlock, 0, st>>>(g, Qs, ctx->P.crit, L, 1, 0, g.V);
+        CK(cudaEventRecord(ev[6], st));
+        CK(cudaEventSynchronize(ev[6]));
+        for (int k = 0; k < 6; k++) {
+            float t = 0;
+            cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
+            acc[k] += t;
+        }
+        float t = 0;
+        cudaEventElapsedTime(&t, ev[0], ev[6]);
+        total += t;
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    for (int k = 0; k < 6; k++) ms[k] = acc[k] / reps;
+    ms[6] = total / reps;
+    CK(cudaGetLastError());
     return DMTZ_OK;
 }
 

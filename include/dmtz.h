@@ -69,7 +69,9 @@ typedef struct {
     int32_t converged;
     int32_t error_flags;        /* bit 0: out-of-range index met by a fix rule,
                                    bit 1: path-walk step cap reached */
-    double seconds;             /* device time of the whole correction */
+    double seconds;             /* device time of the whole correction (CUDA events
+                                   on the context's stream, inputs already on the device) */
+    int64_t kernel_launches;    /* kernels this call launched */
 } dmtz_report;
 
 /* Context: owns the device, a stream and all scratch memory.
@@ -122,6 +124,15 @@ dmtz_status dmtz_path_detect(dmtz_ctx *ctx, int W, int H, int D, const double *o
  * delta_counter.  Returns DMTZ_ERR_NONCONVERGED if opts->max_rounds is hit. */
 dmtz_status dmtz_correct(dmtz_ctx *ctx, int W, int H, int D, const double *orig, double *decp, int on_device,
                          double rel_eps, const dmtz_opts *opts, dmtz_report *report, int32_t *edit_counter_out);
+
+/* Timing of the gradient sweep that every correction round runs (the five
+ * pairing passes of main_3d.cu:6864-6874 plus the critical-cell comparison
+ * of :6903-6909), `reps` times on the context's stream between CUDA events.
+ * ms[0..5] = mean per-launch time of the vertex, edge, triangle, edge,
+ * triangle and criticality kernels; ms[6] = mean time of one whole sweep.
+ * No counterpart call in the reference (measurement only). */
+dmtz_status dmtz_profile_sweep(dmtz_ctx *ctx, int W, int H, int D, const double *orig, const double *decp,
+                               int on_device, int reps, double ms[7]);
 
 #ifdef __cplusplus
 }
