@@ -14,6 +14,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <mutex>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -865,3 +866,80 @@ dmtz_status dmtz_profile_sweep(dmtz_ctx *ctx, int W, int H, int D, const double 
 }
 
 }  // extern "C"
+
+// =============================================================================
+// allocation-free extraction (dmtz_extract_noalloc)
+// =============================================================================
+namespace {
+
+// byte layout of the fixed scratch: the FieldState arrays of one field, each
+// starting on a 256-byte boundary
+constexpr i64 kNaV = DMTZ_NOALLOC_MAX_VERTICES;
+constexpr i64 na_round(i64 b) { return (b + 255) / 256 * 256; }
+constexpr i64 kNaKey = 0;
+constexpr i64 kNaLow = kNaKey + na_round(kNaV * 8);
+constexpr i64 kNaPv = kNaLow + na_round(kNaV * 2);
+constexpr i64 kNaEa2 = kNaPv + na_round(kNaV * 1);
+constexpr i64 kNaFp3 = kNaEa2 + na_round(kNaV * 4);
+constexpr i64 kNaFa3 = kNaFp3 + na_round(kNaV * 2);
+constexpr i64 kNaEup = kNaFa3 + na_round(kNaV * 4);
+constexpr i64 kNaFup = kNaEup + na_round(kNaV * 4);
+constexpr i64 kNaCrit = kNaFup + na_round(kNaV * 4);
+constexpr i64 kNaBytes = kNaCrit + na_round(kNaV * 4);
+
+}  // namespace
+
+// Every array of the gradient state is fully rewritten by the passes before it
+// is read, so the contents a previous call left behind need no clearing.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
+
+namespace {
+std::mutex g_noalloc_mu;
+constexpr int kNaMaxDevices = 64;
+void *g_noalloc_addr[kNaMaxDevices] = {};
+
+// device address of the scratch on the current device, looked up once per device
+cudaError_t noalloc_scratch(int dev, unsigned char **out) {
+    if (dev < 0 || dev >= kNaMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        g_noalloc_addr[dev] = p;
+    }
+    *out = (unsigned char *)g_noalloc_addr[dev];
+    return cudaSuccess;
+}
+}  // namespace
+
+extern "C" dmtz_status dmtz_extract_noalloc(int W, int H, int D, const double *data, int32_t *PV, int32_t *PE,
+                                            int32_t *PF, int32_t *PT, void *stream) {
+    if (W < 2 || H < 2 || D < 2 || !data || !PV || !PE || !PF || !PT) return DMTZ_ERR_ARG;
+    const Grid g = make_grid(W, H, D);
+    if (g.V > kNaV) return DMTZ_ERR_TOO_LARGE;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return DMTZ_ERR_CUDA;
+    unsigned char *base = nullptr;
+    if (noalloc_scratch(dev, &base) != cudaSuccess) return DMTZ_ERR_CUDA;
+    FieldState s;
+    s.val = data;
+    s.key = (uint64_t *)(base + kNaKey);
+    s.low = (uint16_t *)(base + kNaLow);
+    s.pv = (uint8_t *)(base + kNaPv);
+    s.ea2 = (uint32_t *)(base + kNaEa2);
+    s.fp3 = (uint16_t *)(base + kNaFp3);
+    s.fa3 = (uint32_t *)(base + kNaFa3);
+    s.eup = (uint32_t *)(base + kNaEup);
+    s.fup = (uint32_t *)(base + kNaFup);
+    s.crit = (uint32_t *)(base + kNaCrit);
+    cudaStream_t st = (cudaStream_t)stream;
+    const unsigned gr = grid_for(g.V);
+    k_pass_vertex<<<gr, kBlock, 0, st>>>(g, s, 0, g.V);
+    k_pass_edge_a2<<<gr, kBlock, 0, st>>>(g, s, 0, g.V);
+    k_pass_face_a3<<<gr, kBlock, 0, st>>>(g, s, 0, g.V);
+    k_pass_edge_a4<<<gr, kBlock, 0, st>>>(g, s, 0, g.V);
+    k_pass_face_a5<<<gr, kBlock, 0, st>>>(g, s, 0, g.V);
+    k_export<<<gr, kBlock, 0, st>>>(g, s, PV, PE, PF, PT);
+    return cudaGetLastError() == cudaSuccess ? DMTZ_OK : DMTZ_ERR_CUDA;
+}

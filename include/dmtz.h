@@ -38,7 +38,8 @@ typedef enum {
     DMTZ_ERR_CYCLE = 5,         /* a gradient path walk exceeded its step cap */
     DMTZ_ERR_BOUND = 6,         /* an output value violates the error bound */
     DMTZ_ERR_UNSUPPORTED = 7,   /* flag combination not implemented */
-    DMTZ_ERR_OOB = 8            /* the reference rules would index out of range here */
+    DMTZ_ERR_OOB = 8,           /* the reference rules would index out of range here */
+    DMTZ_ERR_TOO_LARGE = 9      /* grid exceeds the fixed scratch of dmtz_extract_noalloc */
 } dmtz_status;
 
 typedef struct dmtz_ctx dmtz_ctx;
@@ -133,6 +134,32 @@ dmtz_status dmtz_correct(dmtz_ctx *ctx, int W, int H, int D, const double *orig,
  * No counterpart call in the reference (measurement only). */
 dmtz_status dmtz_profile_sweep(dmtz_ctx *ctx, int W, int H, int D, const double *orig, const double *decp,
                                int on_device, int reps, double ms[7]);
+
+/* Allocation-free variant of dmtz_extract, for callers that cannot call
+ * cudaMalloc: applications whose device memory is owned by their own pool
+ * allocator (which forbids or cannot account for foreign allocations), and
+ * latency-sensitive pipelines where a cudaMalloc/cudaFree would synchronise
+ * the device in the middle of their stream work.  It has no counterpart in
+ * the reference.
+ *
+ * The caller passes every buffer: `data` (V doubles) and the four output
+ * arrays (dmtz_cell_counts sizes, int32), all DEVICE pointers on the current
+ * device, and a cudaStream_t as `stream` (NULL = the legacy default stream).
+ * The call only enqueues kernels on that stream and returns; results are
+ * ready when the stream reaches that point.  Inputs must be finite (not
+ * checked here).
+ *
+ * Scratch: the per-vertex gradient state lives in one fixed device array
+ * inside the library, sized for at most DMTZ_NOALLOC_MAX_VERTICES vertices
+ * (64^3; about 8.7 MB that every GPU which loads the library keeps until the
+ * process exits).  Larger grids return DMTZ_ERR_TOO_LARGE.  The first call on
+ * a device looks up that array's device address (cudaGetSymbolAddress), so
+ * make that first call before any stream capture.  All calls share the one
+ * array: calls that can overlap on the GPU (different streams, or different
+ * host threads) race and must be serialised by the caller. */
+#define DMTZ_NOALLOC_MAX_VERTICES (64 * 64 * 64)
+dmtz_status dmtz_extract_noalloc(int W, int H, int D, const double *data, int32_t *PV, int32_t *PE, int32_t *PF,
+                                 int32_t *PT, void *stream);
 
 #ifdef __cplusplus
 }
