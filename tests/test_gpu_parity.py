@@ -161,3 +161,21 @@ def test_rejects_bad_input(gpu_ctx):
     assert e.value.status == 7
     with pytest.raises(dm.DmtzError):
         gpu_ctx.extract(np.zeros(4), dims=(1, 2, 2))
+
+
+def test_correction_256_matches_reference_digest(gpu_ctx):
+    """The bench workload: the reference's own 256^3 run (tests/golden/ref_big_p256.json)."""
+    import json
+
+    from conftest import GOLDEN
+    from oracle.ref_harness import case_fields
+
+    m = json.load(open(os.path.join(GOLDEN, "ref_big_p256.json")))
+    dims = tuple(m["dims"])
+    f, g = case_fields(m["kind"], dims, m["seed"], m["rel"], m["decomp"], m["kw"])
+    f, g = f.reshape(-1), g.reshape(-1)
+    out, rep = gpu_ctx.correct(f, g, m["rel"], m["flags"], dims=dims)
+    assert rep["converged"]
+    assert rep["outer_iterations"] + 1 == m["iteration_number"]
+    assert int((out != g).sum()) == m["changed"]
+    assert sha(out) == m["fixed_sha256"]
