@@ -258,7 +258,8 @@ def run_ours(args, rank, world, local_rank):
                            "l2": "inputs and state larger than L2 (f and g alone are 268 MB)",
                            "outer_iterations": rep["outer_iterations"], "cp_rounds": rep["cp_rounds"],
                            "path_rounds": rep["path_rounds"], "initial_mismatch": rep["initial_mismatch"],
-                           "within_bound": ok_bound, "wall_s_per_step": wall / args.steps},
+                           "within_bound": ok_bound, "wall_s_per_step": wall / args.steps,
+                           "phase_ms": rep["phase_ms"]},
                 "time_to_match_s": t_step,
                 "e2e": {"value": world * V / e2e_step / 1e6, "unit": "Mvox/s", "seconds_per_step": e2e_step,
                         "h2d_bytes_per_step": 2 * V * 8, "d2h_bytes_per_step": V * 8 + 4},

@@ -25,7 +25,7 @@ __all__ = ["Context", "DmtzError", "Opts", "Report", "cell_counts", "load_librar
 _lib = None
 
 STATUS = {0: "OK", 1: "ERR_CUDA", 2: "ERR_ARG", 3: "ERR_IO", 4: "ERR_NONCONVERGED", 5: "ERR_CYCLE",
-          6: "ERR_BOUND", 7: "ERR_UNSUPPORTED", 8: "ERR_OOB"}
+          6: "ERR_BOUND", 7: "ERR_UNSUPPORTED", 8: "ERR_OOB", 9: "ERR_TOO_LARGE"}
 
 
 class DmtzError(RuntimeError):
@@ -45,13 +45,16 @@ class Report(ctypes.Structure):
                 ("initial_mismatch", ctypes.c_int64 * 4), ("final_mismatch", ctypes.c_int64 * 4),
                 ("final_paths", ctypes.c_int64 * 2), ("edited_vertices", ctypes.c_int64),
                 ("converged", ctypes.c_int32), ("error_flags", ctypes.c_int32), ("seconds", ctypes.c_double),
-                ("kernel_launches", ctypes.c_int64)]
+                ("kernel_launches", ctypes.c_int64), ("phase_ms", ctypes.c_double * 6)]
+
+    PHASES = ("pairing", "fix_cp", "path_detect", "fix_path", "apply", "setup")
 
     def as_dict(self):
         return dict(outer_iterations=self.outer_iterations, cp_rounds=self.cp_rounds, path_rounds=self.path_rounds,
                     initial_mismatch=list(self.initial_mismatch), final_mismatch=list(self.final_mismatch),
                     final_paths=list(self.final_paths), converged=bool(self.converged),
-                    error_flags=self.error_flags, seconds=self.seconds, kernel_launches=self.kernel_launches)
+                    error_flags=self.error_flags, seconds=self.seconds, kernel_launches=self.kernel_launches,
+                    phase_ms=dict(zip(self.PHASES, [round(x, 4) for x in self.phase_ms])))
 
 
 _i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")

@@ -52,8 +52,10 @@ __global__ void k_crit(Grid g, FieldState s, const uint32_t *crit_o, Lists L, in
     const i64 v = v0 + t;
     int x, y, z;
     decode_v(g, v, x, y, z);
-    const uint32_t m = crit_mask(g, s, v, x, y, z);
+    uint32_t tc;
+    const uint32_t m = crit_mask(g, s, v, x, y, z, &tc);
     s.crit[v] = m;
+    if (s.tcode) s.tcode[v] = tc;
     if (!crit_o) return;
     uint32_t d = m ^ crit_o[v];
     if (!want_saddles) d &= 1u | (0x3Fu << 20);
@@ -150,30 +152,93 @@ struct PathRec {
     unsigned long long *n;  // [0] ascending, [1] descending
 };
 
-// get_false_as_vpath (main_3d.cu:4540-4610): per original 2-saddle triangle,
-// the first coface (search order) whose ascending path meets a difference
-__global__ void k_path_as(RuleCtx c, PathRec R, i64 cap) {
-    const Grid &g = c.g;
-    for (i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x; v < g.V; v += (i64)gridDim.x * blockDim.x) {
-        uint32_t m = (c.P.crit[v] >> 8) & 0xFFFu;
-        if (!m) continue;
+// Original ascending paths (is_false, main_3d.cu:4437-4497) step from a
+// tetrahedron through the facet it is paired with to that facet's other
+// coface.  The original gradient is fixed during a correction, so each
+// tetrahedron's successor is computed once and stored in one byte: the
+// successor's anchor offset ((dx+1) + 3(dy+1) + 9(dz+1), each in -1..1) times
+// 6 plus its slot; 255 = the path ends (boundary facet).  The reference's
+// back-pointer test on the way is always true for a consistent gradient.
+__global__ void k_path_succ(Grid g, const uint32_t *tcodeP, uint8_t *succ) {
+    i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= g.V) return;
+    int x, y, z;
+    decode_v(g, v, x, y, z);
+    const bool cube = cell_ok(g, x, y, z, 1, 1, 1);
+    const uint32_t tc = tcodeP[v];
+    for (int ts = 0; ts < 6; ts++) {
+        uint8_t out = 255;
+        const int j = (tc >> (3 * ts)) & 7;
+        if (cube && j != 7) {
+            const signed char *tf = TOPO_TET_FACE[ts][j];
+            const int fs = tf[3], other = 1 - tf[4];
+            if (other < TOPO_FACE_NCOF[fs]) {
+                const signed char *oc = TOPO_FACE_COF[fs][other];
+                const int dx = tf[0] + oc[0], dy = tf[1] + oc[1], dz = tf[2] + oc[2];
+                if (cell_ok(g, x + dx, y + dy, z + dz, 1, 1, 1))
+                    out = (uint8_t)(((dx + 1) + 3 * (dy + 1) + 9 * (dz + 1)) * 6 + oc[3]);
+            }
+        }
+        succ[v * 6 + ts] = out;
+    }
+}
+
+// compact list of the original 2-saddle triangles (anchor * 12 + slot)
+__global__ void k_sad2_list(Grid g, const uint32_t *critP, i64 *list, unsigned long long *n) {
+    i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= g.V) return;
+    uint32_t m = (critP[v] >> 8) & 0xFFFu;
+    while (m) {
+        const int sl = __ffs(m) - 1;
+        m &= m - 1;
+        list[atomicAdd(n, 1ull)] = v * 12 + sl;
+    }
+}
+
+// get_false_as_vpath (main_3d.cu:4540-4610) with is_false: for each original
+// 2-saddle triangle, its cofaces in search order; along each one's original
+// ascending path, the first tetrahedron whose decompressed pairing differs is
+// recorded, for the first coface that has one.
+__global__ void k_path_as(Grid g, const i64 *sad2, const unsigned long long *nsad, const uint32_t *tcP,
+                          const uint32_t *tcQ, const uint8_t *succ, PathRec R, i64 cap, int *err) {
+    const i64 n = (i64)*nsad;
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+        const i64 code = sad2[i];
+        const i64 v = code / 12;
+        const int sl = (int)(code % 12);
         int x, y, z;
         decode_v(g, v, x, y, z);
-        while (m) {
-            const int sl = __ffs(m) - 1;
-            m &= m - 1;
-            const i64 face = face_ref(g, x, y, z, sl);
-            i64 cof[2];
-            const int nc = face_cofaces(g, face, cof);
-            for (int j = 0; j < nc; j++) {
-                i64 rec;
-                if (walk_ascending(c, cof[j], rec, cap)) {
+        for (int j = 0; j < TOPO_FACE_NCOF[sl]; j++) {
+            const signed char *tc = TOPO_FACE_COF[sl][j];
+            int cx = x + tc[0], cy = y + tc[1], cz = z + tc[2], cs = tc[3];
+            if (!cell_ok(g, cx, cy, cz, 1, 1, 1)) continue;
+            const int sx = cx, sy = cy, sz = cz, ss = cs;
+            bool found = false;
+            i64 steps = 0;
+            while (true) {
+                const i64 ci = cx + (i64)cy * g.W + (i64)cz * g.WH;
+                const int p = (tcP[ci] >> (3 * cs)) & 7;
+                if (p == 7) break;  // an original maximum ends the path
+                if (p != (int)((tcQ[ci] >> (3 * cs)) & 7)) {
                     const unsigned long long at = atomicAdd(&R.n[0], 1ull);
-                    R.as_tet[at] = cof[j];
-                    R.as_cur[at] = rec;
+                    R.as_tet[at] = tet_ref(g, sx, sy, sz, ss);
+                    R.as_cur[at] = tet_ref(g, cx, cy, cz, cs);
+                    found = true;
+                    break;
+                }
+                const int s8 = succ[ci * 6 + cs];
+                if (s8 == 255) break;
+                const int d = s8 / 6;
+                cs = s8 - 6 * d;
+                cx += d % 3 - 1;
+                cy += (d / 3) % 3 - 1;
+                cz += d / 9 - 1;
+                if (++steps > cap) {
+                    atomicOr(err, ERR_WALK);
                     break;
                 }
             }
+            if (found) break;
         }
     }
 }
@@ -318,6 +383,7 @@ struct DevField {
     uint32_t *eup = nullptr;
     uint32_t *fup = nullptr;
     uint32_t *crit = nullptr;
+    uint32_t *tcode = nullptr;
 };
 
 struct dmtz_ctx {
@@ -333,7 +399,10 @@ struct dmtz_ctx {
     i64 *reqlist = nullptr;
     i64 *lists[4] = {nullptr, nullptr, nullptr, nullptr};
     i64 *as_tet = nullptr, *as_cur = nullptr, *ds_edge = nullptr, *ds_vert = nullptr;
-    unsigned long long *counters = nullptr;  // [0..3] cp lists, [4] requests, [5,6] paths, [8,9] min/max keys
+    uint8_t *succ = nullptr;  // original ascending-path successor of each tetrahedron
+    i64 *sad2 = nullptr;      // original 2-saddle triangles
+    unsigned long long *counters = nullptr;  // [0..3] cp lists, [4] requests, [5,6] paths, [8,9] min/max
+                                             // keys, [10] original 2-saddles
     int *errword = nullptr;
     uint8_t *changed = nullptr;
     int64_t launches = 0;  // kernels launched by the current call
@@ -358,7 +427,7 @@ cudaError_t dalloc(T **p, i64 n) {
 
 void free_field(DevField &d) {
     cudaFree(d.key); cudaFree(d.low); cudaFree(d.pv); cudaFree(d.ea2); cudaFree(d.fp3);
-    cudaFree(d.fa3); cudaFree(d.eup); cudaFree(d.fup); cudaFree(d.crit);
+    cudaFree(d.fa3); cudaFree(d.eup); cudaFree(d.fup); cudaFree(d.crit); cudaFree(d.tcode);
     d = DevField();
 }
 void free_all(dmtz_ctx *c) {
@@ -367,6 +436,8 @@ void free_all(dmtz_ctx *c) {
     for (auto &l : c->lists) { cudaFree(l); l = nullptr; }
     cudaFree(c->as_tet); cudaFree(c->as_cur); cudaFree(c->ds_edge); cudaFree(c->ds_vert);
     cudaFree(c->counters); cudaFree(c->errword); cudaFree(c->changed);
+    cudaFree(c->succ); cudaFree(c->sad2);
+    c->succ = nullptr; c->sad2 = nullptr;
     c->f = c->g = nullptr; c->cnt = nullptr; c->reqbits = nullptr; c->reqlist = nullptr;
     c->as_tet = c->as_cur = c->ds_edge = c->ds_vert = nullptr; c->counters = nullptr;
     c->errword = nullptr; c->changed = nullptr;
@@ -376,7 +447,7 @@ void free_all(dmtz_ctx *c) {
 dmtz_status alloc_field(dmtz_ctx *ctx, DevField &d, i64 V) {
     CK(dalloc(&d.key, V)); CK(dalloc(&d.low, V)); CK(dalloc(&d.pv, V)); CK(dalloc(&d.ea2, V));
     CK(dalloc(&d.fp3, V)); CK(dalloc(&d.fa3, V)); CK(dalloc(&d.eup, V)); CK(dalloc(&d.fup, V));
-    CK(dalloc(&d.crit, V));
+    CK(dalloc(&d.crit, V)); CK(dalloc(&d.tcode, V));
     return DMTZ_OK;
 }
 
@@ -396,6 +467,7 @@ dmtz_status ensure(dmtz_ctx *ctx, const Grid &g) {
     CK(dalloc(&ctx->lists[2], g.F)); CK(dalloc(&ctx->lists[3], g.T));
     CK(dalloc(&ctx->as_tet, g.F)); CK(dalloc(&ctx->as_cur, g.F));
     CK(dalloc(&ctx->ds_edge, g.E)); CK(dalloc(&ctx->ds_vert, g.E));
+    CK(dalloc(&ctx->succ, 6 * V)); CK(dalloc(&ctx->sad2, g.F));
     CK(dalloc(&ctx->counters, 16)); CK(dalloc(&ctx->errword, 1)); CK(dalloc(&ctx->changed, V));
     ctx->capV = g.V; ctx->capE = g.E; ctx->capF = g.F; ctx->capT = g.T;
     return DMTZ_OK;
@@ -404,7 +476,7 @@ dmtz_status ensure(dmtz_ctx *ctx, const Grid &g) {
 FieldState view(const DevField &d, const double *val) {
     FieldState s;
     s.val = val; s.key = d.key; s.low = d.low; s.pv = d.pv; s.ea2 = d.ea2; s.fp3 = d.fp3;
-    s.fa3 = d.fa3; s.eup = d.eup; s.fup = d.fup; s.crit = d.crit;
+    s.fa3 = d.fa3; s.eup = d.eup; s.fup = d.fup; s.crit = d.crit; s.tcode = d.tcode;
     return s;
 }
 
@@ -463,6 +535,23 @@ RuleCtx rule_ctx(dmtz_ctx *ctx, const Grid &g, double bound, int edit_type) {
     c.reqcap = g.V;
     c.err = ctx->errword;
     return c;
+}
+
+// static data of the original ascending paths (after the original pairing)
+void prep_paths(dmtz_ctx *ctx, const Grid &g) {
+    cudaMemsetAsync(ctx->counters + 10, 0, sizeof(unsigned long long), ctx->stream);
+    k_path_succ<<<grid_for(g.V), kBlock, 0, ctx->stream>>>(g, ctx->P.tcode, ctx->succ);
+    k_sad2_list<<<grid_for(g.V), kBlock, 0, ctx->stream>>>(g, ctx->P.crit, ctx->sad2, ctx->counters + 10);
+    ctx->launches += 2;
+}
+
+// separatrix detection (ascending and descending) into the path records
+void detect_paths(dmtz_ctx *ctx, const Grid &g, const RuleCtx &rc, const PathRec &R, unsigned grid) {
+    cudaMemsetAsync(ctx->counters + 5, 0, 2 * sizeof(unsigned long long), ctx->stream);
+    k_path_as<<<grid, kBlock, 0, ctx->stream>>>(g, ctx->sad2, ctx->counters + 10, ctx->P.tcode, ctx->Q.tcode,
+                                                  ctx->succ, R, g.T + 16, ctx->errword);
+    k_path_ds<<<grid, kBlock, 0, ctx->stream>>>(rc, R);
+    ctx->launches += 2;
 }
 
 unsigned persistent_grid() {
@@ -641,12 +730,11 @@ dmtz_status dmtz_path_detect(dmtz_ctx *ctx, int W, int H, int D, const double *o
     if (s != DMTZ_OK) return s;
     CK(cudaSetDevice(ctx->device));
     if ((s = setup_pair(ctx, g, orig, decp)) != DMTZ_OK) return s;
-    CK(cudaMemsetAsync(ctx->counters + 5, 0, 2 * sizeof(unsigned long long), ctx->stream));
     CK(cudaMemsetAsync(ctx->errword, 0, sizeof(int), ctx->stream));
     RuleCtx rc = rule_ctx(ctx, g, 0.0, 0);
     PathRec R{ctx->as_tet, ctx->as_cur, ctx->ds_edge, ctx->ds_vert, ctx->counters + 5};
-    k_path_as<<<persistent_grid(), kBlock, 0, ctx->stream>>>(rc, R, g.T + 16);
-    k_path_ds<<<persistent_grid(), kBlock, 0, ctx->stream>>>(rc, R);
+    prep_paths(ctx, g);
+    detect_paths(ctx, g, rc, R, persistent_grid());
     unsigned long long hc[2];
     CK(cudaMemcpyAsync(hc, ctx->counters + 5, sizeof(hc), cudaMemcpyDeviceToHost, ctx->stream));
     int err = 0;
@@ -675,6 +763,43 @@ dmtz_status dmtz_path_detect(dmtz_ctx *ctx, int W, int H, int D, const double *o
     return DMTZ_OK;
 }
 
+// ----------------------------------------------------------------------------- phase timers
+namespace {
+enum { PH_PAIR = 0, PH_FIXCP, PH_PATH, PH_FIXPATH, PH_APPLY, PH_SETUP, PH_N };
+// event pairs recorded on the context's stream around each phase; summed once
+// the stream has finished
+struct PhaseTimer {
+    cudaStream_t st;
+    std::vector<cudaEvent_t> pool;
+    std::vector<std::pair<int, size_t>> marks;  // phase, index of its first event
+    size_t used = 0;
+    cudaEvent_t next() {
+        if (used == pool.size()) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            pool.push_back(e);
+        }
+        return pool[used++];
+    }
+    void begin(int ph) {
+        marks.push_back({ph, used});
+        cudaEventRecord(next(), st);
+    }
+    void end() { cudaEventRecord(next(), st); }
+    void sum(double out[PH_N]) {
+        for (int k = 0; k < PH_N; k++) out[k] = 0;
+        for (auto &m : marks) {
+            float t = 0;
+            cudaEventElapsedTime(&t, pool[m.second], pool[m.second + 1]);
+            out[m.first] += t;
+        }
+    }
+    ~PhaseTimer() {
+        for (auto e : pool) cudaEventDestroy(e);
+    }
+};
+}  // namespace
+
 // ----------------------------------------------------------------------------- the correction loop
 dmtz_status dmtz_correct(dmtz_ctx *ctx, int W, int H, int D, const double *orig, double *decp, int on_device,
                          double rel_eps, const dmtz_opts *opts, dmtz_report *rep, int32_t *edit_counter_out) {
@@ -700,7 +825,9 @@ dmtz_status dmtz_correct(dmtz_ctx *ctx, int W, int H, int D, const double *orig,
     // range and bound exactly as the reference computes them (main_3d.cu:6303-6323)
     double mn, mx;
     ctx->launches = 0;
+    PhaseTimer pt_{st};
     CK(cudaEventRecord(e0, st));
+    pt_.begin(PH_SETUP);
     if ((s = device_minmax(ctx, ctx->f, g.V, mn, mx)) != DMTZ_OK) return s;
     const double bound = (mx - mn) * rel_eps;
     const double range = mx - mn;
@@ -709,6 +836,7 @@ dmtz_status dmtz_correct(dmtz_ctx *ctx, int W, int H, int D, const double *orig,
     CK(cudaMemsetAsync(ctx->counters, 0, 8 * sizeof(unsigned long long), st));
     const FieldState Ps = view(ctx->P, ctx->f), Qs = view(ctx->Q, ctx->g);
     run_pairing(ctx, g, Ps, nullptr, 1);
+    if (pvp == 1) prep_paths(ctx, g);
     if (filt == 1) {
         k_filter<<<grid_for(g.V), kBlock, 0, st>>>(g, ctx->P.crit, ctx->f, ctx->g, bound);
         ctx->launches++;
@@ -716,6 +844,7 @@ dmtz_status dmtz_correct(dmtz_ctx *ctx, int W, int H, int D, const double *orig,
     run_pairing(ctx, g, Qs, ctx->P.crit, 1);
     k_fill_i32<<<grid_for(g.V), kBlock, 0, st>>>(ctx->cnt, 1, g.V);
     ctx->launches++;
+    pt_.end();
     unsigned long long hc[8];
     auto read_counts = [&]() -> dmtz_status {
         CK(cudaMemcpyAsync(hc, ctx->counters, sizeof(hc), cudaMemcpyDeviceToHost, st));
@@ -748,10 +877,16 @@ dmtz_status dmtz_correct(dmtz_ctx *ctx, int W, int H, int D, const double *orig,
             rounds++;
             R.cp_rounds++;
             CK(cudaMemsetAsync(ctx->counters + 4, 0, sizeof(unsigned long long), st));
+            pt_.begin(PH_FIXCP);
             k_fix_cp<<<pgrid, kBlock, 0, st>>>(rc, L, ps);
+            pt_.end();
+            pt_.begin(PH_APPLY);
             k_apply<<<pgrid, kBlock, 0, st>>>(rc, range, pt, 1, ctx->changed, nullptr);
+            pt_.end();
             ctx->launches += 2;
+            pt_.begin(PH_PAIR);
             run_pairing(ctx, g, Qs, ctx->P.crit, ps == 1);
+            pt_.end();
             if ((s = read_counts()) != DMTZ_OK) return s;
             for (int k = 0; k < 4; k++) cc[k] = (i64)hc[k];
         }
@@ -763,22 +898,27 @@ dmtz_status dmtz_correct(dmtz_ctx *ctx, int W, int H, int D, const double *orig,
         // separatrix phase (main_3d.cu:6943-7148)
         rounds++;
         R.path_rounds++;
-        CK(cudaMemsetAsync(ctx->counters + 5, 0, 2 * sizeof(unsigned long long), st));
-        k_path_as<<<pgrid, kBlock, 0, st>>>(rc, PR, g.T + 16);
-        k_path_ds<<<pgrid, kBlock, 0, st>>>(rc, PR);
+        pt_.begin(PH_PATH);
+        detect_paths(ctx, g, rc, PR, pgrid);
+        pt_.end();
         CK(cudaMemsetAsync(ctx->counters + 4, 0, sizeof(unsigned long long), st));
+        pt_.begin(PH_FIXPATH);
         k_fix_path<<<pgrid, kBlock, 0, st>>>(rc, PR);
+        pt_.end();
+        pt_.begin(PH_APPLY);
         k_apply<<<pgrid, kBlock, 0, st>>>(rc, range, pt, 1, ctx->changed, nullptr);
-        ctx->launches += 4;
+        pt_.end();
+        ctx->launches += 2;
+        pt_.begin(PH_PAIR);
         run_pairing(ctx, g, Qs, ctx->P.crit, 1);
+        pt_.end();
         if ((s = read_counts()) != DMTZ_OK) return s;
         for (int k = 0; k < 4; k++) cc[k] = (i64)hc[k];
         n_as = n_ds = n_wall = 0;
         if (!cp_any()) {
-            CK(cudaMemsetAsync(ctx->counters + 5, 0, 2 * sizeof(unsigned long long), st));
-            k_path_as<<<pgrid, kBlock, 0, st>>>(rc, PR, g.T + 16);
-            k_path_ds<<<pgrid, kBlock, 0, st>>>(rc, PR);
-            ctx->launches += 2;
+            pt_.begin(PH_PATH);
+            detect_paths(ctx, g, rc, PR, pgrid);
+            pt_.end();
             if ((s = read_counts()) != DMTZ_OK) return s;
             n_as = (i64)hc[5];
             n_ds = (i64)hc[6];
@@ -804,6 +944,7 @@ dmtz_status dmtz_correct(dmtz_ctx *ctx, int W, int H, int D, const double *orig,
     R.error_flags = err;
     R.seconds = ms * 1e-3;
     R.kernel_launches = ctx->launches;
+    pt_.sum(R.phase_ms);
     if (rep) *rep = R;
     if (err & ERR_OOB) return fail(ctx, DMTZ_ERR_OOB, "a fix rule indexed out of range");
     if (err & ERR_WALK) return fail(ctx, DMTZ_ERR_CYCLE, "ascending path walk exceeded its step cap");
@@ -933,6 +1074,7 @@ extern "C" dmtz_status dmtz_extract_noalloc(int W, int H, int D, const double *d
     s.eup = (uint32_t *)(base + kNaEup);
     s.fup = (uint32_t *)(base + kNaFup);
     s.crit = (uint32_t *)(base + kNaCrit);
+    s.tcode = nullptr;
     cudaStream_t st = (cudaStream_t)stream;
     const unsigned gr = grid_for(g.V);
     k_pass_vertex<<<gr, kBlock, 0, st>>>(g, s, 0, g.V);

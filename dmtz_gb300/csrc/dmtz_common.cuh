@@ -186,6 +186,8 @@ struct FieldState {
     uint32_t *eup;       // final edge -> triangle
     uint32_t *fup;       // final triangle -> tetrahedron
     uint32_t *crit;      // bit 0 vertex, 1..7 edges, 8..19 triangles, 20..25 tetrahedra
+    uint32_t *tcode;     // 6 x 3 bits: which facet (TOPO_TET_FACE order) each tetrahedron
+                         // is paired with, 7 = unpaired or absent (may be null)
 };
 
 }  // namespace dmtz

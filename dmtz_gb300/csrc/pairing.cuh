@@ -299,8 +299,10 @@ __global__ void k_pass_face_a5(Grid g, FieldState s, i64 v0, i64 n) {
     s.fup[v] = out;
 }
 
-// Critical cells of one anchor (unpaired cells), bit layout of FieldState::crit.
-__device__ __forceinline__ uint32_t crit_mask(const Grid &g, const FieldState &s, i64 v, int x, int y, int z) {
+// Critical cells of one anchor (unpaired cells), bit layout of FieldState::crit;
+// *tc receives the tetrahedra's pairing codes (FieldState::tcode).
+__device__ __forceinline__ uint32_t crit_mask(const Grid &g, const FieldState &s, i64 v, int x, int y, int z,
+                                              uint32_t *tc) {
     uint32_t m = 0;
     if (s.pv[v] == 15) m |= 1u;
     const uint32_t eu = s.eup[v];
@@ -328,17 +330,20 @@ __device__ __forceinline__ uint32_t crit_mask(const Grid &g, const FieldState &s
         }
         if (!pe) m |= 1u << (8 + sl);
     }
+    uint32_t code = 0x3FFFFu;  // all seven
     if (cell_ok(g, x, y, z, 1, 1, 1)) {
         for (int ts = 0; ts < 6; ts++) {
-            bool pf = false;
+            int pj = 7;
             for (int j = 0; j < 4; j++) {
                 const signed char *tf = TOPO_TET_FACE[ts][j];
                 const i64 fa = v + tf[0] + (i64)tf[1] * g.W + (i64)tf[2] * g.WH;
-                if (fup_get(s.fup[fa], tf[3]) == tf[4] + 1) pf = true;
+                if (fup_get(s.fup[fa], tf[3]) == tf[4] + 1) pj = j;
             }
-            if (!pf) m |= 1u << (20 + ts);
+            if (pj == 7) m |= 1u << (20 + ts);
+            code = (code & ~(7u << (3 * ts))) | ((uint32_t)pj << (3 * ts));
         }
     }
+    *tc = code;
     return m;
 }
 

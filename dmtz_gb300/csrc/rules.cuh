@@ -694,34 +694,6 @@ __device__ inline int face_cofaces(const Grid &g, i64 t, i64 out[2]) {
     return n;
 }
 
-// is_false (main_3d.cu:4437-4497): walk the ORIGINAL ascending path from tet
-// `id`; returns true and the first tet whose decompressed pairing differs
-__device__ inline bool walk_ascending(const RuleCtx &c, i64 id, i64 &rec, i64 cap) {
-    i64 cur = id, old;
-    i64 steps = 0;
-    do {
-        old = cur;
-        const i64 t = pt_ref(c, c.P, cur);
-        if (t == -1) break;
-        const i64 dt = pt_ref(c, c.Q, cur);
-        if (t != dt) {
-            rec = cur;
-            return true;
-        }
-        const i64 pft = pf_ref(c, c.P, t);
-        if (pft == -1 || pt_ref(c, c.P, pft) != t) break;
-        i64 cof[2] = {-1, -1};
-        const int n = face_cofaces(c.g, t, cof);
-        const i64 t1 = cof[0], t2 = n >= 2 ? cof[1] : -1;
-        cur = t1 == cur ? t2 : t1;
-        if (++steps > cap) {
-            atomicOr(c.err, ERR_WALK);
-            break;
-        }
-    } while (cur != old && cur != -1);
-    return false;
-}
-
 // --------------------------------------------------------------- A15 fix_as_vpath (type 2)
 __device__ inline void rule_as_path(const RuleCtx &c, i64 t_idx) {
     const Grid &G = c.g;

@@ -73,6 +73,10 @@ typedef struct {
     double seconds;             /* device time of the whole correction (CUDA events
                                    on the context's stream, inputs already on the device) */
     int64_t kernel_launches;    /* kernels this call launched */
+    double phase_ms[6];         /* device time per phase, as the reference's timers
+                                   (main_3d.cu:6419-6436): gradient pairing + mismatch
+                                   detection, critical-point fixes, separatrix detection,
+                                   separatrix fixes, value update, set-up */
 } dmtz_report;
 
 /* Context: owns the device, a stream and all scratch memory.
