@@ -279,6 +279,20 @@ def run_ours(args, rank, world, local_rank):
         dist.destroy_process_group()
 
 
+def sweep_only(size: int):
+    """Gradient sweep kernels alone (for kernel profilers): 3 timed sweeps."""
+    import torch
+
+    import dmtz_gb300 as dm
+
+    f, g = workload(0, size)
+    ctx = dm.Context(0)
+    fd, gd = torch.from_numpy(f).cuda(), torch.from_numpy(g).cuda()
+    ms = ctx.profile_sweep(fd.data_ptr(), gd.data_ptr(), (size, size, size), reps=3, on_device=True)
+    print(json.dumps({"size": size, "per_kernel_ms": [round(x, 4) for x in ms[:6]], "sweep_ms": ms[6]}))
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -286,7 +300,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--sweep-only", type=int, default=0, metavar="SIZE",
+                    help="profiling aid: only time the gradient sweep on a SIZE^3 field of the same kind")
     args = ap.parse_args()
+    if args.sweep_only:
+        sweep_only(args.sweep_only)
+        return
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", args.gpus if args.gpus == 1 else 1))
     local_rank = int(os.environ.get("LOCAL_RANK", 0))

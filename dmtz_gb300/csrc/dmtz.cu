@@ -44,28 +44,53 @@ __device__ __forceinline__ void push_list(const Lists &L, int k, i64 id) {
     L.l[k][at] = id;
 }
 
-// criticality of g's gradient; mismatch against the original's criticality
-// (get_false_minimum / saddle / 2_saddle / maximum, main_3d.cu:2492-2550)
-__global__ void k_crit(Grid g, FieldState s, const uint32_t *crit_o, Lists L, int want_saddles, i64 v0, i64 n) {
-    i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
-    const i64 v = v0 + t;
-    int x, y, z;
-    decode_v(g, v, x, y, z);
-    uint32_t tc;
-    const uint32_t m = crit_mask(g, s, v, x, y, z, &tc);
-    s.crit[v] = m;
-    if (s.tcode) s.tcode[v] = tc;
-    if (!crit_o) return;
-    uint32_t d = m ^ crit_o[v];
-    if (!want_saddles) d &= 1u | (0x3Fu << 20);
-    while (d) {
-        const int b = __ffs(d) - 1;
-        d &= d - 1;
-        if (b == 0) push_list(L, 0, v);
-        else if (b < 8) push_list(L, 1, edge_ref(g, x, y, z, b - 1));
-        else if (b < 20) push_list(L, 2, face_ref(g, x, y, z, b - 8));
-        else push_list(L, 3, tet_ref(g, x, y, z, b - 20));
+// mismatch between the decompressed and the original critical cells
+// (get_false_minimum / saddle / 2_saddle / maximum, main_3d.cu:2492-2550):
+// a scan of the two criticality masks, compacting mismatched cells' ids
+__global__ void k_mismatch_scan(Grid g, const uint32_t *crit_d, const uint32_t *crit_o, Lists L, int want_saddles) {
+    for (i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x; v < g.V; v += (i64)gridDim.x * blockDim.x) {
+        uint32_t d = crit_d[v] ^ crit_o[v];
+        if (!want_saddles) d &= 1u | (0x3Fu << 20);
+        if (!d) continue;
+        int x, y, z;
+        decode_v(g, v, x, y, z);
+        while (d) {
+            const int b = __ffs(d) - 1;
+            d &= d - 1;
+            if (b == 0) push_list(L, 0, v);
+            else if (b < 8) push_list(L, 1, edge_ref(g, x, y, z, b - 1));
+            else if (b < 20) push_list(L, 2, face_ref(g, x, y, z, b - 8));
+            else push_list(L, 3, tet_ref(g, x, y, z, b - 20));
+        }
+    }
+}
+
+// bricks whose anchors lie within 5 anchors of a changed vertex: the gradient
+// state of an anchor depends on values no further away (vertex pass +-1, edge
+// pass +-2, first triangle pass -3..2, second edge pass +-3, second triangle
+// pass +-4, criticality -5..4)
+__global__ void k_mark_dirty(Grid g, int nbx, int nby, int nbz, const i64 *verts, const unsigned long long *nverts,
+                             uint8_t *flags) {
+    const i64 n = (i64)*nverts;
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+        int x, y, z;
+        decode_v(g, verts[i], x, y, z);
+        const int x0 = max(x - 5, 0) / DMTZ_BX, x1 = min(x + 5, g.W - 1) / DMTZ_BX;
+        const int y0 = max(y - 5, 0) / DMTZ_BY, y1 = min(y + 5, g.H - 1) / DMTZ_BY;
+        const int z0 = max(z - 5, 0) / DMTZ_BZ, z1 = min(z + 5, g.D - 1) / DMTZ_BZ;
+        for (int bz = z0; bz <= z1; bz++)
+            for (int by = y0; by <= y1; by++)
+                for (int bx = x0; bx <= x1; bx++) flags[bx + (i64)nbx * (by + (i64)nby * bz)] = 1;
+    }
+}
+
+__global__ void k_compact_bricks(int nbx, int nby, int nbz, uint8_t *flags, uint32_t *list, unsigned long long *n) {
+    const i64 nb = (i64)nbx * nby * nbz;
+    for (i64 b = (i64)blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += (i64)gridDim.x * blockDim.x) {
+        if (!flags[b]) continue;
+        flags[b] = 0;
+        const int bx = (int)(b % nbx), by = (int)((b / nbx) % nby), bz = (int)(b / ((i64)nbx * nby));
+        list[atomicAdd(n, 1ull)] = (uint32_t)bx | ((uint32_t)by << 11) | ((uint32_t)bz << 22);
     }
 }
 
@@ -391,7 +416,7 @@ struct dmtz_ctx {
     cudaStream_t stream = nullptr;
     std::string err;
     // sized buffers
-    i64 capV = 0, capE = 0, capF = 0, capT = 0;
+    i64 capV = 0, capE = 0, capF = 0, capT = 0, capB = 0;
     double *f = nullptr, *g = nullptr;
     DevField P, Q;
     int *cnt = nullptr;
@@ -400,9 +425,11 @@ struct dmtz_ctx {
     i64 *lists[4] = {nullptr, nullptr, nullptr, nullptr};
     i64 *as_tet = nullptr, *as_cur = nullptr, *ds_edge = nullptr, *ds_vert = nullptr;
     uint8_t *succ = nullptr;  // original ascending-path successor of each tetrahedron
+    uint8_t *brick_flags = nullptr;   // bricks to re-pair in the next sweep
+    uint32_t *brick_list = nullptr;   // their compacted list (counters[11])
     i64 *sad2 = nullptr;      // original 2-saddle triangles
     unsigned long long *counters = nullptr;  // [0..3] cp lists, [4] requests, [5,6] paths, [8,9] min/max
-                                             // keys, [10] original 2-saddles
+                                             // keys, [10] original 2-saddles, [11] dirty bricks
     int *errword = nullptr;
     uint8_t *changed = nullptr;
     int64_t launches = 0;  // kernels launched by the current call
@@ -436,12 +463,12 @@ void free_all(dmtz_ctx *c) {
     for (auto &l : c->lists) { cudaFree(l); l = nullptr; }
     cudaFree(c->as_tet); cudaFree(c->as_cur); cudaFree(c->ds_edge); cudaFree(c->ds_vert);
     cudaFree(c->counters); cudaFree(c->errword); cudaFree(c->changed);
-    cudaFree(c->succ); cudaFree(c->sad2);
-    c->succ = nullptr; c->sad2 = nullptr;
+    cudaFree(c->succ); cudaFree(c->sad2); cudaFree(c->brick_flags); cudaFree(c->brick_list);
+    c->succ = nullptr; c->sad2 = nullptr; c->brick_flags = nullptr; c->brick_list = nullptr;
     c->f = c->g = nullptr; c->cnt = nullptr; c->reqbits = nullptr; c->reqlist = nullptr;
     c->as_tet = c->as_cur = c->ds_edge = c->ds_vert = nullptr; c->counters = nullptr;
     c->errword = nullptr; c->changed = nullptr;
-    c->capV = c->capE = c->capF = c->capT = 0;
+    c->capV = c->capE = c->capF = c->capT = c->capB = 0;
 }
 
 dmtz_status alloc_field(dmtz_ctx *ctx, DevField &d, i64 V) {
@@ -451,8 +478,12 @@ dmtz_status alloc_field(dmtz_ctx *ctx, DevField &d, i64 V) {
     return DMTZ_OK;
 }
 
+i64 bricks_of(const Grid &g, int &nbx, int &nby, int &nbz);
+
 dmtz_status ensure(dmtz_ctx *ctx, const Grid &g) {
-    if (g.V <= ctx->capV && g.E <= ctx->capE && g.F <= ctx->capF && g.T <= ctx->capT) return DMTZ_OK;
+    int nbx, nby, nbz;
+    const i64 nbr = bricks_of(g, nbx, nby, nbz);
+    if (g.V <= ctx->capV && g.E <= ctx->capE && g.F <= ctx->capF && g.T <= ctx->capT && nbr <= ctx->capB) return DMTZ_OK;
     free_all(ctx);
     const i64 V = g.V;
     CK(dalloc(&ctx->f, V)); CK(dalloc(&ctx->g, V));
@@ -468,6 +499,9 @@ dmtz_status ensure(dmtz_ctx *ctx, const Grid &g) {
     CK(dalloc(&ctx->as_tet, g.F)); CK(dalloc(&ctx->as_cur, g.F));
     CK(dalloc(&ctx->ds_edge, g.E)); CK(dalloc(&ctx->ds_vert, g.E));
     CK(dalloc(&ctx->succ, 6 * V)); CK(dalloc(&ctx->sad2, g.F));
+    CK(dalloc(&ctx->brick_flags, nbr)); CK(dalloc(&ctx->brick_list, nbr));
+    CK(cudaMemset(ctx->brick_flags, 0, (size_t)nbr));
+    ctx->capB = nbr;
     CK(dalloc(&ctx->counters, 16)); CK(dalloc(&ctx->errword, 1)); CK(dalloc(&ctx->changed, V));
     ctx->capV = g.V; ctx->capE = g.E; ctx->capF = g.F; ctx->capT = g.T;
     return DMTZ_OK;
@@ -483,20 +517,76 @@ FieldState view(const DevField &d, const double *val) {
 unsigned persistent_grid();
 
 // five passes + criticality (and mismatch lists when crit_o is given)
-void run_pairing(dmtz_ctx *ctx, const Grid &g, const FieldState &s, const uint32_t *crit_o, int want_saddles) {
-    const unsigned gr = grid_for(g.V);
+i64 bricks_of(const Grid &g, int &nbx, int &nby, int &nbz) {
+    nbx = (g.W + DMTZ_BX - 1) / DMTZ_BX;
+    nby = (g.H + DMTZ_BY - 1) / DMTZ_BY;
+    nbz = (g.D + DMTZ_BZ - 1) / DMTZ_BZ;
+    return (i64)nbx * nby * nbz;
+}
+
+unsigned sweep_grid(i64 nb) {
+    static unsigned cap = 0;
+    if (!cap) cap = persistent_grid() * 2;  // 16 blocks of 128 threads per SM
+    return (unsigned)std::max<i64>(1, std::min<i64>(nb, cap));
+}
+
+// the five pairing passes and the criticality pass over a set of bricks
+void sweep(dmtz_ctx *ctx, const Grid &g, const FieldState &s, const BrickList &bl, i64 nb_max) {
+    const unsigned gr = sweep_grid(nb_max);
     cudaStream_t st = ctx->stream;
-    k_pass_vertex<<<gr, kBlock, 0, st>>>(g, s, 0, g.V);
-    k_pass_edge_a2<<<gr, kBlock, 0, st>>>(g, s, 0, g.V);
-    k_pass_face_a3<<<gr, kBlock, 0, st>>>(g, s, 0, g.V);
-    k_pass_edge_a4<<<gr, kBlock, 0, st>>>(g, s, 0, g.V);
-    k_pass_face_a5<<<gr, kBlock, 0, st>>>(g, s, 0, g.V);
+    k_sweep<PASS_VERTEX><<<gr, DMTZ_BRICK, 0, st>>>(g, s, bl);
+    k_sweep<PASS_E2><<<gr, DMTZ_BRICK, 0, st>>>(g, s, bl);
+    k_sweep<PASS_F3><<<gr, DMTZ_BRICK, 0, st>>>(g, s, bl);
+    k_sweep<PASS_E4><<<gr, DMTZ_BRICK, 0, st>>>(g, s, bl);
+    k_sweep<PASS_F5><<<gr, DMTZ_BRICK, 0, st>>>(g, s, bl);
+    k_sweep<PASS_CRIT><<<gr, DMTZ_BRICK, 0, st>>>(g, s, bl);
+    ctx->launches += 6;
+}
+
+BrickList all_bricks(const Grid &g, i64 &nb) {
+    BrickList bl;
+    bl.list = nullptr;
+    bl.n = nullptr;
+    nb = bricks_of(g, bl.nbx, bl.nby, bl.nbz);
+    return bl;
+}
+
+// mismatch lists of the decompressed gradient against crit_o
+void scan_mismatch(dmtz_ctx *ctx, const Grid &g, const uint32_t *crit_d, const uint32_t *crit_o, int want_saddles) {
     Lists L;
     for (int k = 0; k < 4; k++) L.l[k] = ctx->lists[k];
     L.n = ctx->counters;
-    if (crit_o) cudaMemsetAsync(ctx->counters, 0, 4 * sizeof(unsigned long long), st);
-    k_crit<<<gr, kBlock, 0, st>>>(g, s, crit_o, L, want_saddles, 0, g.V);
-    ctx->launches += 6;
+    cudaMemsetAsync(ctx->counters, 0, 4 * sizeof(unsigned long long), ctx->stream);
+    k_mismatch_scan<<<persistent_grid(), kBlock, 0, ctx->stream>>>(g, crit_d, crit_o, L, want_saddles);
+    ctx->launches++;
+}
+
+// full gradient of one field (and its mismatch lists when crit_o is given)
+void run_pairing(dmtz_ctx *ctx, const Grid &g, const FieldState &s, const uint32_t *crit_o, int want_saddles) {
+    i64 nb;
+    const BrickList bl = all_bricks(g, nb);
+    sweep(ctx, g, s, bl, nb);
+    if (crit_o) scan_mismatch(ctx, g, s.crit, crit_o, want_saddles);
+}
+
+// re-pair only the bricks near the vertices the last update requested
+// (ctx->reqlist), then rebuild the mismatch lists
+void repair_dirty(dmtz_ctx *ctx, const Grid &g, const FieldState &s, const uint32_t *crit_o, int want_saddles) {
+    int nbx, nby, nbz;
+    const i64 nb = bricks_of(g, nbx, nby, nbz);
+    cudaStream_t st = ctx->stream;
+    cudaMemsetAsync(ctx->counters + 11, 0, sizeof(unsigned long long), st);
+    k_mark_dirty<<<persistent_grid(), kBlock, 0, st>>>(g, nbx, nby, nbz, ctx->reqlist, ctx->counters + 4,
+                                                        ctx->brick_flags);
+    k_compact_bricks<<<persistent_grid(), kBlock, 0, st>>>(nbx, nby, nbz, ctx->brick_flags, ctx->brick_list,
+                                                            ctx->counters + 11);
+    ctx->launches += 2;
+    BrickList bl;
+    bl.list = ctx->brick_list;
+    bl.n = ctx->counters + 11;
+    bl.nbx = nbx; bl.nby = nby; bl.nbz = nbz;
+    sweep(ctx, g, s, bl, nb);
+    scan_mismatch(ctx, g, s.crit, crit_o, want_saddles);
 }
 
 double key_to_double(unsigned long long k) {
@@ -564,6 +654,8 @@ unsigned persistent_grid() {
 dmtz_status check_dims(dmtz_ctx *ctx, int W, int H, int D, Grid &g) {
     if (!ctx) return DMTZ_ERR_ARG;
     if (W < 2 || H < 2 || D < 2) return fail(ctx, DMTZ_ERR_ARG, "dims must be >= 2");
+    if (W > 2047 * DMTZ_BX || H > 2047 * DMTZ_BY || D > 1023 * DMTZ_BZ)
+        return fail(ctx, DMTZ_ERR_ARG, "dims exceed 16376 x 8188 x 4092");
     g = make_grid(W, H, D);
     return DMTZ_OK;
 }
@@ -885,7 +977,7 @@ dmtz_status dmtz_correct(dmtz_ctx *ctx, int W, int H, int D, const double *orig,
             pt_.end();
             ctx->launches += 2;
             pt_.begin(PH_PAIR);
-            run_pairing(ctx, g, Qs, ctx->P.crit, ps == 1);
+            repair_dirty(ctx, g, Qs, ctx->P.crit, ps == 1);
             pt_.end();
             if ((s = read_counts()) != DMTZ_OK) return s;
             for (int k = 0; k < 4; k++) cc[k] = (i64)hc[k];
@@ -910,7 +1002,7 @@ dmtz_status dmtz_correct(dmtz_ctx *ctx, int W, int H, int D, const double *orig,
         pt_.end();
         ctx->launches += 2;
         pt_.begin(PH_PAIR);
-        run_pairing(ctx, g, Qs, ctx->P.crit, 1);
+        repair_dirty(ctx, g, Qs, ctx->P.crit, 1);
         pt_.end();
         if ((s = read_counts()) != DMTZ_OK) return s;
         for (int k = 0; k < 4; k++) cc[k] = (i64)hc[k];
@@ -970,24 +1062,22 @@ dmtz_status dmtz_profile_sweep(dmtz_ctx *ctx, int W, int H, int D, const double 
     for (auto &e : ev) CK(cudaEventCreate(&e));
     double acc[6] = {0, 0, 0, 0, 0, 0};
     float total = 0;
-    Lists L;
-    for (int k = 0; k < 4; k++) L.l[k] = ctx->lists[k];
-    L.n = ctx->counters;
-    const unsigned gr = grid_for(g.V);
+    i64 nb;
+    const BrickList bl = all_bricks(g, nb);
+    const unsigned gr = sweep_grid(nb);
     for (int r = 0; r < reps; r++) {
-        CK(cudaMemsetAsync(ctx->counters, 0, 4 * sizeof(unsigned long long), st));
         CK(cudaEventRecord(ev[0], st));
-        k_pass_vertex<<<gr, kBlock, 0, st>>>(g, Qs, 0, g.V);
+        k_sweep<PASS_VERTEX><<<gr, DMTZ_BRICK, 0, st>>>(g, Qs, bl);
         CK(cudaEventRecord(ev[1], st));
-        k_pass_edge_a2<<<gr, kBlock, 0, st>>>(g, Qs, 0, g.V);
+        k_sweep<PASS_E2><<<gr, DMTZ_BRICK, 0, st>>>(g, Qs, bl);
         CK(cudaEventRecord(ev[2], st));
-        k_pass_face_a3<<<gr, kBlock, 0, st>>>(g, Qs, 0, g.V);
+        k_sweep<PASS_F3><<<gr, DMTZ_BRICK, 0, st>>>(g, Qs, bl);
         CK(cudaEventRecord(ev[3], st));
-        k_pass_edge_a4<<<gr, kBlock, 0, st>>>(g, Qs, 0, g.V);
+        k_sweep<PASS_E4><<<gr, DMTZ_BRICK, 0, st>>>(g, Qs, bl);
         CK(cudaEventRecord(ev[4], st));
-        k_pass_face_a5<<<gr, kBlock, 0, st>>>(g, Qs, 0, g.V);
+        k_sweep<PASS_F5><<<gr, DMTZ_BRICK, 0, st>>>(g, Qs, bl);
         CK(cudaEventRecord(ev[5], st));
-        k_crit<<<gr, kBlock, 0, st>>>(g, Qs, ctx->P.crit, L, 1, 0, g.V);
+        k_sweep<PASS_CRIT><<<gr, DMTZ_BRICK, 0, st>>>(g, Qs, bl);
         CK(cudaEventRecord(ev[6], st));
         CK(cudaEventSynchronize(ev[6]));
         for (int k = 0; k < 6; k++) {
@@ -1076,12 +1166,14 @@ extern "C" dmtz_status dmtz_extract_noalloc(int W, int H, int D, const double *d
     s.crit = (uint32_t *)(base + kNaCrit);
     s.tcode = nullptr;
     cudaStream_t st = (cudaStream_t)stream;
-    const unsigned gr = grid_for(g.V);
-    k_pass_vertex<<<gr, kBlock, 0, st>>>(g, s, 0, g.V);
-    k_pass_edge_a2<<<gr, kBlock, 0, st>>>(g, s, 0, g.V);
-    k_pass_face_a3<<<gr, kBlock, 0, st>>>(g, s, 0, g.V);
-    k_pass_edge_a4<<<gr, kBlock, 0, st>>>(g, s, 0, g.V);
-    k_pass_face_a5<<<gr, kBlock, 0, st>>>(g, s, 0, g.V);
-    k_export<<<gr, kBlock, 0, st>>>(g, s, PV, PE, PF, PT);
+    i64 nb;
+    const BrickList bl = all_bricks(g, nb);
+    const unsigned gb = sweep_grid(nb);
+    k_sweep<PASS_VERTEX><<<gb, DMTZ_BRICK, 0, st>>>(g, s, bl);
+    k_sweep<PASS_E2><<<gb, DMTZ_BRICK, 0, st>>>(g, s, bl);
+    k_sweep<PASS_F3><<<gb, DMTZ_BRICK, 0, st>>>(g, s, bl);
+    k_sweep<PASS_E4><<<gb, DMTZ_BRICK, 0, st>>>(g, s, bl);
+    k_sweep<PASS_F5><<<gb, DMTZ_BRICK, 0, st>>>(g, s, bl);
+    k_export<<<grid_for(g.V), kBlock, 0, st>>>(g, s, PV, PE, PF, PT);
     return cudaGetLastError() == cudaSuccess ? DMTZ_OK : DMTZ_ERR_CUDA;
 }

@@ -26,12 +26,7 @@ __device__ __forceinline__ bool key_less(uint64_t ka, i64 a, uint64_t kb, i64 b)
 }
 
 // Pass 1: order keys, lower-neighbour masks, steepest descent.
-__global__ void k_pass_vertex(Grid g, FieldState s, i64 v0, i64 n) {
-    i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
-    i64 v = v0 + t;
-    int x, y, z;
-    decode_v(g, v, x, y, z);
+__device__ __forceinline__ void pass_vertex_at(const Grid &g, const FieldState &s, i64 v, int x, int y, int z) {
     const uint64_t kv = okey(s.val[v]);
     uint64_t bk = DMTZ_KEY_DBL_MAX;
     i64 bid = -1;
@@ -73,12 +68,7 @@ __device__ __forceinline__ Corner corner_at(const Grid &g, i64 v, int x, int y, 
 __device__ __forceinline__ bool below_dir(const uint16_t *low, i64 a, int d) { return (low[a] >> d) & 1; }
 
 // Pass 2: edge -> triangle, candidates below both endpoints (a2 = 0).
-__global__ void k_pass_edge_a2(Grid g, FieldState s, i64 v0, i64 n) {
-    i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
-    i64 v = v0 + t;
-    int x, y, z;
-    decode_v(g, v, x, y, z);
+__device__ __forceinline__ void pass_edge_a2_at(const Grid &g, const FieldState &s, i64 v, int x, int y, int z) {
     uint32_t out = 0;
     for (int k = 0; k < 7; k++) {
         int mx, my, mz;
@@ -131,12 +121,7 @@ __device__ __forceinline__ void tri_order(const uint16_t *low, const Corner c[3]
 }
 
 // Pass 3: triangle -> tetrahedron, candidates below all three (a2 = 0).
-__global__ void k_pass_face_a3(Grid g, FieldState s, i64 v0, i64 n) {
-    i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
-    i64 v = v0 + t;
-    int x, y, z;
-    decode_v(g, v, x, y, z);
+__device__ __forceinline__ void pass_face_a3_at(const Grid &g, const FieldState &s, i64 v, int x, int y, int z) {
     uint32_t out = 0;
     uint32_t paired = 0;
     for (int sl = 0; sl < 12; sl++) {
@@ -184,12 +169,7 @@ __global__ void k_pass_face_a3(Grid g, FieldState s, i64 v0, i64 n) {
 
 // Pass 4: still-unpaired edges -> triangle whose third vertex lies between
 // the endpoints (a2 = 1), if that triangle is still free.
-__global__ void k_pass_edge_a4(Grid g, FieldState s, i64 v0, i64 n) {
-    i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
-    i64 v = v0 + t;
-    int x, y, z;
-    decode_v(g, v, x, y, z);
+__device__ __forceinline__ void pass_edge_a4_at(const Grid &g, const FieldState &s, i64 v, int x, int y, int z) {
     const uint32_t a2 = s.ea2[v];
     uint32_t out = a2;
     for (int k = 0; k < 7; k++) {
@@ -234,12 +214,7 @@ __global__ void k_pass_edge_a4(Grid g, FieldState s, i64 v0, i64 n) {
 
 // Pass 5: still-unpaired triangles -> tetrahedron whose fourth vertex is
 // below exactly two of the three (a2 = 1), if that tetrahedron is still free.
-__global__ void k_pass_face_a5(Grid g, FieldState s, i64 v0, i64 n) {
-    i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
-    i64 v = v0 + t;
-    int x, y, z;
-    decode_v(g, v, x, y, z);
+__device__ __forceinline__ void pass_face_a5_at(const Grid &g, const FieldState &s, i64 v, int x, int y, int z) {
     const uint32_t a3 = s.fa3[v];
     const uint32_t p3 = s.fp3[v];
     uint32_t out = a3;
@@ -345,6 +320,70 @@ __device__ __forceinline__ uint32_t crit_mask(const Grid &g, const FieldState &s
     }
     *tc = code;
     return m;
+}
+
+}  // namespace dmtz
+
+namespace dmtz {
+
+// ---------------------------------------------------------------------------
+// Brick-driven sweeps.  Anchors are grouped in bricks of 8 x 4 x 4 (x fastest,
+// one 128-thread block per brick).  A sweep runs over an explicit list of
+// bricks (packed bx | by << 11 | bz << 22) or, with list == nullptr, over all
+// bricks of the grid.  Blocks stride over the list, so the grid size does not
+// depend on its length and the length can stay on the device.
+// ---------------------------------------------------------------------------
+#define DMTZ_BX 8
+#define DMTZ_BY 4
+#define DMTZ_BZ 4
+#define DMTZ_BRICK (DMTZ_BX * DMTZ_BY * DMTZ_BZ)
+
+struct BrickList {
+    const uint32_t *list;           // packed brick coordinates, or nullptr for all bricks
+    const unsigned long long *n;    // number of listed bricks (device), when list != nullptr
+    int nbx, nby, nbz;              // bricks per axis
+};
+
+__device__ __forceinline__ i64 brick_count(const BrickList &bl) {
+    return bl.list ? (i64)*bl.n : (i64)bl.nbx * bl.nby * bl.nbz;
+}
+__device__ __forceinline__ void brick_coords(const BrickList &bl, i64 b, int &bx, int &by, int &bz) {
+    if (bl.list) {
+        const uint32_t e = bl.list[b];
+        bx = e & 0x7FF;
+        by = (e >> 11) & 0x7FF;
+        bz = e >> 22;
+    } else {
+        const int bi = (int)b;
+        bx = bi % bl.nbx;
+        by = (bi / bl.nbx) % bl.nby;
+        bz = bi / (bl.nbx * bl.nby);
+    }
+}
+
+enum { PASS_VERTEX = 0, PASS_E2, PASS_F3, PASS_E4, PASS_F5, PASS_CRIT };
+
+template <int PASS>
+__global__ void __launch_bounds__(DMTZ_BRICK) k_sweep(Grid g, FieldState s, BrickList bl) {
+    const i64 nb = brick_count(bl);
+    const int lx = threadIdx.x % DMTZ_BX, ly = (threadIdx.x / DMTZ_BX) % DMTZ_BY, lz = threadIdx.x / (DMTZ_BX * DMTZ_BY);
+    for (i64 b = blockIdx.x; b < nb; b += gridDim.x) {
+        int bx, by, bz;
+        brick_coords(bl, b, bx, by, bz);
+        const int x = bx * DMTZ_BX + lx, y = by * DMTZ_BY + ly, z = bz * DMTZ_BZ + lz;
+        if (x >= g.W || y >= g.H || z >= g.D) continue;
+        const i64 v = x + (i64)y * g.W + (i64)z * g.WH;
+        if (PASS == PASS_VERTEX) pass_vertex_at(g, s, v, x, y, z);
+        else if (PASS == PASS_E2) pass_edge_a2_at(g, s, v, x, y, z);
+        else if (PASS == PASS_F3) pass_face_a3_at(g, s, v, x, y, z);
+        else if (PASS == PASS_E4) pass_edge_a4_at(g, s, v, x, y, z);
+        else if (PASS == PASS_F5) pass_face_a5_at(g, s, v, x, y, z);
+        else {
+            uint32_t tc;
+            s.crit[v] = crit_mask(g, s, v, x, y, z, &tc);
+            if (s.tcode) s.tcode[v] = tc;
+        }
+    }
 }
 
 }  // namespace dmtz
