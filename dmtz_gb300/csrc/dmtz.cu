@@ -24,6 +24,7 @@
 #include "../../include/dmtz.h"
 #include "dmtz_common.cuh"
 #include "pairing.cuh"
+#include "pairing_fast.cuh"
 #include "rules.cuh"
 
 using namespace dmtz;

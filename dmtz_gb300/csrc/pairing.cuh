@@ -361,29 +361,4 @@ __device__ __forceinline__ void brick_coords(const BrickList &bl, i64 b, int &bx
     }
 }
 
-enum { PASS_VERTEX = 0, PASS_E2, PASS_F3, PASS_E4, PASS_F5, PASS_CRIT };
-
-template <int PASS>
-__global__ void __launch_bounds__(DMTZ_BRICK) k_sweep(Grid g, FieldState s, BrickList bl) {
-    const i64 nb = brick_count(bl);
-    const int lx = threadIdx.x % DMTZ_BX, ly = (threadIdx.x / DMTZ_BX) % DMTZ_BY, lz = threadIdx.x / (DMTZ_BX * DMTZ_BY);
-    for (i64 b = blockIdx.x; b < nb; b += gridDim.x) {
-        int bx, by, bz;
-        brick_coords(bl, b, bx, by, bz);
-        const int x = bx * DMTZ_BX + lx, y = by * DMTZ_BY + ly, z = bz * DMTZ_BZ + lz;
-        if (x >= g.W || y >= g.H || z >= g.D) continue;
-        const i64 v = x + (i64)y * g.W + (i64)z * g.WH;
-        if (PASS == PASS_VERTEX) pass_vertex_at(g, s, v, x, y, z);
-        else if (PASS == PASS_E2) pass_edge_a2_at(g, s, v, x, y, z);
-        else if (PASS == PASS_F3) pass_face_a3_at(g, s, v, x, y, z);
-        else if (PASS == PASS_E4) pass_edge_a4_at(g, s, v, x, y, z);
-        else if (PASS == PASS_F5) pass_face_a5_at(g, s, v, x, y, z);
-        else {
-            uint32_t tc;
-            s.crit[v] = crit_mask(g, s, v, x, y, z, &tc);
-            if (s.tcode) s.tcode[v] = tc;
-        }
-    }
-}
-
 }  // namespace dmtz

@@ -1,0 +1,375 @@
+// pairing_fast.cuh — interior fast path of the pairing passes.
+//
+// An anchor at 1 <= x,y,z <= dim-2 owns all 26 of its cells and every vertex
+// its passes look at (offsets -1..2) exists, so no bounds test is needed.
+// These versions unroll every loop over edge families, triangle slots and
+// cofaces at compile time: the topology tables become immediates and each
+// "is n below u" test is one shift of a 14-bit mask by a constant.  They
+// compute exactly what pass_*_at in pairing.cuh computes (same candidates,
+// same argmin rule, same free-target checks); the sweep uses them for interior
+// anchors and the generic code for the boundary layer.
+#pragma once
+#include <utility>
+
+#include "pairing.cuh"
+
+namespace dmtz {
+namespace cxt {
+#define TOPO_QUAL static constexpr
+#include "topology_tables.inc"
+#undef TOPO_QUAL
+
+__host__ __device__ constexpr int cdir(int dx, int dy, int dz) {
+    return (dx < -1 || dx > 1 || dy < -1 || dy > 1 || dz < -1 || dz > 1) ? -1
+                                                                         : TOPO_DIR_LUT[(dx + 1) + 3 * (dy + 1) + 9 * (dz + 1)];
+}
+__host__ __device__ constexpr int ccx(int c) { return c & 1; }
+__host__ __device__ constexpr int ccy(int c) { return (c >> 1) & 1; }
+__host__ __device__ constexpr int ccz(int c) { return (c >> 2) & 1; }
+// direction from corner c to offset (x, y, z), all relative to the same anchor
+__host__ __device__ constexpr int cdir_to(int c, int x, int y, int z) { return cdir(x - ccx(c), y - ccy(c), z - ccz(c)); }
+// index of the corner with offset (x,y,z) among a tet's four corners (-1 if none)
+__host__ __device__ constexpr int tet_corner_index(int ts, int x, int y, int z) {
+    return (TOPO_TET_V[ts][0] == x + 2 * y + 4 * z)   ? 0
+           : (TOPO_TET_V[ts][1] == x + 2 * y + 4 * z) ? 1
+           : (TOPO_TET_V[ts][2] == x + 2 * y + 4 * z) ? 2
+           : (TOPO_TET_V[ts][3] == x + 2 * y + 4 * z) ? 3
+                                                      : -1;
+}
+}  // namespace cxt
+
+// linear offset of a compile-time displacement
+template <int DX, int DY, int DZ>
+__device__ __forceinline__ i64 off(const Grid &g) {
+    return (i64)DX + (i64)DY * g.W + (i64)DZ * g.WH;
+}
+
+template <int... Is, class F>
+__device__ __forceinline__ void static_for(std::integer_sequence<int, Is...>, F &&f) {
+    (f(std::integral_constant<int, Is>{}), ...);
+}
+#define DMTZ_FOR(N, VAR, ...) static_for(std::make_integer_sequence<int, N>{}, [&](auto VAR) __VA_ARGS__)
+
+__device__ __forceinline__ bool bit(uint32_t m, int d) { return (m >> d) & 1u; }
+
+// ---------------------------------------------------------------- pass 1
+__device__ __forceinline__ void fast_vertex(const Grid &g, const FieldState &s, i64 v) {
+    const uint64_t kv = okey(s.val[v]);
+    uint64_t bk = DMTZ_KEY_DBL_MAX;
+    i64 bid = -1;
+    int bdir = 15;
+    uint32_t lm = 0;
+#pragma unroll
+    for (int i = 0; i < 14; i++) {
+        const i64 nb = v + g.doff[i];
+        const uint64_t kn = okey(s.val[nb]);
+        if (key_less(kn, nb, kv, v)) {
+            lm |= 1u << i;
+            if (key_less(kn, nb, bk, bid)) {
+                bk = kn;
+                bid = nb;
+                bdir = i;
+            }
+        }
+    }
+    s.key[v] = kv;
+    s.low[v] = (uint16_t)lm;
+    s.pv[v] = (uint8_t)bdir;
+}
+
+// ---------------------------------------------------------------- pass 2 / 4 (edges)
+// A2 = true: candidates below both endpoints (pass 2); false: between them (pass 4)
+template <int K, bool A2>
+__device__ __forceinline__ int fast_edge_choice(const Grid &g, const FieldState &s, i64 v, bool &claimed) {
+    constexpr int cp = cxt::TOPO_EDGE_V[K][0], cq = cxt::TOPO_EDGE_V[K][1];
+    constexpr int dpq = cxt::TOPO_CORNER_DIR[cp][cq], dqp = cxt::TOPO_CORNER_DIR[cq][cp];
+    const i64 p = v + g.coff[cp], q = v + g.coff[cq];
+    const uint32_t lp = s.low[p], lq = s.low[q];
+    const bool qb = bit(lp, dpq);  // q below p: p is the higher endpoint
+    claimed = qb ? (s.pv[p] == dpq) : (s.pv[q] == dqp);
+    if (claimed) return -1;
+    const uint32_t lhi = qb ? lp : lq, llo = qb ? lq : lp;
+    uint64_t bk = DMTZ_KEY_DBL_MAX;
+    i64 bid = INT_MAX;
+    int bj = -1;
+    DMTZ_FOR(cxt::TOPO_EDGE_NCOF[K], J, {
+        constexpr int j = decltype(J)::value;
+        constexpr int tx = cxt::TOPO_EDGE_THIRD[K][j][0], ty = cxt::TOPO_EDGE_THIRD[K][j][1],
+                      tz = cxt::TOPO_EDGE_THIRD[K][j][2];
+        constexpr int dp = cxt::cdir_to(cp, tx, ty, tz), dq = cxt::cdir_to(cq, tx, ty, tz);
+        const int dlo = qb ? dq : dp, dhi = qb ? dp : dq;
+        const bool ok = A2 ? bit(llo, dlo) : (bit(lhi, dhi) && !bit(llo, dlo));
+        if (ok) {
+            const i64 nb = v + off<tx, ty, tz>(g);
+            const uint64_t kn = s.key[nb];
+            if (key_less(kn, nb, bk, bid)) {
+                bk = kn;
+                bid = nb;
+                bj = j;
+            }
+        }
+    });
+    return bj;
+}
+
+__device__ __forceinline__ void fast_edge_a2(const Grid &g, const FieldState &s, i64 v) {
+    uint32_t out = 0;
+    DMTZ_FOR(7, K, {
+        constexpr int k = decltype(K)::value;
+        bool claimed;
+        const int bj = fast_edge_choice<k, true>(g, s, v, claimed);
+        if (bj >= 0) out |= (uint32_t)(bj + 1) << (3 * k);
+    });
+    s.ea2[v] = out;
+}
+
+// is the face (anchor offset, slot) paired after pass 3?
+template <int K, int J>
+__device__ __forceinline__ bool cof_face_paired3(const Grid &g, const FieldState &s, i64 v) {
+    constexpr int fx = cxt::TOPO_EDGE_COF[K][J][0], fy = cxt::TOPO_EDGE_COF[K][J][1],
+                  fz = cxt::TOPO_EDGE_COF[K][J][2], fs = cxt::TOPO_EDGE_COF[K][J][3];
+    return bit(s.fp3[v + off<fx, fy, fz>(g)], fs);
+}
+
+__device__ __forceinline__ void fast_edge_a4(const Grid &g, const FieldState &s, i64 v) {
+    const uint32_t a2 = s.ea2[v];
+    uint32_t out = a2;
+    DMTZ_FOR(7, K, {
+        constexpr int k = decltype(K)::value;
+        if (!eup_get(a2, k)) {
+            bool claimed;
+            const int bj = fast_edge_choice<k, false>(g, s, v, claimed);
+            if (bj >= 0) {
+                bool taken = false;
+                DMTZ_FOR(cxt::TOPO_EDGE_NCOF[k], J, {
+                    constexpr int j = decltype(J)::value;
+                    if (bj == j) taken = cof_face_paired3<k, j>(g, s, v);
+                });
+                if (!taken) out |= (uint32_t)(bj + 1) << (3 * k);
+            }
+        }
+    });
+    s.eup[v] = out;
+}
+
+// ---------------------------------------------------------------- triangles
+// value order of the triangle's corners (j = 0,1,2 by id): lowest / middle
+template <int S>
+__device__ __forceinline__ void fast_tri_order(const FieldState &s, const uint32_t l[3], int &jlo, int &jmid) {
+    constexpr int c0 = cxt::TOPO_FACE_V[S][0], c1 = cxt::TOPO_FACE_V[S][1], c2 = cxt::TOPO_FACE_V[S][2];
+    const bool b01 = bit(l[0], cxt::TOPO_CORNER_DIR[c0][c1]);
+    const bool b02 = bit(l[0], cxt::TOPO_CORNER_DIR[c0][c2]);
+    const bool b12 = bit(l[1], cxt::TOPO_CORNER_DIR[c1][c2]);
+    const int r0 = (int)b01 + (int)b02, r1 = (int)(!b01) + (int)b12;
+    jlo = r0 == 0 ? 0 : (r1 == 0 ? 1 : 2);
+    const int jhi = r0 == 2 ? 0 : (r1 == 2 ? 1 : 2);
+    jmid = 3 - jlo - jhi;
+}
+
+// does the edge of slot S opposite corner j point (through `arr`) to this triangle?
+template <int S>
+__device__ __forceinline__ bool edge_points_to_face(const Grid &g, const uint32_t *arr, i64 v, int j) {
+    bool r = false;
+    DMTZ_FOR(3, J, {
+        constexpr int jj = decltype(J)::value;
+        constexpr int ex = cxt::TOPO_FACE_EDGE[S][jj][0], ey = cxt::TOPO_FACE_EDGE[S][jj][1],
+                      ez = cxt::TOPO_FACE_EDGE[S][jj][2], ek = cxt::TOPO_FACE_EDGE[S][jj][3],
+                      ei = cxt::TOPO_FACE_EDGE[S][jj][4];
+        if (j == jj) r = eup_get(arr[v + off<ex, ey, ez>(g)], ek) == ei + 1;
+    });
+    return r;
+}
+
+// argmin over the triangle's cofaces of the fourth vertex, among those with
+// "below lo" (A3) or "below mid and above lo" (A5)
+template <int S, bool A3>
+__device__ __forceinline__ int fast_face_choice(const Grid &g, const FieldState &s, i64 v, const uint32_t l[3], int jlo,
+                                                int jmid) {
+    constexpr int c0 = cxt::TOPO_FACE_V[S][0], c1 = cxt::TOPO_FACE_V[S][1], c2 = cxt::TOPO_FACE_V[S][2];
+    const uint32_t llo = jlo == 0 ? l[0] : (jlo == 1 ? l[1] : l[2]);
+    const uint32_t lmid = jmid == 0 ? l[0] : (jmid == 1 ? l[1] : l[2]);
+    uint64_t bk = DMTZ_KEY_DBL_MAX;
+    i64 bid = INT_MAX;
+    int bj = -1;
+    DMTZ_FOR(cxt::TOPO_FACE_NCOF[S], J, {
+        constexpr int j = decltype(J)::value;
+        constexpr int nx = cxt::TOPO_FACE_FOURTH[S][j][0], ny = cxt::TOPO_FACE_FOURTH[S][j][1],
+                      nz = cxt::TOPO_FACE_FOURTH[S][j][2];
+        constexpr int d0 = cxt::cdir_to(c0, nx, ny, nz), d1 = cxt::cdir_to(c1, nx, ny, nz),
+                      d2 = cxt::cdir_to(c2, nx, ny, nz);
+        const int dlo = jlo == 0 ? d0 : (jlo == 1 ? d1 : d2);
+        const int dmid = jmid == 0 ? d0 : (jmid == 1 ? d1 : d2);
+        const bool ok = A3 ? bit(llo, dlo) : (bit(lmid, dmid) && !bit(llo, dlo));
+        if (ok) {
+            const i64 nb = v + off<nx, ny, nz>(g);
+            const uint64_t kn = s.key[nb];
+            if (key_less(kn, nb, bk, bid)) {
+                bk = kn;
+                bid = nb;
+                bj = j;
+            }
+        }
+    });
+    return bj;
+}
+
+template <int S>
+__device__ __forceinline__ void load_corner_lows(const Grid &g, const FieldState &s, i64 v, uint32_t l[3]) {
+    constexpr int c0 = cxt::TOPO_FACE_V[S][0], c1 = cxt::TOPO_FACE_V[S][1], c2 = cxt::TOPO_FACE_V[S][2];
+    l[0] = s.low[v + off<cxt::ccx(c0), cxt::ccy(c0), cxt::ccz(c0)>(g)];
+    l[1] = s.low[v + off<cxt::ccx(c1), cxt::ccy(c1), cxt::ccz(c1)>(g)];
+    l[2] = s.low[v + off<cxt::ccx(c2), cxt::ccy(c2), cxt::ccz(c2)>(g)];
+}
+
+__device__ __forceinline__ void fast_face_a3(const Grid &g, const FieldState &s, i64 v) {
+    uint32_t out = 0, paired = 0;
+    DMTZ_FOR(12, S, {
+        constexpr int sl = decltype(S)::value;
+        uint32_t l[3];
+        load_corner_lows<sl>(g, s, v, l);
+        int jlo, jmid;
+        fast_tri_order<sl>(s, l, jlo, jmid);
+        if (edge_points_to_face<sl>(g, s.ea2, v, jlo)) {
+            paired |= 1u << sl;
+        } else {
+            const int bj = fast_face_choice<sl, true>(g, s, v, l, jlo, jmid);
+            if (bj >= 0) {
+                out |= (uint32_t)(bj + 1) << (2 * sl);
+                paired |= 1u << sl;
+            }
+        }
+    });
+    s.fa3[v] = out;
+    s.fp3[v] = (uint16_t)paired;
+}
+
+// was coface tet J of slot S claimed in pass 3?  Its claimer there is its
+// triangle opposite its lowest vertex, which is corner jlo of the triangle.
+template <int S, int J>
+__device__ __forceinline__ bool cof_tet_claimed3(const Grid &g, const FieldState &s, i64 v, int jlo) {
+    constexpr int tx = cxt::TOPO_FACE_COF[S][J][0], ty = cxt::TOPO_FACE_COF[S][J][1], tz = cxt::TOPO_FACE_COF[S][J][2],
+                  ts = cxt::TOPO_FACE_COF[S][J][3];
+    bool r = false;
+    DMTZ_FOR(3, JL, {
+        constexpr int jl = decltype(JL)::value;
+        constexpr int c = cxt::TOPO_FACE_V[S][jl];
+        constexpr int qi = cxt::tet_corner_index(ts, cxt::ccx(c) - tx, cxt::ccy(c) - ty, cxt::ccz(c) - tz);
+        static_assert(qi >= 0, "face corner must be a corner of its coface");
+        constexpr int fx = tx + cxt::TOPO_TET_FACE[ts][qi][0], fy = ty + cxt::TOPO_TET_FACE[ts][qi][1],
+                      fz = tz + cxt::TOPO_TET_FACE[ts][qi][2], fsl = cxt::TOPO_TET_FACE[ts][qi][3],
+                      fci = cxt::TOPO_TET_FACE[ts][qi][4];
+        if (jlo == jl) r = fup_get(s.fa3[v + off<fx, fy, fz>(g)], fsl) == fci + 1;
+    });
+    return r;
+}
+
+__device__ __forceinline__ void fast_face_a5(const Grid &g, const FieldState &s, i64 v) {
+    const uint32_t a3 = s.fa3[v];
+    const uint32_t p3 = s.fp3[v];
+    uint32_t out = a3;
+    DMTZ_FOR(12, S, {
+        constexpr int sl = decltype(S)::value;
+        if (!bit(p3, sl)) {
+            const bool ep = edge_points_to_face<sl>(g, s.eup, v, 0) || edge_points_to_face<sl>(g, s.eup, v, 1) ||
+                            edge_points_to_face<sl>(g, s.eup, v, 2);
+            if (!ep) {
+                uint32_t l[3];
+                load_corner_lows<sl>(g, s, v, l);
+                int jlo, jmid;
+                fast_tri_order<sl>(s, l, jlo, jmid);
+                const int bj = fast_face_choice<sl, false>(g, s, v, l, jlo, jmid);
+                if (bj >= 0) {
+                    bool claimed = false;
+                    DMTZ_FOR(cxt::TOPO_FACE_NCOF[sl], J, {
+                        constexpr int j = decltype(J)::value;
+                        if (bj == j) claimed = cof_tet_claimed3<sl, j>(g, s, v, jlo);
+                    });
+                    if (!claimed) out |= (uint32_t)(bj + 1) << (2 * sl);
+                }
+            }
+        }
+    });
+    s.fup[v] = out;
+}
+
+// ---------------------------------------------------------------- criticality
+__device__ __forceinline__ void fast_crit(const Grid &g, const FieldState &s, i64 v) {
+    uint32_t m = s.pv[v] == 15 ? 1u : 0u;
+    const uint32_t eu = s.eup[v], fu = s.fup[v];
+    DMTZ_FOR(7, K, {
+        constexpr int k = decltype(K)::value;
+        constexpr int cp = cxt::TOPO_EDGE_V[k][0], cq = cxt::TOPO_EDGE_V[k][1];
+        if (!eup_get(eu, k)) {
+            const bool vp = s.pv[v + g.coff[cp]] == cxt::TOPO_CORNER_DIR[cp][cq] ||
+                            s.pv[v + g.coff[cq]] == cxt::TOPO_CORNER_DIR[cq][cp];
+            if (!vp) m |= 1u << (1 + k);
+        }
+    });
+    DMTZ_FOR(12, S, {
+        constexpr int sl = decltype(S)::value;
+        if (!fup_get(fu, sl)) {
+            const bool pe = edge_points_to_face<sl>(g, s.eup, v, 0) || edge_points_to_face<sl>(g, s.eup, v, 1) ||
+                            edge_points_to_face<sl>(g, s.eup, v, 2);
+            if (!pe) m |= 1u << (8 + sl);
+        }
+    });
+    uint32_t code = 0;
+    DMTZ_FOR(6, TS, {
+        constexpr int ts = decltype(TS)::value;
+        int pj = 7;
+        DMTZ_FOR(4, J, {
+            constexpr int j = decltype(J)::value;
+            constexpr int fx = cxt::TOPO_TET_FACE[ts][j][0], fy = cxt::TOPO_TET_FACE[ts][j][1],
+                          fz = cxt::TOPO_TET_FACE[ts][j][2], fsl = cxt::TOPO_TET_FACE[ts][j][3],
+                          fci = cxt::TOPO_TET_FACE[ts][j][4];
+            if (fup_get(s.fup[v + off<fx, fy, fz>(g)], fsl) == fci + 1) pj = j;
+        });
+        if (pj == 7) m |= 1u << (20 + ts);
+        code |= (uint32_t)pj << (3 * ts);
+    });
+    s.crit[v] = m;
+    if (s.tcode) s.tcode[v] = code;
+}
+
+// ---------------------------------------------------------------- brick sweep
+enum { PASS_VERTEX = 0, PASS_E2, PASS_F3, PASS_E4, PASS_F5, PASS_CRIT };
+
+template <int PASS>
+__global__ void __launch_bounds__(DMTZ_BRICK) k_sweep(Grid g, FieldState s, BrickList bl) {
+    const i64 nb = brick_count(bl);
+    const int lx = threadIdx.x % DMTZ_BX, ly = (threadIdx.x / DMTZ_BX) % DMTZ_BY, lz = threadIdx.x / (DMTZ_BX * DMTZ_BY);
+    for (i64 b = blockIdx.x; b < nb; b += gridDim.x) {
+        int bx, by, bz;
+        brick_coords(bl, b, bx, by, bz);
+        const int x = bx * DMTZ_BX + lx, y = by * DMTZ_BY + ly, z = bz * DMTZ_BZ + lz;
+        if (x >= g.W || y >= g.H || z >= g.D) continue;
+        const i64 v = x + (i64)y * g.W + (i64)z * g.WH;
+        const bool interior = x >= 1 && y >= 1 && z >= 1 && x <= g.W - 2 && y <= g.H - 2 && z <= g.D - 2;
+        if (PASS == PASS_VERTEX) {
+            if (interior) fast_vertex(g, s, v);
+            else pass_vertex_at(g, s, v, x, y, z);
+        } else if (PASS == PASS_E2) {
+            if (interior) fast_edge_a2(g, s, v);
+            else pass_edge_a2_at(g, s, v, x, y, z);
+        } else if (PASS == PASS_F3) {
+            if (interior) fast_face_a3(g, s, v);
+            else pass_face_a3_at(g, s, v, x, y, z);
+        } else if (PASS == PASS_E4) {
+            if (interior) fast_edge_a4(g, s, v);
+            else pass_edge_a4_at(g, s, v, x, y, z);
+        } else if (PASS == PASS_F5) {
+            if (interior) fast_face_a5(g, s, v);
+            else pass_face_a5_at(g, s, v, x, y, z);
+        } else {
+            if (interior) {
+                fast_crit(g, s, v);
+            } else {
+                uint32_t tc;
+                s.crit[v] = crit_mask(g, s, v, x, y, z, &tc);
+                if (s.tcode) s.tcode[v] = tc;
+            }
+        }
+    }
+}
+
+}  // namespace dmtz
