@@ -1,15 +1,14 @@
 """Build recipe for libdmtz (sm_103a) and the drop-in `dmtz` executable.
 
 nvcc is called directly (no cmake, no torch extension machinery): one
-translation unit for the library, one small host file for the executable,
-compiled in parallel.  Outputs go to dmtz_gb300/_lib/ (git-ignored).
+translation unit for the library and one small host file for the executable,
+linked against it.  Outputs go to dmtz_gb300/_lib/ (git-ignored).
 """
 from __future__ import annotations
 
 import os
 import subprocess
 import sys
-from concurrent.futures import ThreadPoolExecutor
 
 PKG = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(PKG)
@@ -50,14 +49,14 @@ def build(force: bool = False, verbose: bool = False) -> str:
         jobs.append([NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
                      *(["-Xptxas", "-v"] if verbose else []),
                      "-o", LIB, os.path.join(CSRC, "dmtz.cu")])
+    for job in jobs:
+        r = _run(job)
+        if verbose:
+            sys.stdout.write(r.stdout + r.stderr)
+    # the executable is host code linked against the library beside it
     cli = os.path.join(CSRC, "dmtz_cli.cpp")
-    if os.path.exists(cli) and (force or _stale(EXE, deps)):
-        jobs.append([NVCC, *ARCH, "-O3", "-std=c++17", "-o", EXE, cli, os.path.join(CSRC, "dmtz.cu")])
-    if jobs:
-        with ThreadPoolExecutor(len(jobs)) as ex:
-            for r in ex.map(_run, jobs):
-                if verbose:
-                    sys.stdout.write(r.stdout + r.stderr)
+    if os.path.exists(cli) and (force or jobs or _stale(EXE, deps)):
+        _run([NVCC, "-O3", "-std=c++17", "-o", EXE, cli, "-L" + LIBDIR, "-ldmtz", "-Xlinker", "-rpath,$ORIGIN"])
     return LIB
 
 

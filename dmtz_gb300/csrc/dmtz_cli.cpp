@@ -1,0 +1,347 @@
+// dmtz_cli.cpp — the `dmtz` executable: a drop-in for the reference program.
+//
+// Same invocation as the reference (main_3d.cu:6255-6291):
+//   dmtz "<name>,<W>,<H>,<D>" <rel_eps> <compressor_id> <preserve_saddles>
+//        <preserve_vpath> <preserve_geometry> <filtration> <preserve_connectors>
+//        <preserve_type> <edit_type>
+// and the same files (main_3d.cu:153-181, 1315-1327, 1494-1757, 6327-6393,
+// 7151-7235), below a data root that defaults to the reference's hard-coded
+// prefix and can be moved with DMTZ_DATA_ROOT:
+//   in : ./<name>.bin                                   raw float64, x fastest
+//        <root>/decompressed_data/decp_<name>_<eps %.6e><compressor_id>_.bin
+//        <root>/compressed_data/compressed_<name>_<eps>.sz|.zfp (size only)
+//   out: <root>/fixed_decp_data/fixed_decp_<name>_<eps>.bin  size_t N + N float64
+//        <root>/data1<name>.bin (edit_type 1: 3-bit counter bitmap) or
+//        <root>/data<name>.bin (edit_type 0: delta-coded int32 indices),
+//        <root>/data_edits<name>.bin, each followed by `zstd -f` when zstd exists
+//        ./stat_result/result_<name>_<cid>_detailed[_additional_time].txt (appended)
+//        ./stat_result/performance1_cuda_<name>_<bound>_<cid>.txt (appended)
+// Errors print a message and exit non-zero (the reference exits through
+// checkCudaError, main_3d.cu:1307-1313).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <filesystem>
+#include <fstream>
+#include <iomanip>
+#include <iostream>
+#include <limits>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/dmtz.h"
+
+namespace fs = std::filesystem;
+
+namespace {
+
+struct Run {
+    std::string name, cid, root, input_file, compressed_file;
+    int W = 0, H = 0, D = 0;
+    double rel = 0, bound = 0, min_g = 0, max_g = 0;
+    int flags[7] = {0, 0, 0, 0, 0, 0, 0};
+    double compression_time = 0, additional_time = 0;
+};
+
+std::vector<double> read_doubles(const std::string &path, bool &ok) {
+    std::ifstream in(path, std::ios::binary | std::ios::ate);
+    std::vector<double> v;
+    ok = false;
+    if (!in) {
+        std::cerr << "can not open file " << path << std::endl;
+        return v;
+    }
+    const std::streamsize size = in.tellg();
+    in.seekg(0, std::ios::beg);
+    v.resize((size_t)size / sizeof(double));
+    ok = (bool)in.read(reinterpret_cast<char *>(v.data()), (std::streamsize)(v.size() * sizeof(double)));
+    return v;
+}
+
+bool write_bytes(const std::string &path, const void *p, size_t n) {
+    std::ofstream out(path, std::ios::binary | std::ios::out);
+    if (!out) {
+        std::cerr << "cannot open file: " << path << std::endl;
+        return false;
+    }
+    out.write(reinterpret_cast<const char *>(p), (std::streamsize)n);
+    return true;
+}
+
+bool have_zstd() { return std::system("command -v zstd > /dev/null 2>&1") == 0; }
+
+void zstd_file(const std::string &path) {
+    if (!have_zstd()) {
+        std::cerr << "warning: zstd not found; " << path << " left uncompressed" << std::endl;
+        return;
+    }
+    const std::string cmd = "zstd -f " + path;
+    std::cout << "Executing command: " << cmd << std::endl;
+    std::cout << (std::system(cmd.c_str()) == 0 ? "Compression successful." : "Compression failed.") << std::endl;
+}
+
+uintmax_t size_or_raw(const std::string &zst, const std::string &raw) {
+    std::error_code ec;
+    uintmax_t s = fs::file_size(zst, ec);
+    if (!ec) return s;
+    s = fs::file_size(raw, ec);
+    return ec ? 0 : s;
+}
+
+// calculateMSE / calculatePSNR (main_3d.cu:1330-1352); range = max - min of
+// the decompressed field, as the reference passes it
+double psnr(const std::vector<double> &a, const std::vector<double> &b, double range) {
+    double mse = 0.0;
+    for (size_t i = 0; i < a.size(); i++) mse += std::pow(a[i] - b[i], 2);
+    mse /= (double)a.size();
+    if (mse == 0) return std::numeric_limits<double>::infinity();
+    return -20.0 * std::log10(std::sqrt(mse) / range);
+}
+
+// encodeTo3BitBitmap (main_3d.cu:1446-1476): counters 0..6 packed 3 bits each,
+// low bits first, spilling into the next byte
+std::vector<uint8_t> bitmap3(const std::vector<int> &vals) {
+    std::vector<uint8_t> out;
+    uint8_t cur = 0;
+    int bit = 0;
+    for (int v : vals) {
+        if (v < 0 || v > 6) {
+            std::cerr << "error, value out of (0~6)" << v << std::endl;
+            return {};
+        }
+        cur |= (uint8_t)(v << bit);
+        bit += 3;
+        if (bit >= 8) {
+            out.push_back(cur);
+            bit -= 8;
+            cur = (uint8_t)(v >> (3 - bit));
+        }
+    }
+    if (bit > 0) out.push_back(cur);
+    return out;
+}
+
+void append_stats(const Run &r, const std::string &file, double ocr, double cr, double obr, double br, double p0,
+                  double p1, double ratio) {
+    std::ofstream o(file, std::ios::app);
+    if (!o) {
+        std::cerr << "Unable to open file for writing." << std::endl;
+        return;
+    }
+    const char *names[7] = {"preserve_saddles", "preserve_vpath", "preserve_geometry", "filtration",
+                            "preserve_connectors", "preserve_types", "edit_type"};
+    o << std::to_string(r.bound) << ":" << std::endl;
+    o << std::setprecision(17) << "related_error: " << r.rel << std::endl;
+    for (int k = 0; k < 7; k++) o << names[k] << ": " << r.flags[k] << std::endl;
+    o << std::setprecision(17) << "OCR: " << ocr << std::endl;
+    o << std::setprecision(17) << "CR: " << cr << std::endl;
+    o << std::setprecision(17) << "OBR: " << obr << std::endl;
+    o << std::setprecision(17) << "BR: " << br << std::endl;
+    o << std::setprecision(17) << "psnr: " << p0 << std::endl;
+    o << std::setprecision(17) << "fixed_psnr: " << p1 << std::endl;
+    o << std::setprecision(17) << "edit_ratio: " << ratio << std::endl;
+    o << std::setprecision(17) << "compression_time: " << r.compression_time << std::endl;
+    o << std::setprecision(17) << "additional_time: " << r.additional_time << std::endl;
+    o << "\n" << std::endl;
+}
+
+// cost (edit_type 1, main_3d.cu:1494-1646) and original_cost (edit_type 0,
+// main_3d.cu:1649-1757): edit index/value files and the appended stat file
+void write_costs(const Run &r, const std::vector<double> &fixed, const std::vector<double> &decp0,
+                 const std::vector<double> &orig, const std::vector<int> &counter) {
+    const size_t n = orig.size();
+    size_t cnt = 0;
+    std::string idx_file, idx_zst, edits_file = r.root + "/data_edits" + r.name + ".bin";
+    std::vector<double> edits;
+    if (r.flags[6] == 1) {
+        std::vector<int> idx(n, 0);
+        for (size_t i = 0; i < n; i++)
+            if (decp0[i] != fixed[i]) {
+                idx[i] = counter[i];
+                if (idx[i] == 6) edits.push_back(-(decp0[i] - (orig[i] - r.bound)));
+                cnt++;
+            }
+        const std::vector<uint8_t> bm = bitmap3(idx);
+        idx_file = r.root + "/data1" + r.name + ".bin";
+        write_bytes(idx_file, bm.data(), bm.size());
+    } else {
+        std::vector<double> pos;
+        for (size_t i = 0; i < n; i++)
+            if (decp0[i] != fixed[i]) {
+                pos.push_back((double)i);
+                edits.push_back(fixed[i] - decp0[i]);
+                cnt++;
+            }
+        std::vector<int> diffs;
+        if (!pos.empty()) diffs.push_back((int)pos[0]);
+        for (size_t i = 1; i < pos.size(); i++) diffs.push_back((int)(pos[i] - pos[i - 1]));
+        idx_file = r.root + "/data" + r.name + ".bin";
+        write_bytes(idx_file, diffs.data(), diffs.size() * sizeof(int));
+    }
+    const double ratio = (double)cnt / (double)n;
+    std::cout << cnt << "," << ratio << std::endl;
+    zstd_file(idx_file);
+    write_bytes(edits_file, edits.data(), edits.size() * sizeof(double));
+    zstd_file(edits_file);
+    const uintmax_t c_idx = size_or_raw(idx_file + ".zst", idx_file), c_edit = size_or_raw(edits_file + ".zst", edits_file);
+    std::error_code ec;
+    const uintmax_t o_idx = fs::file_size(idx_file, ec);
+    const uintmax_t o_data = fs::file_size(r.input_file, ec);
+    uintmax_t c_data = fs::file_size(r.compressed_file, ec);
+    if (ec) {
+        std::cerr << "warning: compressed file " << r.compressed_file << " not found; ratios use size 0" << std::endl;
+        c_data = 0;
+    }
+    const double ocr = (double)o_data / (double)(c_data + c_edit + c_idx);
+    const double range = r.max_g - r.min_g;
+    const double p0 = psnr(orig, decp0, range), p1 = psnr(orig, fixed, range);
+    const std::string stat = r.flags[6] == 1 ? "./stat_result/result_" + r.name + "_" + r.cid + "_detailed_additional_time.txt"
+                                             : "./stat_result/result_" + r.name + "_" + r.cid + "_detailed.txt";
+    append_stats(r, stat, ocr, (double)o_data / (double)c_data, 64 / ocr, 64 / ((double)o_idx / (double)c_data), p0, p1,
+                 ratio);
+}
+
+}  // namespace
+
+int main(int argc, char **argv) {
+    std::cout.precision(std::numeric_limits<double>::max_digits10);
+    if (argc < 11) {
+        std::cerr << "usage: " << argv[0]
+                  << " <name>,<W>,<H>,<D> <rel_eps> <compressor_id> <preserve_saddles> <preserve_vpath>"
+                     " <preserve_geometry> <filtration> <preserve_connectors> <preserve_type> <edit_type>"
+                  << std::endl;
+        return 2;
+    }
+    Run r;
+    {
+        std::istringstream iss(argv[1]);
+        char sep;
+        if (!(std::getline(iss, r.name, ',') && iss >> r.W >> sep && sep == ',' && iss >> r.H >> sep && sep == ',' &&
+              iss >> r.D)) {
+            std::cerr << "Parsing error for dimensions" << std::endl;
+            return 2;
+        }
+    }
+    r.rel = std::stod(argv[2]);
+    r.cid = argv[3];
+    for (int k = 0; k < 7; k++) r.flags[k] = std::stoi(argv[4 + k]);
+    const char *root_env = std::getenv("DMTZ_DATA_ROOT");
+    r.root = root_env ? root_env : "/pscratch/sd/y/yuxiaoli/MSCz";
+    std::cout << "Filename: " << r.name << std::endl << "Width: " << r.W << std::endl << "Height: " << r.H << std::endl
+              << "Depth: " << r.D << std::endl;
+    r.input_file = r.name + ".bin";
+    bool ok;
+    std::vector<double> orig = read_doubles(r.input_file, ok);
+    const size_t n = (size_t)r.W * r.H * r.D;
+    if (!ok || orig.size() < n) {
+        std::cerr << "input " << r.input_file << " is missing or shorter than " << n << " values" << std::endl;
+        return 3;
+    }
+    orig.resize(n);
+    const auto mm = std::minmax_element(orig.begin(), orig.end());
+    r.bound = (*mm.second - *mm.first) * r.rel;
+    std::cout << "bound1: " << r.bound << std::endl;
+    std::ostringstream eps;
+    eps << std::scientific << std::setprecision(6) << r.rel;
+    std::ostringstream bnd;
+    bnd << std::scientific << std::setprecision(17) << r.bound;
+    const std::string decp_file = r.root + "/decompressed_data/decp_" + r.name + "_" + eps.str() + r.cid + "_.bin";
+    r.compressed_file = r.root + "/compressed_data/compressed_" + r.name + "_" + eps.str() + (r.cid == "zfp" ? ".zfp" : ".sz");
+    const std::string fix_file = r.root + "/fixed_decp_data/fixed_decp_" + r.name + "_" + eps.str() + ".bin";
+    auto t0 = std::chrono::high_resolution_clock::now();
+    if (r.cid == "sz3" || r.cid == "zfp") {  // main_3d.cu:6331-6356
+        const std::string cmd =
+            r.cid == "sz3"
+                ? "sz3 -i " + r.input_file + " -z " + r.compressed_file + " -o " + decp_file + " -d  -1 " +
+                      std::to_string(n) + " -M REL " + eps.str() + " -a"
+                : "zfp -i " + r.input_file + " -z " + r.compressed_file + " -o " + decp_file + " -d  -1 " +
+                      std::to_string(n) + " -a " + bnd.str() + " -s";
+        std::cout << "Executing command: " << cmd << std::endl;
+        std::cout << (std::system(cmd.c_str()) == 0 ? "Compression successful." : "Compression failed.") << std::endl;
+    }
+    r.compression_time = std::chrono::duration<double>(std::chrono::high_resolution_clock::now() - t0).count();
+    std::vector<double> decp = read_doubles(decp_file, ok);
+    if (!ok || decp.size() < n) {
+        std::cerr << "decompressed field " << decp_file << " is missing or short" << std::endl;
+        return 3;
+    }
+    decp.resize(n);
+    const auto mg = std::minmax_element(decp.begin(), decp.end());
+    r.min_g = *mg.first;
+    r.max_g = *mg.second;
+    const std::vector<double> decp0(decp);
+
+    dmtz_ctx *ctx = nullptr;
+    if (dmtz_ctx_create(&ctx, 0) != DMTZ_OK) {
+        std::cerr << "no CUDA device" << std::endl;
+        return 4;
+    }
+    dmtz_opts o;
+    o.preserve_saddles = r.flags[0];
+    o.preserve_vpath = r.flags[1];
+    o.preserve_geometry = r.flags[2];
+    o.filtration = r.flags[3];
+    o.preserve_connectors = r.flags[4];
+    o.preserve_type = r.flags[5];
+    o.edit_type = r.flags[6];
+    o.max_rounds = 0;
+    o.use_graph = 0;
+    const char *cap = std::getenv("DMTZ_MAX_ROUNDS");
+    if (cap) o.max_rounds = std::atoi(cap);
+    dmtz_report rep;
+    std::vector<int> counter(n);
+    t0 = std::chrono::high_resolution_clock::now();
+    const dmtz_status st = dmtz_correct(ctx, r.W, r.H, r.D, orig.data(), decp.data(), 0, r.rel, &o, &rep, counter.data());
+    r.additional_time = std::chrono::duration<double>(std::chrono::high_resolution_clock::now() - t0).count();
+    if (st != DMTZ_OK) {
+        std::cerr << "correction failed (" << (int)st << "): " << dmtz_last_error(ctx) << std::endl;
+        dmtz_ctx_destroy(ctx);
+        return 5;
+    }
+    dmtz_ctx_destroy(ctx);
+    size_t changed = 0;
+    for (size_t i = 0; i < n; i++) changed += decp[i] != decp0[i];
+    {
+        std::error_code ec;
+        fs::create_directories(fs::path(fix_file).parent_path(), ec);
+        std::ofstream out(fix_file, std::ios::binary);
+        if (!out) {
+            std::cerr << "Error opening file for writing: " << fix_file << std::endl;
+            return 3;
+        }
+        const size_t sz = n;
+        out.write(reinterpret_cast<const char *>(&sz), sizeof(sz));
+        out.write(reinterpret_cast<const char *>(decp.data()), (std::streamsize)(n * sizeof(double)));
+    }
+    write_costs(r, decp, decp0, orig, counter);
+    std::cout << changed << std::endl;
+    // phase timers, named as the reference prints them (main_3d.cu:7187-7188)
+    const double *ph = rep.phase_ms;
+    std::cout << "build_cells: " << 0.0 << " ,gradient_pairing: " << ph[0] / 1000 << ",get_f_cp: " << 0.0
+              << " ,get_f_path: " << ph[2] / 1000 << " ,fix_f_cp: " << (ph[1] + ph[4]) / 1000
+              << " ,fix_f_vpath: " << ph[3] / 1000 << ", init_cells: " << ph[5] / 1000 << std::endl;
+    std::ofstream pf("./stat_result/performance1_cuda_" + r.name + "_" + std::to_string(r.bound) + "_" + r.cid + ".txt",
+                     std::ios::app);
+    if (!pf) {
+        std::cerr << "Unable to open file for writing." << std::endl;
+        return 1;
+    }
+    const char *names[7] = {"preserve_saddles", "preserve_vpath", "preserve_geometry", "filtration",
+                            "preserve_connectors", "preserve_types", "edit_type"};
+    pf << std::setprecision(17) << "related_error: " << r.rel << std::endl;
+    for (int k = 0; k < 6; k++) pf << names[k] << ": " << r.flags[k] << std::endl;
+    pf << "build_cells: " << 0.0 << std::endl;
+    pf << "gradient_pairing: " << ph[0] / 1000 << std::endl;
+    pf << "get_f_cp: " << 0.0 << std::endl;
+    pf << "get_f_path: " << ph[2] / 1000 << std::endl;
+    pf << "fix_f_cp: " << (ph[1] + ph[4]) / 1000 << std::endl;
+    pf << "fix_f_vpath:" << ph[3] / 1000 << std::endl;
+    pf << "init_cells:" << ph[5] / 1000 << std::endl;
+    pf << "iteration number:" << rep.outer_iterations + 1 << std::endl;
+    pf << "\n" << std::endl;
+    return 0;
+}

@@ -239,6 +239,16 @@ def run(out_dir, only=None, timeout=240, big=False):
                 res["req_idx"] = np.concatenate(r_idx)
                 res["req_buf"] = np.concatenate(r_buf)
                 res["req_val"] = np.concatenate(r_val)
+            # the side files of the reference's cost()/original_cost(): edit indices
+            # (3-bit counter bitmap or delta-coded indices) and edit values
+            for stem in ("data1", "data", "data_edits"):
+                p_ = os.path.join(wd, "mscz", f"{stem}{name}.bin")
+                if os.path.exists(p_):
+                    res["file_" + stem] = np.frombuffer(open(p_, "rb").read(), np.uint8).copy()
+            for fn in os.listdir(os.path.join(wd, "stat_result")):
+                if fn.startswith("result_"):
+                    rec["stat_result_file"] = fn
+                    rec["stat_result_text"] = open(os.path.join(wd, "stat_result", fn)).read()
             perf = [x for x in os.listdir(os.path.join(wd, "stat_result")) if x.startswith("performance1")]
             if perf:
                 txt = open(os.path.join(wd, "stat_result", perf[0])).read()

@@ -15,6 +15,8 @@ tests/golden/ref_<case>.npz per case holding
   cnt_*       indices/values of edit counters that are not 1
   r0_idx, r0_buf  first fix round: vertices whose delta buffer entry is not
               the sentinel, and the buffer values
+  file_*      (small cases) the reference's edit-index and edit-value files
+              (data1<name>.bin or data<name>.bin, data_edits<name>.bin)
 
 Usage: python tests/golden/make_fixtures.py gpurun_out/ref
 """
@@ -53,6 +55,15 @@ def convert(src, dst_dir=HERE):
     ci = np.nonzero(cnt != 1)[0].astype(np.int32)
     out["cnt_idx"] = ci
     out["cnt_val"] = cnt[ci].astype(np.int8)
+    # side files of the reference's cost()/original_cost() (small cases only)
+    if f.size <= 20000:
+        for k in ("file_data1", "file_data", "file_data_edits"):
+            if k in z:
+                out[k] = z[k]
+        if "stat_result_text" in m:
+            keep["stat_result_file"] = m["stat_result_file"]
+            keep["stat_result_text"] = m["stat_result_text"]
+        out["meta"] = json.dumps(keep)
     if "req_round" in z:
         sel = z["req_round"] == 0
         out["r0_idx"] = z["req_idx"][sel].astype(np.int32)

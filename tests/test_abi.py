@@ -41,3 +41,13 @@ def test_cell_counts_without_gpu():
         V, E, F, T = got
         W, H, D = dims
         assert V == W * H * D and T == 6 * (W - 1) * (H - 1) * (D - 1)
+
+
+def test_cli_builds_and_prints_usage():
+    import subprocess
+
+    from dmtz_gb300 import build
+
+    build.build()
+    p = subprocess.run([build.EXE], capture_output=True, text=True)
+    assert p.returncode == 2 and "usage" in p.stderr
