@@ -87,6 +87,8 @@ def load_library(build_if_missing: bool = True):
     L.dmtz_correct.argtypes = [_vp, _int, _int, _int, _vp, _vp, _int, ctypes.c_double, ctypes.POINTER(Opts),
                                ctypes.POINTER(Report), _vp]
     L.dmtz_profile_sweep.argtypes = [_vp, _int, _int, _int, _vp, _vp, _int, _int, _f64p]
+    L.dmtz_labels.argtypes = [_vp, _int, _int, _int, _vp, _int, _i32p, _i32p]
+    L.dmtz_labels.restype = _int
     for fn in ("dmtz_ctx_create", "dmtz_cell_counts", "dmtz_extract", "dmtz_mismatch", "dmtz_fix_round",
                "dmtz_path_detect", "dmtz_correct", "dmtz_profile_sweep"):
         getattr(L, fn).restype = _int
@@ -151,6 +153,15 @@ class Context:
         out = [np.empty(n, np.int32) for n in (V, E, F, T)]
         self._check(self._L.dmtz_extract(self._h, *dims, d.ctypes.data, 0, *out))
         return tuple(out)
+
+    def labels(self, data, dims=None):
+        """Manifold labels (descending per vertex, ascending per tetrahedron, reference ids)."""
+        dims = _dims_of(np.asarray(data), dims)
+        d = _flat(data)
+        V, E, F, T = cell_counts(dims)
+        desc, asc = np.empty(V, np.int32), np.empty(T, np.int32)
+        self._check(self._L.dmtz_labels(self._h, *dims, d.ctypes.data, 0, desc, asc))
+        return desc, asc
 
     def mismatch(self, f, g, dims=None):
         """Sorted critical-cell mismatch lists (min, 1-saddle, 2-saddle, max)."""

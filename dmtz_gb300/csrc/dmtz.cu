@@ -366,6 +366,80 @@ __global__ void k_filter(Grid g, const uint32_t *crit_o, const double *f, double
     }
 }
 
+// --------------------------------------------------------------- manifold labels
+// Descending manifold label of a vertex: the minimum its steepest-descent path
+// (vertex -> other endpoint of its paired edge, processVertices'
+// pairing) reaches.  Ascending label of a tetrahedron: the maximum (unpaired
+// tetrahedron) its ascending path (is_false's walk, main_3d.cu:4437-4497)
+// reaches, or -1 when the path leaves through the boundary.  Both by pointer
+// jumping: lab <- lab[lab] until nothing changes.
+__global__ void k_desc_init(Grid g, const uint8_t *pv, i64 *lab) {
+    for (i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x; v < g.V; v += (i64)gridDim.x * blockDim.x) {
+        const int d = pv[v];
+        lab[v] = d == 15 ? v : v + g.doff[d];
+    }
+}
+__global__ void k_asc_init(Grid g, const uint32_t *tcode, const uint8_t *succ, i64 *lab) {
+    for (i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x; t < 6 * g.V; t += (i64)gridDim.x * blockDim.x) {
+        const i64 v = t / 6;
+        const int ts = (int)(t - 6 * v);
+        int x, y, z;
+        decode_v(g, v, x, y, z);
+        if (!cell_ok(g, x, y, z, 1, 1, 1)) {
+            lab[t] = -2;  // no such tetrahedron
+            continue;
+        }
+        if (((tcode[v] >> (3 * ts)) & 7) == 7) {
+            lab[t] = t;  // a maximum
+            continue;
+        }
+        const int s8 = succ[t];
+        if (s8 == 255) {
+            lab[t] = -1;  // leaves through the boundary
+            continue;
+        }
+        const int d = s8 / 6;
+        const i64 nv = v + (d % 3 - 1) + (i64)((d / 3) % 3 - 1) * g.W + (i64)(d / 9 - 1) * g.WH;
+        lab[t] = nv * 6 + (s8 - 6 * d);
+    }
+}
+__global__ void k_jump(i64 *lab, i64 n, int *changed) {
+    int any = 0;
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+        const i64 l = lab[i];
+        if (l < 0) continue;
+        const i64 ll = lab[l];
+        if (ll != l) {
+            lab[i] = ll;
+            any = 1;
+        }
+    }
+    if (__syncthreads_or(any) && threadIdx.x == 0) atomicOr(changed, 1);
+}
+// reference ids of the labels
+__global__ void k_desc_out(Grid g, const i64 *lab, int32_t *out) {
+    for (i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x; v < g.V; v += (i64)gridDim.x * blockDim.x)
+        out[v] = (int32_t)lab[v];
+}
+__global__ void k_asc_out(Grid g, const i64 *lab, int32_t *out) {
+    for (i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x; t < 6 * g.V; t += (i64)gridDim.x * blockDim.x) {
+        const i64 v = t / 6;
+        const int ts = (int)(t - 6 * v);
+        int x, y, z;
+        decode_v(g, v, x, y, z);
+        if (!cell_ok(g, x, y, z, 1, 1, 1)) continue;
+        const i64 l = lab[t];
+        int32_t r = -1;
+        if (l >= 0) {
+            const i64 lv = l / 6;
+            int lx, ly, lz;
+            decode_v(g, lv, lx, ly, lz);
+            r = (int32_t)tet_ref(g, lx, ly, lz, (int)(l - 6 * lv));
+        }
+        out[tet_ref(g, x, y, z, ts)] = r;
+    }
+}
+
 // exact min / max of a field through its order keys
 __global__ void k_minmax(const double *a, i64 n, unsigned long long *kmin, unsigned long long *kmax) {
     unsigned long long lo = ~0ull, hi = 0ull;
@@ -1043,6 +1117,55 @@ dmtz_status dmtz_correct(dmtz_ctx *ctx, int W, int H, int D, const double *orig,
     if (err & ERR_WALK) return fail(ctx, DMTZ_ERR_CYCLE, "ascending path walk exceeded its step cap");
     if (!converged) return fail(ctx, DMTZ_ERR_NONCONVERGED, "round cap reached before the complexes agree");
     return DMTZ_OK;
+}
+
+// pointer jumping to a fixed point; false if it does not settle within the cap
+static dmtz_status jump_to_roots(dmtz_ctx *ctx, i64 *lab, i64 n) {
+    for (int round = 0; round < 64; round++) {
+        CK(cudaMemsetAsync(ctx->errword, 0, sizeof(int), ctx->stream));
+        k_jump<<<persistent_grid(), kBlock, 0, ctx->stream>>>(lab, n, ctx->errword);
+        int changed = 0;
+        CK(cudaMemcpyAsync(&changed, ctx->errword, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        if (!changed) return DMTZ_OK;
+    }
+    return fail(ctx, DMTZ_ERR_CYCLE, "manifold labels did not settle (cycle in the gradient paths)");
+}
+
+dmtz_status dmtz_labels(dmtz_ctx *ctx, int W, int H, int D, const double *data, int on_device, int32_t *desc,
+                        int32_t *asc) {
+    Grid g;
+    dmtz_status s = check_dims(ctx, W, H, D, g);
+    if (s != DMTZ_OK) return s;
+    if (g.F >= INT32_MAX) return fail(ctx, DMTZ_ERR_ARG, "grid too large for 32-bit reference ids");
+    CK(cudaSetDevice(ctx->device));
+    if ((s = ensure(ctx, g)) != DMTZ_OK) return s;
+    if ((s = upload(ctx, ctx->f, data, g.V, on_device)) != DMTZ_OK) return s;
+    run_pairing(ctx, g, view(ctx->P, ctx->f), nullptr, 1);
+    k_path_succ<<<grid_for(g.V), kBlock, 0, ctx->stream>>>(g, ctx->P.tcode, ctx->succ);
+    i64 *dl = nullptr, *al = nullptr;
+    int32_t *dout = nullptr, *aout = nullptr;
+    CK(dalloc(&dl, g.V));
+    CK(dalloc(&al, 6 * g.V));
+    CK(dalloc(&dout, g.V));
+    CK(dalloc(&aout, g.T));
+    const unsigned pg = persistent_grid();
+    k_desc_init<<<pg, kBlock, 0, ctx->stream>>>(g, ctx->P.pv, dl);
+    k_asc_init<<<pg, kBlock, 0, ctx->stream>>>(g, ctx->P.tcode, ctx->succ, al);
+    if ((s = jump_to_roots(ctx, dl, g.V)) == DMTZ_OK) s = jump_to_roots(ctx, al, 6 * g.V);
+    if (s == DMTZ_OK) {
+        k_desc_out<<<pg, kBlock, 0, ctx->stream>>>(g, dl, dout);
+        k_asc_out<<<pg, kBlock, 0, ctx->stream>>>(g, al, aout);
+        CK(cudaMemcpyAsync(desc, dout, sizeof(int32_t) * (size_t)g.V, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(asc, aout, sizeof(int32_t) * (size_t)g.T, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    cudaFree(dl);
+    cudaFree(al);
+    cudaFree(dout);
+    cudaFree(aout);
+    CK(cudaGetLastError());
+    return s;
 }
 
 dmtz_status dmtz_profile_sweep(dmtz_ctx *ctx, int W, int H, int D, const double *orig, const double *decp,

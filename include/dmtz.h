@@ -130,6 +130,19 @@ dmtz_status dmtz_path_detect(dmtz_ctx *ctx, int W, int H, int D, const double *o
 dmtz_status dmtz_correct(dmtz_ctx *ctx, int W, int H, int D, const double *orig, double *decp, int on_device,
                          double rel_eps, const dmtz_opts *opts, dmtz_report *report, int32_t *edit_counter_out);
 
+/* Manifold labels of one field's discrete gradient (no reference kernel
+ * materialises them; they follow the reference's own path rules):
+ *   desc[v] (V ints): the minimum reached from vertex v by repeatedly moving
+ *     to the other endpoint of its paired edge (processVertices pairing);
+ *   asc[t] (T ints): the maximum tetrahedron reached from tetrahedron t by
+ *     the ascending walk of is_false (main_3d.cu:4437-4497: paired facet, then
+ *     that facet's other coface), or -1 when the walk leaves the domain.
+ * Separatrix labels are these labels at the endpoints of 1-saddle edges and
+ * at the cofaces of 2-saddle triangles.  Returns DMTZ_ERR_CYCLE if pointer
+ * jumping does not settle in 64 rounds. */
+dmtz_status dmtz_labels(dmtz_ctx *ctx, int W, int H, int D, const double *data, int on_device, int32_t *desc,
+                        int32_t *asc);
+
 /* Timing of the gradient sweep that every correction round runs (the five
  * pairing passes of main_3d.cu:6864-6874 plus the critical-cell comparison
  * of :6903-6909), `reps` times on the context's stream between CUDA events.

@@ -1504,3 +1504,80 @@ int orc_correct(int W, int H, int D, const double *f, double *g, double rel_eps,
     free(as_tet); free(as_cur); free(ds_e); free(ds_v); free(cnt); free(buf);
     return 0;
 }
+
+/* ---------------------------------------------------------------------------
+ * N4: manifold labels of one field, by following the reference's path rules
+ * serially (descending: processVertices pairing; ascending: is_false's walk,
+ * main_3d.cu:4437-4497).  desc[v] = minimum reached, asc[t] = maximum reached
+ * or -1 when the walk leaves the domain.  Returns the number of walks that hit
+ * the step cap (0 for a valid gradient).
+ * ------------------------------------------------------------------------- */
+int orc_labels(int W, int H, int D, const double *data, int *desc, int *asc, int nthreads) {
+    grid_t G;
+    grid_init(&G, W, H, D);
+    int *P = (int *)malloc(sizeof(int) * ((size_t)G.V + G.E + G.F + G.T));
+    int *PV = P, *PE = P + G.V, *PF = PE + G.E, *PT = PF + G.F;
+    pair_all(&G, data, PV, PE, PF, PT, nthreads);
+    ctx_t c;
+    memset(&c, 0, sizeof(c));
+    c.G = G;
+    c.PV = PV; c.PE = PE; c.PF = PF; c.PT = PT;
+    int bad = 0;
+    for (int v = 0; v < G.V; v++) {
+        int cur = v;
+        long long steps = 0;
+        while (PV[cur] != -1) {
+            int a, b;
+            edge_verts(&G, PV[cur], &a, &b);
+            cur = a == cur ? b : a;
+            if (++steps > G.V) {
+                bad++;
+                break;
+            }
+        }
+        desc[v] = cur;
+    }
+    for (int t0 = 0; t0 < G.T; t0++) {
+        int cur = t0, old, lab = -1;
+        long long steps = 0;
+        do {
+            old = cur;
+            int t = PT[cur];
+            if (t == -1) {
+                lab = cur;
+                break;
+            }
+            if (PF[t] == -1 || PT[PF[t]] != t) break;
+            int t1 = -1, t2 = -1;
+            cell_tetra(&c, t, &t1, &t2);
+            cur = t1 == cur ? t2 : t1;
+            if (++steps > G.T) {
+                bad++;
+                break;
+            }
+        } while (cur != old && cur != -1);
+        asc[t0] = lab;
+    }
+    free(P);
+    return bad;
+}
+
+/* helpers for tests: cofaces of triangles in get_cell_tetra order (-1 when
+ * absent) and endpoints of edges (higher id first) */
+void orc_face_cofaces(int W, int H, int D, int n, const int *faces, int *out2) {
+    ctx_t c;
+    memset(&c, 0, sizeof(c));
+    grid_init(&c.G, W, H, D);
+    for (int i = 0; i < n; i++) {
+        int x = -1, y = -1;
+        cell_tetra(&c, faces[i], &x, &y);
+        out2[2 * i] = x;
+        out2[2 * i + 1] = y;
+    }
+}
+
+void orc_edge_verts(int W, int H, int D, int n, const int *edges, int *out2) {
+    grid_t G;
+    grid_init(&G, W, H, D);
+    for (int i = 0; i < n; i++) edge_verts(&G, edges[i], &out2[2 * i], &out2[2 * i + 1]);
+}

@@ -82,6 +82,16 @@ int orc_correct(int W, int H, int D, const double *f, double *g,
                 double rel_eps, const int flags[7], int max_outer,
                 int nthreads, long long stats[8], int *cnt_out);
 
+/* Manifold labels: desc[v] = minimum reached along the steepest-descent
+ * pairing, asc[t] = maximum reached by the ascending tetrahedron walk, -1 if
+ * it leaves the domain.  Returns the number of walks that hit the step cap. */
+int orc_labels(int W, int H, int D, const double *data, int *desc, int *asc, int nthreads);
+
+/* cofaces of triangles (get_cell_tetra order, -1 when absent) and edge
+ * endpoints (higher id first), two ints per input id */
+void orc_face_cofaces(int W, int H, int D, int n, const int *faces, int *out2);
+void orc_edge_verts(int W, int H, int D, int n, const int *edges, int *out2);
+
 #ifdef __cplusplus
 }
 #endif

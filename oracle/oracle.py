@@ -49,6 +49,10 @@ def lib():
         L.orc_correct.argtypes = [ctypes.c_int] * 3 + [_f64p, _f64p, ctypes.c_double, _i32p, ctypes.c_int,
                                                         ctypes.c_int, _i64p, _i32p]
         L.orc_correct.restype = ctypes.c_int
+        L.orc_labels.argtypes = [ctypes.c_int] * 3 + [_f64p, _i32p, _i32p, ctypes.c_int]
+        L.orc_labels.restype = ctypes.c_int
+        L.orc_face_cofaces.argtypes = [ctypes.c_int] * 4 + [_i32p, _i32p]
+        L.orc_edge_verts.argtypes = [ctypes.c_int] * 4 + [_i32p, _i32p]
         _lib = L
     return _lib
 
@@ -129,3 +133,31 @@ def correct(f, g, dims, rel_eps, flags, max_outer=0, threads=1):
     stats = dict(outer_iterations=int(st[0]), cp_iterations=int(st[1]), oob=int(st[2]), converged=bool(st[3]),
                  initial_mismatch=[int(x) for x in st[4:8]])
     return gg, stats, cnt
+
+
+def labels(data, dims, threads: int = 1):
+    """Manifold labels (desc per vertex, asc per tetrahedron), reference ids."""
+    W, H, D = dims
+    V, E, F, T = counts(dims)
+    desc = np.empty(V, np.int32)
+    asc = np.empty(T, np.int32)
+    bad = lib().orc_labels(W, H, D, np.ascontiguousarray(data, np.float64).reshape(-1), desc, asc, threads)
+    if bad:
+        raise RuntimeError(f"{bad} label walks hit the step cap")
+    return desc, asc
+
+
+def face_cofaces(faces, dims):
+    """(n, 2) cofaces of triangles in get_cell_tetra order, -1 when absent."""
+    f = np.ascontiguousarray(faces, np.int32)
+    out = np.empty(2 * max(f.size, 1), np.int32)
+    lib().orc_face_cofaces(*dims, int(f.size), f if f.size else np.zeros(1, np.int32), out)
+    return out[: 2 * f.size].reshape(-1, 2)
+
+
+def edge_verts(edges, dims):
+    """(n, 2) endpoints of edges, higher id first."""
+    e = np.ascontiguousarray(edges, np.int32)
+    out = np.empty(2 * max(e.size, 1), np.int32)
+    lib().orc_edge_verts(*dims, int(e.size), e if e.size else np.zeros(1, np.int32), out)
+    return out[: 2 * e.size].reshape(-1, 2)

@@ -179,3 +179,47 @@ def test_correction_256_matches_reference_digest(gpu_ctx):
     assert rep["outer_iterations"] + 1 == m["iteration_number"]
     assert int((out != g).sum()) == m["changed"]
     assert sha(out) == m["fixed_sha256"]
+
+
+@pytest.mark.parametrize("path", FIXTURES[:8], ids=_id)
+def test_labels_match_oracle(gpu_ctx, path):
+    meta, z, f, g = load_fixture(path)
+    dims = tuple(meta["dims"])
+    for field in (f, g):
+        d, a = gpu_ctx.labels(field, dims)
+        od, oa = O.labels(field, dims)
+        assert np.array_equal(d, od)
+        assert np.array_equal(a, oa)
+
+
+@pytest.mark.parametrize("name,dims,kind,seed", EDGE_CASES, ids=[c[0] for c in EDGE_CASES])
+def test_labels_edge_cases(gpu_ctx, name, dims, kind, seed):
+    f = _edge_field(kind, dims, seed)
+    d, a = gpu_ctx.labels(f, dims)
+    od, oa = O.labels(f, dims)
+    assert np.array_equal(d, od) and np.array_equal(a, oa)
+
+
+@pytest.mark.parametrize("path", [p for p in FIXTURES if "_111" in os.path.basename(p)], ids=_id)
+def test_corrected_field_keeps_msc(gpu_ctx, path):
+    """Acceptance: the corrected field's re-extracted complex has the original's
+    critical cells, and the cofaces of every original 2-saddle reach the same
+    maxima as in the original (ascending separatrix labels).  Descending
+    separatrices are checked by the reference rules only at their first step,
+    so their agreement is measured, not required."""
+    meta, z, f, g = load_fixture(path)
+    dims = tuple(meta["dims"])
+    out, rep = gpu_ctx.correct(f, g, meta["rel"], meta["flags"], dims=dims)
+    assert all(len(x) == 0 for x in gpu_ctx.mismatch(f, out, dims))
+    P = gpu_ctx.extract(f, dims)
+    Q = gpu_ctx.extract(out, dims)
+    for a, b in zip(P, Q):
+        assert np.array_equal(a == -1, b == -1)
+    desc_f, asc_f = gpu_ctx.labels(f, dims)
+    desc_o, asc_o = gpu_ctx.labels(out, dims)
+    cof = O.face_cofaces(np.nonzero(P[2] == -1)[0], dims)
+    cof = cof[cof >= 0]
+    assert np.array_equal(asc_f[cof], asc_o[cof])
+    ends = O.edge_verts(np.nonzero(P[1] == -1)[0], dims).reshape(-1)
+    agree = float(np.mean(desc_f[ends] == desc_o[ends])) if ends.size else 1.0
+    assert agree > 0.5  # measured, typically close to 1
