@@ -186,7 +186,8 @@ def run_ours(args, rank, world, local_rank):
     def step():
         g_dev.copy_(g0_dev)
         torch.cuda.synchronize()
-        return ctx.correct_ptr(f_dev.data_ptr(), g_dev.data_ptr(), dims, REL_EPS, FLAGS, on_device=True)
+        return ctx.correct_ptr(f_dev.data_ptr(), g_dev.data_ptr(), dims, REL_EPS, FLAGS, on_device=True,
+                               use_graph=args.graph)
 
     rep = None
     for _ in range(args.warmup):
@@ -225,12 +226,13 @@ def run_ours(args, rank, world, local_rank):
     g0_pin = torch.from_numpy(g).pin_memory()
     g_pin = g0_pin.clone().pin_memory()
     g_pin.copy_(g0_pin)
-    ctx.correct_ptr(f_pin.data_ptr(), g_pin.data_ptr(), dims, REL_EPS, FLAGS, on_device=False)
+    ctx.correct_ptr(f_pin.data_ptr(), g_pin.data_ptr(), dims, REL_EPS, FLAGS, on_device=False, use_graph=args.graph)
     e2e_t = []
     for _ in range(args.steps):
         g_pin.copy_(g0_pin)
         t1 = time.perf_counter()
-        ctx.correct_ptr(f_pin.data_ptr(), g_pin.data_ptr(), dims, REL_EPS, FLAGS, on_device=False)
+        ctx.correct_ptr(f_pin.data_ptr(), g_pin.data_ptr(), dims, REL_EPS, FLAGS, on_device=False,
+                        use_graph=args.graph)
         e2e_t.append(time.perf_counter() - t1)
     e2e_step = float(np.mean(e2e_t))
     if dist:
@@ -254,7 +256,7 @@ def run_ours(args, rank, world, local_rank):
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": {"workload": f"powerlaw {SIZE}^3 seed=rank, sz decompression, eps=1e-4 x range, "
                                        f"flags {''.join(map(str, FLAGS))}",
-                           "parallelism": f"replicas x{world}",
+                           "parallelism": f"replicas x{world}", "loop": "cuda graph" if args.graph else "host",
                            "l2": "inputs and state larger than L2 (f and g alone are 268 MB)",
                            "outer_iterations": rep["outer_iterations"], "cp_rounds": rep["cp_rounds"],
                            "path_rounds": rep["path_rounds"], "initial_mismatch": rep["initial_mismatch"],
@@ -300,6 +302,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--graph", type=int, default=1, help="1: loop as a CUDA graph with a device-side flag")
     ap.add_argument("--sweep-only", type=int, default=0, metavar="SIZE",
                     help="profiling aid: only time the gradient sweep on a SIZE^3 field of the same kind")
     args = ap.parse_args()

@@ -930,6 +930,73 @@ dmtz_status dmtz_path_detect(dmtz_ctx *ctx, int W, int H, int D, const double *o
     return DMTZ_OK;
 }
 
+// ----------------------------------------------------------------------------- graph-driven loop
+// The host loop of main_3d.cu:6784-7149 as a state machine that runs on the
+// device: a CUDA graph holds a WHILE node whose body switches on the state,
+// runs that state's kernels, then lets one thread decide the next state and
+// the loop condition from the device-side counters.  States:
+//   CP     one critical-point round (fix rules, update, re-pair, mismatch)
+//   PDF    path phase: detect separatrix records, fix, update, re-pair, mismatch
+//   PCHECK detect separatrix records only (the reference's end-of-round check)
+//   PFIX   path phase on the records PCHECK just made (the reference detects
+//          them again at the start of its next outer iteration; same inputs,
+//          same records)
+namespace {
+enum { LS_CP = 0, LS_PDF = 1, LS_PCHECK = 2, LS_PFIX = 3, LS_DONE = 4 };
+struct LoopCtl {
+    int state, pvp, converged, pad;
+    long long rounds, max_rounds, outer, cp_rounds, path_rounds;
+    long long cc[4];
+    long long n_as, n_ds;
+    long long runs[4];  // body executions per state
+};
+}  // namespace
+
+__global__ void k_set_switch(const LoopCtl *ctl, cudaGraphConditionalHandle h) {
+    cudaGraphSetConditional(h, (unsigned)ctl->state);
+}
+
+__global__ void k_loop_ctl(LoopCtl *ctl, const unsigned long long *counters, cudaGraphConditionalHandle hwhile) {
+    LoopCtl c = *ctl;
+    const int st = c.state;
+    c.runs[st]++;
+    if (st != LS_PCHECK)
+        for (int k = 0; k < 4; k++) c.cc[k] = (long long)counters[k];
+    const bool cp_any = c.cc[0] > 0 || c.cc[1] > 0 || c.cc[2] > 0 || c.cc[3] > 0;
+    int next;
+    if (st == LS_CP) {
+        c.rounds++;
+        c.cp_rounds++;
+        next = cp_any ? LS_CP : (c.pvp ? LS_PDF : LS_DONE);
+    } else if (st == LS_PDF || st == LS_PFIX) {
+        c.rounds++;
+        c.path_rounds++;
+        c.n_as = c.n_ds = 0;
+        if (cp_any) {
+            c.outer++;
+            next = LS_CP;
+        } else {
+            next = LS_PCHECK;
+        }
+    } else {
+        c.n_as = (long long)counters[5];
+        c.n_ds = (long long)counters[6];
+        if (c.n_as + c.n_ds > 0) {
+            c.outer++;
+            next = LS_PFIX;
+        } else {
+            next = LS_DONE;
+        }
+    }
+    if (next != LS_DONE && c.rounds >= c.max_rounds) {
+        c.converged = 0;
+        next = LS_DONE;
+    }
+    c.state = next;
+    *ctl = c;
+    cudaGraphSetConditional(hwhile, next != LS_DONE ? 1u : 0u);
+}
+
 // ----------------------------------------------------------------------------- phase timers
 namespace {
 enum { PH_PAIR = 0, PH_FIXCP, PH_PATH, PH_FIXPATH, PH_APPLY, PH_SETUP, PH_N };
@@ -966,6 +1033,103 @@ struct PhaseTimer {
     }
 };
 }  // namespace
+
+// Build and run the graph-driven loop.  Returns the final LoopCtl in *out.
+static dmtz_status run_graph_loop(dmtz_ctx *ctx, const Grid &g, const RuleCtx &rc, const CpLists &L,
+                                  const PathRec &PR, const FieldState &Qs, double range, int ps, int pt,
+                                  LoopCtl init, LoopCtl *out) {
+    cudaStream_t st = ctx->stream;
+    const unsigned pgrid = persistent_grid();
+    LoopCtl *dctl = nullptr;
+    CK(dalloc(&dctl, 1));
+    CK(cudaMemcpyAsync(dctl, &init, sizeof(LoopCtl), cudaMemcpyHostToDevice, st));
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    dmtz_status res = DMTZ_OK;
+    do {
+        if (cudaGraphCreate(&graph, 0) != cudaSuccess) { res = DMTZ_ERR_CUDA; break; }
+        cudaGraphConditionalHandle hwhile;
+        if (cudaGraphConditionalHandleCreate(&hwhile, graph, 1, cudaGraphCondAssignDefault) != cudaSuccess) {
+            res = DMTZ_ERR_CUDA;
+            break;
+        }
+        cudaGraphNodeParams wp = {};
+        wp.type = cudaGraphNodeTypeConditional;
+        wp.conditional.handle = hwhile;
+        wp.conditional.type = cudaGraphCondTypeWhile;
+        wp.conditional.size = 1;
+        cudaGraphNode_t wnode;
+        if (cudaGraphAddNode(&wnode, graph, nullptr, nullptr, 0, &wp) != cudaSuccess) { res = DMTZ_ERR_CUDA; break; }
+        cudaGraph_t body = wp.conditional.phGraph_out[0];
+        cudaGraphConditionalHandle hsw;
+        if (cudaGraphConditionalHandleCreate(&hsw, body, 0, 0) != cudaSuccess) { res = DMTZ_ERR_CUDA; break; }
+        // body: set the switch from the state, switch over the four states, decide
+        cudaGraphNode_t n_set, n_sw, n_ctl;
+        {
+            if (cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+                res = DMTZ_ERR_CUDA;
+                break;
+            }
+            k_set_switch<<<1, 1, 0, st>>>(dctl, hsw);
+            cudaGraph_t tmp;
+            if (cudaStreamEndCapture(st, &tmp) != cudaSuccess) { res = DMTZ_ERR_CUDA; break; }
+            size_t nn = 1;
+            cudaGraphGetNodes(body, &n_set, &nn);
+        }
+        cudaGraphNodeParams sp = {};
+        sp.type = cudaGraphNodeTypeConditional;
+        sp.conditional.handle = hsw;
+        sp.conditional.type = cudaGraphCondTypeSwitch;
+        sp.conditional.size = 4;
+        if (cudaGraphAddNode(&n_sw, body, &n_set, nullptr, 1, &sp) != cudaSuccess) { res = DMTZ_ERR_CUDA; break; }
+        for (int state = 0; state < 4 && res == DMTZ_OK; state++) {
+            cudaGraph_t child = sp.conditional.phGraph_out[state];
+            if (cudaStreamBeginCaptureToGraph(st, child, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+                res = DMTZ_ERR_CUDA;
+                break;
+            }
+            if (state == LS_PDF || state == LS_PCHECK) {
+                cudaMemsetAsync(ctx->counters + 5, 0, 2 * sizeof(unsigned long long), st);
+                k_path_as<<<pgrid, kBlock, 0, st>>>(g, ctx->sad2, ctx->counters + 10, ctx->P.tcode, ctx->Q.tcode,
+                                                     ctx->succ, PR, g.T + 16, ctx->errword);
+                k_path_ds<<<pgrid, kBlock, 0, st>>>(rc, PR);
+            }
+            if (state != LS_PCHECK) {
+                cudaMemsetAsync(ctx->counters + 4, 0, sizeof(unsigned long long), st);
+                if (state == LS_CP) k_fix_cp<<<pgrid, kBlock, 0, st>>>(rc, L, ps);
+                else k_fix_path<<<pgrid, kBlock, 0, st>>>(rc, PR);
+                k_apply<<<pgrid, kBlock, 0, st>>>(rc, range, pt, 1, ctx->changed, nullptr);
+                repair_dirty(ctx, g, Qs, ctx->P.crit, state == LS_CP ? (ps == 1) : 1);
+            }
+            cudaGraph_t tmp;
+            if (cudaStreamEndCapture(st, &tmp) != cudaSuccess) res = DMTZ_ERR_CUDA;
+        }
+        if (res != DMTZ_OK) break;
+        {
+            if (cudaStreamBeginCaptureToGraph(st, body, &n_sw, nullptr, 1, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+                res = DMTZ_ERR_CUDA;
+                break;
+            }
+            k_loop_ctl<<<1, 1, 0, st>>>(dctl, ctx->counters, hwhile);
+            cudaGraph_t tmp;
+            if (cudaStreamEndCapture(st, &tmp) != cudaSuccess) { res = DMTZ_ERR_CUDA; break; }
+            (void)n_ctl;
+        }
+        if (cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) { res = DMTZ_ERR_CUDA; break; }
+        if (cudaGraphLaunch(exec, st) != cudaSuccess) { res = DMTZ_ERR_CUDA; break; }
+        if (cudaMemcpyAsync(out, dctl, sizeof(LoopCtl), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess)
+            res = DMTZ_ERR_CUDA;
+    } while (0);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    cudaFree(dctl);
+    if (res != DMTZ_OK) {
+        cudaGetLastError();
+        return fail(ctx, res, "building or running the loop graph failed");
+    }
+    return DMTZ_OK;
+}
 
 // ----------------------------------------------------------------------------- the correction loop
 dmtz_status dmtz_correct(dmtz_ctx *ctx, int W, int H, int D, const double *orig, double *decp, int on_device,
@@ -1033,7 +1197,35 @@ dmtz_status dmtz_correct(dmtz_ctx *ctx, int W, int H, int D, const double *orig,
     L.n = ctx->counters;
     PathRec PR{ctx->as_tet, ctx->as_cur, ctx->ds_edge, ctx->ds_vert, ctx->counters + 5};
     auto cp_any = [&]() { return cc[0] > 0 || cc[1] > 0 || cc[2] > 0 || cc[3] > 0; };
-    while (n_as > 0 || n_ds > 0 || n_wall > 0 || cp_any()) {
+    if (opts->use_graph) {
+        // same loop, decided on the device (see run_graph_loop)
+        LoopCtl c;
+        memset(&c, 0, sizeof(c));
+        c.pvp = pvp;
+        c.converged = 1;
+        c.max_rounds = max_rounds;
+        c.outer = 1;
+        for (int k = 0; k < 4; k++) c.cc[k] = cc[k];
+        c.state = cp_any() ? LS_CP : (pvp ? LS_PDF : LS_DONE);
+        LoopCtl fin = c;
+        if (c.state != LS_DONE) {
+            pt_.begin(PH_PAIR);
+            if ((s = run_graph_loop(ctx, g, rc, L, PR, Qs, range, ps, pt, c, &fin)) != DMTZ_OK) return s;
+            pt_.end();
+            // kernels per body run: switch + control, plus each state's own
+            ctx->launches += 2 * (fin.runs[0] + fin.runs[1] + fin.runs[2] + fin.runs[3]) + 11 * fin.runs[LS_CP] +
+                             13 * fin.runs[LS_PDF] + 2 * fin.runs[LS_PCHECK] + 11 * fin.runs[LS_PFIX];
+        }
+        R.outer_iterations = fin.outer;
+        R.cp_rounds = fin.cp_rounds;
+        R.path_rounds = fin.path_rounds;
+        for (int k = 0; k < 4; k++) cc[k] = fin.cc[k];
+        n_as = fin.n_as;
+        n_ds = fin.n_ds;
+        n_wall = 0;
+        converged = fin.converged;
+    }
+    while (!opts->use_graph && (n_as > 0 || n_ds > 0 || n_wall > 0 || cp_any())) {
         if (rounds >= max_rounds) {
             converged = 0;
             break;

@@ -70,11 +70,13 @@ def test_path_detect_matches_oracle(gpu_ctx, path):
     assert sorted(zip(got[2].tolist(), got[3].tolist())) == sorted(zip(d_e.tolist(), d_v.tolist()))
 
 
+@pytest.mark.parametrize("use_graph", [0, 1], ids=["host_loop", "graph_loop"])
 @pytest.mark.parametrize("path", FIXTURES, ids=_id)
-def test_correction_matches_reference(gpu_ctx, path):
+def test_correction_matches_reference(gpu_ctx, path, use_graph):
     meta, z, f, g = load_fixture(path)
     dims = tuple(meta["dims"])
-    out, rep, cnt = gpu_ctx.correct(f, g, meta["rel"], meta["flags"], dims=dims, return_counter=True)
+    out, rep, cnt = gpu_ctx.correct(f, g, meta["rel"], meta["flags"], dims=dims, return_counter=True,
+                                    use_graph=use_graph)
     ref = reference_fixed(z, g)
     assert rep["converged"]
     bad = np.nonzero(out != ref)[0]
@@ -174,9 +176,12 @@ def test_correction_256_matches_reference_digest(gpu_ctx):
     dims = tuple(m["dims"])
     f, g = case_fields(m["kind"], dims, m["seed"], m["rel"], m["decomp"], m["kw"])
     f, g = f.reshape(-1), g.reshape(-1)
-    out, rep = gpu_ctx.correct(f, g, m["rel"], m["flags"], dims=dims)
-    assert rep["converged"]
-    assert rep["outer_iterations"] + 1 == m["iteration_number"]
+    for use_graph in (0, 1):
+        out, rep = gpu_ctx.correct(f, g, m["rel"], m["flags"], dims=dims, use_graph=use_graph)
+        assert rep["converged"]
+        assert rep["outer_iterations"] + 1 == m["iteration_number"]
+        assert int((out != g).sum()) == m["changed"]
+        assert sha(out) == m["fixed_sha256"]
     assert int((out != g).sum()) == m["changed"]
     assert sha(out) == m["fixed_sha256"]
 
