@@ -89,6 +89,13 @@ def load_library(build_if_missing: bool = True):
     L.dmtz_profile_sweep.argtypes = [_vp, _int, _int, _int, _vp, _vp, _int, _int, _f64p]
     L.dmtz_labels.argtypes = [_vp, _int, _int, _int, _vp, _int, _i32p, _i32p]
     L.dmtz_labels.restype = _int
+    L.dmtz_correct_batch.argtypes = [_vp, _int, _vp, ctypes.POINTER(Opts), _vp, _vp, _int]
+    L.dmtz_set_tuning.argtypes = [_vp, _int, _int]
+    L.dmtz_get_tuning.argtypes = [_vp, ctypes.POINTER(_int), ctypes.POINTER(_int)]
+    L.dmtz_autotune.argtypes = [_vp, _int, _int, _int, _vp, _vp, _int, ctypes.POINTER(_int), ctypes.POINTER(ctypes.c_double)]
+    L.dmtz_device_name.argtypes = [_vp, ctypes.c_char_p, _int]
+    for fn in ("dmtz_correct_batch", "dmtz_set_tuning", "dmtz_get_tuning", "dmtz_autotune", "dmtz_device_name"):
+        getattr(L, fn).restype = _int
     for fn in ("dmtz_ctx_create", "dmtz_cell_counts", "dmtz_extract", "dmtz_mismatch", "dmtz_fix_round",
                "dmtz_path_detect", "dmtz_correct", "dmtz_profile_sweep"):
         getattr(L, fn).restype = _int
@@ -116,6 +123,13 @@ def _dims_of(a, dims):
         raise ValueError("pass dims=(W, H, D) for flat arrays")
     D, H, W = a.shape
     return (W, H, D)
+
+
+class Instance(ctypes.Structure):
+    """One field of dmtz_correct_batch (see include/dmtz.h)."""
+    _fields_ = [("W", ctypes.c_int), ("H", ctypes.c_int), ("D", ctypes.c_int), ("dtype", ctypes.c_int),
+                ("orig", ctypes.c_void_p), ("decp", ctypes.c_void_p), ("out", ctypes.c_void_p),
+                ("rel_eps", ctypes.c_double)]
 
 
 class Context:
@@ -208,6 +222,57 @@ class Context:
         rep = r.as_dict()
         rep["edited_vertices"] = int((gg != _flat(g)).sum())
         return (gg, rep, cnt) if return_counter else (gg, rep)
+
+    def correct_batch(self, fields, flags=(1, 1, 1, 0, 0, 0, 0), workers=8, max_rounds=0, use_graph=1):
+        """Correct many fields of any sizes in one call.
+
+        fields: iterable of (f, g, rel_eps) with f, g float32 or float64 arrays of
+        shape (D, H, W).  Returns a list of (corrected float64 array (D, H, W),
+        report dict, status int); status 0 = converged."""
+        fields = list(fields)
+        keep, insts, outs = [], [], []
+        for f, g, rel in fields:
+            f = np.ascontiguousarray(f)
+            g = np.ascontiguousarray(g, dtype=f.dtype)
+            if f.dtype not in (np.float32, np.float64) or f.ndim != 3 or g.shape != f.shape:
+                raise ValueError("fields must be float32/float64 arrays of shape (D, H, W)")
+            D, H, W = f.shape
+            out = np.empty(f.shape, np.float64)
+            keep += [f, g]
+            outs.append(out)
+            insts.append(Instance(W, H, D, 0 if f.dtype == np.float64 else 1, f.ctypes.data, g.ctypes.data,
+                                  out.ctypes.data, float(rel)))
+        n = len(insts)
+        arr = (Instance * max(n, 1))(*insts)
+        reps = (Report * max(n, 1))()
+        sts = np.zeros(max(n, 1), np.int32)
+        o = Opts(*[int(x) for x in flags], int(max_rounds), int(use_graph))
+        self._L.dmtz_correct_batch(self._h, n, ctypes.cast(arr, ctypes.c_void_p), ctypes.byref(o),
+                                   ctypes.cast(reps, ctypes.c_void_p), sts.ctypes.data, int(workers))
+        return [(outs[i], reps[i].as_dict(), int(sts[i])) for i in range(n)]
+
+    def device_name(self):
+        buf = ctypes.create_string_buffer(256)
+        self._check(self._L.dmtz_device_name(self._h, buf, 256))
+        return buf.value.decode()
+
+    def set_tuning(self, shape, blocks_per_sm):
+        self._check(self._L.dmtz_set_tuning(self._h, int(shape), int(blocks_per_sm)))
+
+    def get_tuning(self):
+        a, b = _int(), _int()
+        self._check(self._L.dmtz_get_tuning(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def autotune(self, f, g, dims=None):
+        """Time the gradient sweep for every brick shape / blocks-per-SM choice on
+        (f, g); keep the fastest in this context.  Returns (shape, blocks_per_sm, ms)."""
+        dims = _dims_of(np.asarray(f), dims)
+        ff, gg = _flat(f), _flat(g)
+        best = (_int * 2)()
+        ms = ctypes.c_double()
+        self._check(self._L.dmtz_autotune(self._h, *dims, ff.ctypes.data, gg.ctypes.data, 0, best, ctypes.byref(ms)))
+        return best[0], best[1], ms.value
 
     def correct_ptr(self, f_ptr: int, g_ptr: int, dims, rel_eps, flags=(1, 1, 1, 0, 0, 0, 0), on_device=True,
                     max_rounds=0, use_graph=0):

@@ -14,7 +14,9 @@
 
 #include <algorithm>
 #include <chrono>
+#include <atomic>
 #include <mutex>
+#include <thread>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -70,15 +72,15 @@ __global__ void k_mismatch_scan(Grid g, const uint32_t *crit_d, const uint32_t *
 // state of an anchor depends on values no further away (vertex pass +-1, edge
 // pass +-2, first triangle pass -3..2, second edge pass +-3, second triangle
 // pass +-4, criticality -5..4)
-__global__ void k_mark_dirty(Grid g, int nbx, int nby, int nbz, const i64 *verts, const unsigned long long *nverts,
-                             uint8_t *flags) {
+__global__ void k_mark_dirty(Grid g, int nbx, int nby, int nbz, int sx, int sy, int sz, const i64 *verts,
+                             const unsigned long long *nverts, uint8_t *flags) {
     const i64 n = (i64)*nverts;
     for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
         int x, y, z;
         decode_v(g, verts[i], x, y, z);
-        const int x0 = max(x - 5, 0) / DMTZ_BX, x1 = min(x + 5, g.W - 1) / DMTZ_BX;
-        const int y0 = max(y - 5, 0) / DMTZ_BY, y1 = min(y + 5, g.H - 1) / DMTZ_BY;
-        const int z0 = max(z - 5, 0) / DMTZ_BZ, z1 = min(z + 5, g.D - 1) / DMTZ_BZ;
+        const int x0 = max(x - 5, 0) / sx, x1 = min(x + 5, g.W - 1) / sx;
+        const int y0 = max(y - 5, 0) / sy, y1 = min(y + 5, g.H - 1) / sy;
+        const int z0 = max(z - 5, 0) / sz, z1 = min(z + 5, g.D - 1) / sz;
         for (int bz = z0; bz <= z1; bz++)
             for (int by = y0; by <= y1; by++)
                 for (int bx = x0; bx <= x1; bx++) flags[bx + (i64)nbx * (by + (i64)nby * bz)] = 1;
@@ -508,6 +510,9 @@ struct dmtz_ctx {
     int *errword = nullptr;
     uint8_t *changed = nullptr;
     int64_t launches = 0;  // kernels launched by the current call
+    int tune_shape = 0;    // brick shape (DMTZ_SHAPES) chosen by dmtz_autotune
+    int tune_bps = 16;     // sweep blocks per SM
+    std::vector<dmtz_ctx *> pool;  // worker contexts of dmtz_correct_batch
 };
 
 namespace {
@@ -553,11 +558,12 @@ dmtz_status alloc_field(dmtz_ctx *ctx, DevField &d, i64 V) {
     return DMTZ_OK;
 }
 
-i64 bricks_of(const Grid &g, int &nbx, int &nby, int &nbz);
+i64 bricks_of(const Grid &g, int shape, int &nbx, int &nby, int &nbz);
 
 dmtz_status ensure(dmtz_ctx *ctx, const Grid &g) {
     int nbx, nby, nbz;
-    const i64 nbr = bricks_of(g, nbx, nby, nbz);
+    i64 nbr = 0;
+    for (int sh = 0; sh < DMTZ_NSHAPES; sh++) nbr = std::max(nbr, bricks_of(g, sh, nbx, nby, nbz));
     if (g.V <= ctx->capV && g.E <= ctx->capE && g.F <= ctx->capF && g.T <= ctx->capT && nbr <= ctx->capB) return DMTZ_OK;
     free_all(ctx);
     const i64 V = g.V;
@@ -592,37 +598,43 @@ FieldState view(const DevField &d, const double *val) {
 unsigned persistent_grid();
 
 // five passes + criticality (and mismatch lists when crit_o is given)
-i64 bricks_of(const Grid &g, int &nbx, int &nby, int &nbz) {
-    nbx = (g.W + DMTZ_BX - 1) / DMTZ_BX;
-    nby = (g.H + DMTZ_BY - 1) / DMTZ_BY;
-    nbz = (g.D + DMTZ_BZ - 1) / DMTZ_BZ;
+i64 bricks_of(const Grid &g, int shape, int &nbx, int &nby, int &nbz) {
+    nbx = (g.W + DMTZ_SHAPES[shape][0] - 1) / DMTZ_SHAPES[shape][0];
+    nby = (g.H + DMTZ_SHAPES[shape][1] - 1) / DMTZ_SHAPES[shape][1];
+    nbz = (g.D + DMTZ_SHAPES[shape][2] - 1) / DMTZ_SHAPES[shape][2];
     return (i64)nbx * nby * nbz;
 }
+// brick coordinates are packed as bx | by << 11 | bz << 22
+bool shape_fits(const Grid &g, int shape) {
+    int nbx, nby, nbz;
+    bricks_of(g, shape, nbx, nby, nbz);
+    return nbx <= 2048 && nby <= 2048 && nbz <= 1024;
+}
 
-unsigned sweep_grid(i64 nb) {
-    static unsigned cap = 0;
-    if (!cap) cap = persistent_grid() * 2;  // 16 blocks of 128 threads per SM
+unsigned sweep_grid(const dmtz_ctx *ctx, i64 nb) {
+    const unsigned cap = (unsigned)(persistent_grid() / 8) * (unsigned)ctx->tune_bps;
     return (unsigned)std::max<i64>(1, std::min<i64>(nb, cap));
 }
 
 // the five pairing passes and the criticality pass over a set of bricks
 void sweep(dmtz_ctx *ctx, const Grid &g, const FieldState &s, const BrickList &bl, i64 nb_max) {
-    const unsigned gr = sweep_grid(nb_max);
+    const unsigned gr = sweep_grid(ctx, nb_max);
     cudaStream_t st = ctx->stream;
-    k_sweep<PASS_VERTEX><<<gr, DMTZ_BRICK, 0, st>>>(g, s, bl);
-    k_sweep<PASS_E2><<<gr, DMTZ_BRICK, 0, st>>>(g, s, bl);
-    k_sweep<PASS_F3><<<gr, DMTZ_BRICK, 0, st>>>(g, s, bl);
-    k_sweep<PASS_E4><<<gr, DMTZ_BRICK, 0, st>>>(g, s, bl);
-    k_sweep<PASS_F5><<<gr, DMTZ_BRICK, 0, st>>>(g, s, bl);
-    k_sweep<PASS_CRIT><<<gr, DMTZ_BRICK, 0, st>>>(g, s, bl);
+    launch_pass<PASS_VERTEX>(g, s, bl, gr, st);
+    launch_pass<PASS_E2>(g, s, bl, gr, st);
+    launch_pass<PASS_F3>(g, s, bl, gr, st);
+    launch_pass<PASS_E4>(g, s, bl, gr, st);
+    launch_pass<PASS_F5>(g, s, bl, gr, st);
+    launch_pass<PASS_CRIT>(g, s, bl, gr, st);
     ctx->launches += 6;
 }
 
-BrickList all_bricks(const Grid &g, i64 &nb) {
+BrickList all_bricks(const Grid &g, int shape, i64 &nb) {
     BrickList bl;
     bl.list = nullptr;
     bl.n = nullptr;
-    nb = bricks_of(g, bl.nbx, bl.nby, bl.nbz);
+    bl.shape = shape;
+    nb = bricks_of(g, shape, bl.nbx, bl.nby, bl.nbz);
     return bl;
 }
 
@@ -639,7 +651,7 @@ void scan_mismatch(dmtz_ctx *ctx, const Grid &g, const uint32_t *crit_d, const u
 // full gradient of one field (and its mismatch lists when crit_o is given)
 void run_pairing(dmtz_ctx *ctx, const Grid &g, const FieldState &s, const uint32_t *crit_o, int want_saddles) {
     i64 nb;
-    const BrickList bl = all_bricks(g, nb);
+    const BrickList bl = all_bricks(g, ctx->tune_shape, nb);
     sweep(ctx, g, s, bl, nb);
     if (crit_o) scan_mismatch(ctx, g, s.crit, crit_o, want_saddles);
 }
@@ -648,10 +660,12 @@ void run_pairing(dmtz_ctx *ctx, const Grid &g, const FieldState &s, const uint32
 // (ctx->reqlist), then rebuild the mismatch lists
 void repair_dirty(dmtz_ctx *ctx, const Grid &g, const FieldState &s, const uint32_t *crit_o, int want_saddles) {
     int nbx, nby, nbz;
-    const i64 nb = bricks_of(g, nbx, nby, nbz);
+    const int shape = ctx->tune_shape;
+    const i64 nb = bricks_of(g, shape, nbx, nby, nbz);
     cudaStream_t st = ctx->stream;
     cudaMemsetAsync(ctx->counters + 11, 0, sizeof(unsigned long long), st);
-    k_mark_dirty<<<persistent_grid(), kBlock, 0, st>>>(g, nbx, nby, nbz, ctx->reqlist, ctx->counters + 4,
+    k_mark_dirty<<<persistent_grid(), kBlock, 0, st>>>(g, nbx, nby, nbz, DMTZ_SHAPES[shape][0], DMTZ_SHAPES[shape][1],
+                                                        DMTZ_SHAPES[shape][2], ctx->reqlist, ctx->counters + 4,
                                                         ctx->brick_flags);
     k_compact_bricks<<<persistent_grid(), kBlock, 0, st>>>(nbx, nby, nbz, ctx->brick_flags, ctx->brick_list,
                                                             ctx->counters + 11);
@@ -660,6 +674,7 @@ void repair_dirty(dmtz_ctx *ctx, const Grid &g, const FieldState &s, const uint3
     bl.list = ctx->brick_list;
     bl.n = ctx->counters + 11;
     bl.nbx = nbx; bl.nby = nby; bl.nbz = nbz;
+    bl.shape = shape;
     sweep(ctx, g, s, bl, nb);
     scan_mismatch(ctx, g, s.crit, crit_o, want_saddles);
 }
@@ -729,9 +744,9 @@ unsigned persistent_grid() {
 dmtz_status check_dims(dmtz_ctx *ctx, int W, int H, int D, Grid &g) {
     if (!ctx) return DMTZ_ERR_ARG;
     if (W < 2 || H < 2 || D < 2) return fail(ctx, DMTZ_ERR_ARG, "dims must be >= 2");
-    if (W > 2047 * DMTZ_BX || H > 2047 * DMTZ_BY || D > 1023 * DMTZ_BZ)
-        return fail(ctx, DMTZ_ERR_ARG, "dims exceed 16376 x 8188 x 4092");
     g = make_grid(W, H, D);
+    if (!shape_fits(g, 0)) return fail(ctx, DMTZ_ERR_ARG, "dims exceed 16384 x 8192 x 4096");
+    if (!shape_fits(g, ctx->tune_shape)) ctx->tune_shape = 0;
     return DMTZ_OK;
 }
 
@@ -772,6 +787,8 @@ dmtz_status dmtz_ctx_create(dmtz_ctx **out, int device) {
 
 void dmtz_ctx_destroy(dmtz_ctx *ctx) {
     if (!ctx) return;
+    for (dmtz_ctx *w : ctx->pool) dmtz_ctx_destroy(w);
+    ctx->pool.clear();
     cudaSetDevice(ctx->device);
     free_all(ctx);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -1360,6 +1377,137 @@ dmtz_status dmtz_labels(dmtz_ctx *ctx, int W, int H, int D, const double *data, 
     return s;
 }
 
+dmtz_status dmtz_device_name(const dmtz_ctx *ctx, char *buf, int len) {
+    if (!ctx || !buf || len < 1) return DMTZ_ERR_ARG;
+    cudaDeviceProp p;
+    if (cudaGetDeviceProperties(&p, ctx->device) != cudaSuccess) return DMTZ_ERR_CUDA;
+    snprintf(buf, (size_t)len, "%s", p.name);
+    return DMTZ_OK;
+}
+
+dmtz_status dmtz_set_tuning(dmtz_ctx *ctx, int shape, int blocks_per_sm) {
+    if (!ctx || shape < 0 || shape >= DMTZ_NSHAPES || blocks_per_sm < 1 || blocks_per_sm > 64) return DMTZ_ERR_ARG;
+    ctx->tune_shape = shape;
+    ctx->tune_bps = blocks_per_sm;
+    return DMTZ_OK;
+}
+
+dmtz_status dmtz_get_tuning(const dmtz_ctx *ctx, int *shape, int *blocks_per_sm) {
+    if (!ctx) return DMTZ_ERR_ARG;
+    if (shape) *shape = ctx->tune_shape;
+    if (blocks_per_sm) *blocks_per_sm = ctx->tune_bps;
+    return DMTZ_OK;
+}
+
+dmtz_status dmtz_autotune(dmtz_ctx *ctx, int W, int H, int D, const double *orig, const double *decp, int on_device,
+                          int best[2], double *best_ms) {
+    Grid g;
+    dmtz_status s = check_dims(ctx, W, H, D, g);
+    if (s != DMTZ_OK) return s;
+    CK(cudaSetDevice(ctx->device));
+    if ((s = ensure(ctx, g)) != DMTZ_OK) return s;
+    if ((s = upload(ctx, ctx->f, orig, g.V, on_device)) != DMTZ_OK) return s;
+    if ((s = upload(ctx, ctx->g, decp, g.V, on_device)) != DMTZ_OK) return s;
+    cudaStream_t st = ctx->stream;
+    const FieldState Ps = view(ctx->P, ctx->f), Qs = view(ctx->Q, ctx->g);
+    run_pairing(ctx, g, Ps, nullptr, 1);
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    static const int bps_opts[4] = {4, 8, 16, 32};
+    double best_t = 1e30;
+    int bs = 0, bb = 16;
+    for (int sh = 0; sh < DMTZ_NSHAPES; sh++) {
+        if (!shape_fits(g, sh)) continue;
+        for (int bi = 0; bi < 4; bi++) {
+            ctx->tune_shape = sh;
+            ctx->tune_bps = bps_opts[bi];
+            run_pairing(ctx, g, Qs, nullptr, 1);  // warm
+            float t_min = 1e30f;
+            for (int r = 0; r < 3; r++) {
+                CK(cudaEventRecord(e0, st));
+                run_pairing(ctx, g, Qs, nullptr, 1);
+                CK(cudaEventRecord(e1, st));
+                CK(cudaEventSynchronize(e1));
+                float t = 0;
+                cudaEventElapsedTime(&t, e0, e1);
+                t_min = std::min(t_min, t);
+            }
+            if (t_min < best_t) {
+                best_t = t_min;
+                bs = sh;
+                bb = bps_opts[bi];
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx->tune_shape = bs;
+    ctx->tune_bps = bb;
+    if (best) {
+        best[0] = bs;
+        best[1] = bb;
+    }
+    if (best_ms) *best_ms = best_t;
+    CK(cudaGetLastError());
+    return DMTZ_OK;
+}
+
+dmtz_status dmtz_correct_batch(dmtz_ctx *ctx, int n, const dmtz_instance *inst, const dmtz_opts *opts,
+                               dmtz_report *reports, dmtz_status *status, int workers) {
+    if (!ctx || n < 0 || (n > 0 && (!inst || !opts))) return DMTZ_ERR_ARG;
+    if (workers < 1) workers = 8;
+    workers = std::min(workers, std::max(n, 1));
+    while ((int)ctx->pool.size() < workers) {
+        dmtz_ctx *w = nullptr;
+        const dmtz_status cs = dmtz_ctx_create(&w, ctx->device);
+        if (cs != DMTZ_OK) return fail(ctx, cs, "cannot create a worker context");
+        ctx->pool.push_back(w);
+    }
+    std::atomic<int> next(0);
+    std::vector<dmtz_status> st((size_t)n, DMTZ_OK);
+    auto work = [&](dmtz_ctx *w) {
+        w->tune_shape = ctx->tune_shape;
+        w->tune_bps = ctx->tune_bps;
+        std::vector<double> fo, go;
+        for (int i = next++; i < n; i = next++) {
+            const dmtz_instance &I = inst[i];
+            const size_t V = (size_t)std::max(I.W, 0) * (size_t)std::max(I.H, 0) * (size_t)std::max(I.D, 0);
+            if (!I.orig || !I.decp || !I.out || V == 0 || (I.dtype != DMTZ_F64 && I.dtype != DMTZ_F32)) {
+                st[i] = DMTZ_ERR_ARG;
+                continue;
+            }
+            const double *f64 = (const double *)I.orig;
+            if (I.dtype == DMTZ_F32) {  // float32 widens exactly; the correction runs in float64
+                fo.resize(V);
+                const float *a = (const float *)I.orig, *b = (const float *)I.decp;
+                for (size_t k = 0; k < V; k++) {
+                    fo[k] = a[k];
+                    I.out[k] = b[k];
+                }
+                f64 = fo.data();
+            } else {
+                memcpy(I.out, I.decp, V * sizeof(double));
+            }
+            dmtz_report r;
+            st[i] = dmtz_correct(w, I.W, I.H, I.D, f64, I.out, 0, I.rel_eps, opts, &r, nullptr);
+            if (reports) reports[i] = r;
+        }
+    };
+    std::vector<std::thread> th;
+    for (int k = 0; k < workers; k++) th.emplace_back(work, ctx->pool[k]);
+    for (auto &t : th) t.join();
+    dmtz_status res = DMTZ_OK;
+    for (int i = 0; i < n; i++) {
+        if (status) status[i] = st[i];
+        if (st[i] != DMTZ_OK && res == DMTZ_OK) {
+            res = st[i];
+            ctx->err = "instance " + std::to_string(i) + " failed with status " + std::to_string((int)st[i]);
+        }
+    }
+    return res;
+}
+
 dmtz_status dmtz_profile_sweep(dmtz_ctx *ctx, int W, int H, int D, const double *orig, const double *decp,
                                int on_device, int reps, double ms[7]) {
     Grid g;
@@ -1379,21 +1527,21 @@ dmtz_status dmtz_profile_sweep(dmtz_ctx *ctx, int W, int H, int D, const double 
     double acc[6] = {0, 0, 0, 0, 0, 0};
     float total = 0;
     i64 nb;
-    const BrickList bl = all_bricks(g, nb);
-    const unsigned gr = sweep_grid(nb);
+    const BrickList bl = all_bricks(g, ctx->tune_shape, nb);
+    const unsigned gr = sweep_grid(ctx, nb);
     for (int r = 0; r < reps; r++) {
         CK(cudaEventRecord(ev[0], st));
-        k_sweep<PASS_VERTEX><<<gr, DMTZ_BRICK, 0, st>>>(g, Qs, bl);
+        launch_pass<PASS_VERTEX>(g, Qs, bl, gr, st);
         CK(cudaEventRecord(ev[1], st));
-        k_sweep<PASS_E2><<<gr, DMTZ_BRICK, 0, st>>>(g, Qs, bl);
+        launch_pass<PASS_E2>(g, Qs, bl, gr, st);
         CK(cudaEventRecord(ev[2], st));
-        k_sweep<PASS_F3><<<gr, DMTZ_BRICK, 0, st>>>(g, Qs, bl);
+        launch_pass<PASS_F3>(g, Qs, bl, gr, st);
         CK(cudaEventRecord(ev[3], st));
-        k_sweep<PASS_E4><<<gr, DMTZ_BRICK, 0, st>>>(g, Qs, bl);
+        launch_pass<PASS_E4>(g, Qs, bl, gr, st);
         CK(cudaEventRecord(ev[4], st));
-        k_sweep<PASS_F5><<<gr, DMTZ_BRICK, 0, st>>>(g, Qs, bl);
+        launch_pass<PASS_F5>(g, Qs, bl, gr, st);
         CK(cudaEventRecord(ev[5], st));
-        k_sweep<PASS_CRIT><<<gr, DMTZ_BRICK, 0, st>>>(g, Qs, bl);
+        launch_pass<PASS_CRIT>(g, Qs, bl, gr, st);
         CK(cudaEventRecord(ev[6], st));
         CK(cudaEventSynchronize(ev[6]));
         for (int k = 0; k < 6; k++) {
@@ -1483,13 +1631,13 @@ extern "C" dmtz_status dmtz_extract_noalloc(int W, int H, int D, const double *d
     s.tcode = nullptr;
     cudaStream_t st = (cudaStream_t)stream;
     i64 nb;
-    const BrickList bl = all_bricks(g, nb);
-    const unsigned gb = sweep_grid(nb);
-    k_sweep<PASS_VERTEX><<<gb, DMTZ_BRICK, 0, st>>>(g, s, bl);
-    k_sweep<PASS_E2><<<gb, DMTZ_BRICK, 0, st>>>(g, s, bl);
-    k_sweep<PASS_F3><<<gb, DMTZ_BRICK, 0, st>>>(g, s, bl);
-    k_sweep<PASS_E4><<<gb, DMTZ_BRICK, 0, st>>>(g, s, bl);
-    k_sweep<PASS_F5><<<gb, DMTZ_BRICK, 0, st>>>(g, s, bl);
+    const BrickList bl = all_bricks(g, 0, nb);
+    const unsigned gb = (unsigned)std::max<i64>(1, std::min<i64>(nb, (i64)persistent_grid() * 2));
+    launch_pass<PASS_VERTEX>(g, s, bl, gb, st);
+    launch_pass<PASS_E2>(g, s, bl, gb, st);
+    launch_pass<PASS_F3>(g, s, bl, gb, st);
+    launch_pass<PASS_E4>(g, s, bl, gb, st);
+    launch_pass<PASS_F5>(g, s, bl, gb, st);
     k_export<<<grid_for(g.V), kBlock, 0, st>>>(g, s, PV, PE, PF, PT);
     return cudaGetLastError() == cudaSuccess ? DMTZ_OK : DMTZ_ERR_CUDA;
 }

@@ -327,8 +327,9 @@ __device__ __forceinline__ uint32_t crit_mask(const Grid &g, const FieldState &s
 namespace dmtz {
 
 // ---------------------------------------------------------------------------
-// Brick-driven sweeps.  Anchors are grouped in bricks of 8 x 4 x 4 (x fastest,
-// one 128-thread block per brick).  A sweep runs over an explicit list of
+// Brick-driven sweeps.  Anchors are grouped in bricks of 128 (x fastest, one
+// 128-thread block per brick; shape chosen by the autotuner, 8 x 4 x 4 by
+// default).  A sweep runs over an explicit list of
 // bricks (packed bx | by << 11 | bz << 22) or, with list == nullptr, over all
 // bricks of the grid.  Blocks stride over the list, so the grid size does not
 // depend on its length and the length can stay on the device.
@@ -342,7 +343,11 @@ struct BrickList {
     const uint32_t *list;           // packed brick coordinates, or nullptr for all bricks
     const unsigned long long *n;    // number of listed bricks (device), when list != nullptr
     int nbx, nby, nbz;              // bricks per axis
+    int shape;                      // brick shape index (DMTZ_SHAPES)
 };
+// brick shapes (anchors per brick along x, y, z); each is one 128-thread block
+#define DMTZ_NSHAPES 3
+static const int DMTZ_SHAPES[DMTZ_NSHAPES][3] = {{8, 4, 4}, {16, 4, 2}, {32, 2, 2}};
 
 __device__ __forceinline__ i64 brick_count(const BrickList &bl) {
     return bl.list ? (i64)*bl.n : (i64)bl.nbx * bl.nby * bl.nbz;

@@ -334,14 +334,15 @@ __device__ __forceinline__ void fast_crit(const Grid &g, const FieldState &s, i6
 // ---------------------------------------------------------------- brick sweep
 enum { PASS_VERTEX = 0, PASS_E2, PASS_F3, PASS_E4, PASS_F5, PASS_CRIT };
 
-template <int PASS>
+template <int PASS, int SX, int SY, int SZ>
 __global__ void __launch_bounds__(DMTZ_BRICK) k_sweep(Grid g, FieldState s, BrickList bl) {
+    static_assert(SX * SY * SZ == DMTZ_BRICK, "a brick is one block");
     const i64 nb = brick_count(bl);
-    const int lx = threadIdx.x % DMTZ_BX, ly = (threadIdx.x / DMTZ_BX) % DMTZ_BY, lz = threadIdx.x / (DMTZ_BX * DMTZ_BY);
+    const int lx = threadIdx.x % SX, ly = (threadIdx.x / SX) % SY, lz = threadIdx.x / (SX * SY);
     for (i64 b = blockIdx.x; b < nb; b += gridDim.x) {
         int bx, by, bz;
         brick_coords(bl, b, bx, by, bz);
-        const int x = bx * DMTZ_BX + lx, y = by * DMTZ_BY + ly, z = bz * DMTZ_BZ + lz;
+        const int x = bx * SX + lx, y = by * SY + ly, z = bz * SZ + lz;
         if (x >= g.W || y >= g.H || z >= g.D) continue;
         const i64 v = x + (i64)y * g.W + (i64)z * g.WH;
         const bool interior = x >= 1 && y >= 1 && z >= 1 && x <= g.W - 2 && y <= g.H - 2 && z <= g.D - 2;
@@ -372,4 +373,16 @@ __global__ void __launch_bounds__(DMTZ_BRICK) k_sweep(Grid g, FieldState s, Bric
     }
 }
 
+}  // namespace dmtz
+
+namespace dmtz {
+// launch one pass over a brick list with the list's brick shape
+template <int PASS>
+inline void launch_pass(const Grid &g, const FieldState &s, const BrickList &bl, unsigned grid, cudaStream_t st) {
+    switch (bl.shape) {
+    case 1: k_sweep<PASS, 16, 4, 2><<<grid, DMTZ_BRICK, 0, st>>>(g, s, bl); break;
+    case 2: k_sweep<PASS, 32, 2, 2><<<grid, DMTZ_BRICK, 0, st>>>(g, s, bl); break;
+    default: k_sweep<PASS, 8, 4, 4><<<grid, DMTZ_BRICK, 0, st>>>(g, s, bl); break;
+    }
+}
 }  // namespace dmtz

@@ -97,3 +97,27 @@ def make_case(kind: str, dims, seed: int, rel_eps: float, decomp: str = "uniform
     else:
         raise ValueError(decomp)
     return f, g
+
+
+def batch_workload(n: int = 64, seed: int = 2024, lo: int = 32, hi: int = 192):
+    """The uneven batch: n fields with dims drawn per axis from [lo, hi], even
+    index float32 / odd float64, Gaussian mixture or power-law alternately, and
+    eps per field from {1e-2, 1e-3, 1e-4} x range.  Returns a list of
+    (f, g, rel_eps) with f, g of the field's dtype, shape (D, H, W)."""
+    r = _rng(seed)
+    out = []
+    for i in range(n):
+        dims = tuple(int(x) for x in r.integers(lo, hi + 1, size=3))
+        rel = float(r.choice([1e-2, 1e-3, 1e-4]))
+        kind = "gauss" if i % 4 in (0, 1) else "powerlaw"
+        sub = int(r.integers(0, 2**31 - 1))
+        if kind == "gauss":
+            scale = float(np.mean(dims)) / 64.0
+            f = gaussian_mix(dims, sub, n_gauss=32, sigma=(2.0 * scale, 8.0 * scale))
+        else:
+            f = power_law(dims, sub)
+        eps = rel * value_range(f)
+        g = decompress_uniform(f, eps, sub) if kind == "gauss" else decompress_sz(f, eps, sub)
+        dt = np.float32 if i % 2 == 0 else np.float64
+        out.append((f.astype(dt), g.astype(dt), rel))
+    return out

@@ -143,6 +143,43 @@ dmtz_status dmtz_correct(dmtz_ctx *ctx, int W, int H, int D, const double *orig,
 dmtz_status dmtz_labels(dmtz_ctx *ctx, int W, int H, int D, const double *data, int on_device, int32_t *desc,
                         int32_t *asc);
 
+/* ---- batching and tuning (no counterpart in the reference, which corrects
+ * one field per process run) ---- */
+
+enum { DMTZ_F64 = 0, DMTZ_F32 = 1 };
+
+/* One field of a batch, in host memory.  orig/decp hold W*H*D values of
+ * `dtype`; float32 input is widened to float64 (exactly) and corrected in
+ * float64, as the reference would correct the widened file.  out receives
+ * the corrected field (W*H*D doubles). */
+typedef struct {
+    int W, H, D;
+    int dtype;
+    const void *orig;
+    const void *decp;
+    double *out;
+    double rel_eps;
+} dmtz_instance;
+
+/* Correct n fields of any sizes.  `workers` contexts (default 8), each with
+ * its own stream and buffers, take fields from a shared queue and run the
+ * correction (with opts->use_graph, as a device-driven graph); their kernels
+ * overlap on the GPU.  reports[i] / status[i] (optional) per field; returns
+ * the first failing status or DMTZ_OK. */
+dmtz_status dmtz_correct_batch(dmtz_ctx *ctx, int n, const dmtz_instance *inst, const dmtz_opts *opts,
+                               dmtz_report *reports, dmtz_status *status, int workers);
+
+/* Brick shape (0: 8x4x4, 1: 16x4x2, 2: 32x2x2 anchors) and blocks per SM of
+ * the gradient sweeps.  Results do not depend on them, only speed.
+ * dmtz_autotune times a full sweep of `decp` for every shape and 4, 8, 16, 32
+ * blocks per SM, keeps the fastest in the context and returns it in best[2]. */
+dmtz_status dmtz_set_tuning(dmtz_ctx *ctx, int shape, int blocks_per_sm);
+/* name of the context's device (for keying tuning caches) */
+dmtz_status dmtz_device_name(const dmtz_ctx *ctx, char *buf, int len);
+dmtz_status dmtz_get_tuning(const dmtz_ctx *ctx, int *shape, int *blocks_per_sm);
+dmtz_status dmtz_autotune(dmtz_ctx *ctx, int W, int H, int D, const double *orig, const double *decp, int on_device,
+                          int best[2], double *best_ms);
+
 /* Timing of the gradient sweep that every correction round runs (the five
  * pairing passes of main_3d.cu:6864-6874 plus the critical-cell comparison
  * of :6903-6909), `reps` times on the context's stream between CUDA events.

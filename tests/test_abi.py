@@ -51,3 +51,10 @@ def test_cli_builds_and_prints_usage():
     build.build()
     p = subprocess.run([build.EXE], capture_output=True, text=True)
     assert p.returncode == 2 and "usage" in p.stderr
+
+
+def test_autotune_size_class():
+    from dmtz_gb300 import autotune
+
+    assert autotune.size_class((256, 256, 256)) == "256x256x256"
+    assert autotune.size_class((200, 33, 2)) == "256x64x2"
