@@ -117,6 +117,16 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def bf16_peak():
+    """Dense bf16 tensor peak (burst, for a kernel timed alone), TFLOP/s."""
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as fh:
+            p = json.load(fh)
+        return float(p["bf16_tflops"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 1900.0, "fallback"
+
+
 def sweep_traffic():
     """DRAM bytes per gradient sweep from the committed ncu summary, if present."""
     try:
@@ -314,6 +324,102 @@ def run_batch(args):
     ctx.close()
 
 
+# tensor-core work of one forward pass per vertex, as executed: 3x3x3 taps,
+# channels 16->32->32->32->16 (the last layer's 16 outputs are the MMA width;
+# one is used)
+CNN_FLOP_PER_VOX = 2 * 27 * (16 * 32 + 32 * 32 + 32 * 32 + 32 * 16)
+
+
+def run_cnn(args):
+    """Throughput of the learned-proposal network kernels on a SIZE^3 grid of
+    the benchmark field's features: forward (inference), training step, and
+    the dominant 32->32 convolution launch against the bf16 tensor peak."""
+    import torch
+
+    import dmtz_gb300 as dm
+
+    size = args.cnn_size
+    f, g = workload(0, size)
+    dims = (size, size, size)
+    V = size ** 3
+    ctx = dm.Context(0)
+    net = dm.Network(0, seed=0)
+    fd, gd = torch.from_numpy(f).cuda(), torch.from_numpy(g).cuda()
+    feat = torch.empty((V, 16), dtype=torch.bfloat16, device="cuda")
+    active = torch.empty(V, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    ctx.features(fd.data_ptr(), gd.data_ptr(), dims, REL_EPS, feat.data_ptr(), active.data_ptr())
+    out = torch.empty(V, dtype=torch.float32, device="cuda")
+    target = torch.zeros(V, dtype=torch.float32, device="cuda")
+    ones = torch.ones(V, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    ms = net.profile(feat.data_ptr(), out.data_ptr(), target.data_ptr(), ones.data_ptr(), dims, reps=max(args.steps, 1))
+    pk, pk_src = bf16_peak()
+    conv_flop = 2 * 27 * 32 * 32 * V
+    tf_conv = conv_flop / (ms[2] * 1e-3) / 1e12
+    line = {"metric": "learned-proposal network, forward TFLOP/s (bf16 tensor cores)",
+            "value": CNN_FLOP_PER_VOX * V / (ms[0] * 1e-3) / 1e12, "unit": "TFLOP/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": 1, "ms_per_step": ms[0], "higher_is_better": True, "dtype": "bf16",
+            "data": "synthetic",
+            "config": {"workload": f"features of the powerlaw {size}^3 benchmark field", "voxels": V,
+                       "flop_per_voxel_forward": CNN_FLOP_PER_VOX, "train_step_ms": ms[1],
+                       "train_step_tflops": 3 * CNN_FLOP_PER_VOX * V / (ms[1] * 1e-3) / 1e12,
+                       "wgrad32_ms": ms[3], "wgrad32_tflops": conv_flop / (ms[3] * 1e-3) / 1e12},
+            "roofline": {"bound": "tensor", "kernel": "k_conv<32,32> (one 32->32 layer)", "achieved": tf_conv,
+                         "peak": pk, "unit": "TFLOP/s", "frac": tf_conv / pk, "peak_source": pk_src,
+                         "traffic": None}}
+    print(json.dumps(line), flush=True)
+    net.close()
+    ctx.close()
+
+
+def run_learned(args):
+    """Plain vs learned warm start: train the network on traces of 128^3
+    power-law fields (seeds 1000.., eps=1e-4 x range, full-MSC flags), then
+    correct held-out fields both ways and compare device time and rounds."""
+    import dmtz_gb300 as dm
+    from dmtz_gb300 import learned
+
+    ctx = dm.Context(0)
+    t0 = time.perf_counter()
+    traces, skipped = learned.make_traces(ctx, args.traces, (128, 128, 128), 1000, REL_EPS)
+    gen_s = time.perf_counter() - t0
+    net = dm.Network(0, seed=0)
+    t1 = time.perf_counter()
+    hist = learned.train(net, traces, epochs=args.epochs, lr=args.lr)
+    train_s = time.perf_counter() - t1
+    if args.save_params:
+        net.save(args.save_params)
+    n_used = len(traces)
+    del traces
+    evals = []
+    for size, seed in ((256, 0), (args.eval_size, 7)):
+        from dmtz_gb300 import synth
+
+        f, g = synth.make_case("powerlaw", (size,) * 3, seed, REL_EPS, "sz")
+        learned.evaluate(ctx, net, f[:64, :64, :64], g[:64, :64, :64], REL_EPS, max_rounds=50)  # warm-up
+        r = learned.evaluate(ctx, net, f, g, REL_EPS, max_rounds=args.max_rounds)
+        keep = ("seconds", "wall_s", "cp_rounds", "path_rounds", "outer_iterations", "converged", "edited_vertices",
+                "max_err_over_bound", "initial_mismatch")
+        evals.append({"field": f"powerlaw {size}^3 seed {seed}",
+                      **{k: {x: r[k][x] for x in keep} for k in ("plain", "learned")},
+                      "speedup": r["plain"]["seconds"] / r["learned"]["seconds"]})
+    line = {"metric": "time to full MSC match: plain loop vs learned warm start", "value": evals[-1]["speedup"],
+            "unit": "x (plain s / learned s)", "n_gpus": 1, "steps": 1, "warmup": 1,
+            "ms_per_step": evals[-1]["learned"]["seconds"] * 1e3, "higher_is_better": True, "dtype": "bf16+f64",
+            "data": "synthetic",
+            "config": {"workload": f"train {args.traces} x 128^3 traces, {args.epochs} epochs, lr {args.lr}; "
+                                   f"evaluate 256^3 and {args.eval_size}^3", "trace_generation_s": gen_s,
+                       "traces_used": n_used, "skipped_nonconverged_seeds": skipped,
+                       "train_s": train_s, "train_steps": len(hist),
+                       "loss_first_epoch": float(np.mean(hist[:max(1, len(hist) // max(args.epochs, 1))])),
+                       "loss_last_epoch": float(np.mean(hist[-max(1, len(hist) // max(args.epochs, 1)):]))},
+            "evaluations": evals}
+    print(json.dumps(line), flush=True)
+    net.close()
+    ctx.close()
+
+
 def sweep_only(size: int):
     """Gradient sweep kernels alone (for kernel profilers): 3 timed sweeps."""
     import torch
@@ -338,11 +444,23 @@ def main():
     ap.add_argument("--graph", type=int, default=1, help="1: loop as a CUDA graph with a device-side flag")
     ap.add_argument("--sweep-only", type=int, default=0, metavar="SIZE",
                     help="profiling aid: only time the gradient sweep on a SIZE^3 field of the same kind")
-    ap.add_argument("--workload", choices=["field256", "batch"], default="field256")
+    ap.add_argument("--workload", choices=["field256", "batch", "cnn", "learned"], default="field256")
     ap.add_argument("--max-rounds", type=int, default=2000)
+    ap.add_argument("--cnn-size", type=int, default=256, help="cnn workload: grid size")
+    ap.add_argument("--traces", type=int, default=64, help="learned workload: training traces")
+    ap.add_argument("--epochs", type=int, default=10, help="learned workload: epochs")
+    ap.add_argument("--lr", type=float, default=1e-3, help="learned workload: Adam learning rate")
+    ap.add_argument("--eval-size", type=int, default=512, help="learned workload: held-out field size")
+    ap.add_argument("--save-params", default="", help="learned workload: write the trained parameters (.npy)")
     args = ap.parse_args()
     if args.workload == "batch":
         run_batch(args)
+        return
+    if args.workload == "cnn":
+        run_cnn(args)
+        return
+    if args.workload == "learned":
+        run_learned(args)
         return
     if args.sweep_only:
         sweep_only(args.sweep_only)

@@ -20,7 +20,7 @@ import numpy as np
 
 from . import build as _build
 
-__all__ = ["Context", "DmtzError", "Opts", "Report", "cell_counts", "load_library"]
+__all__ = ["Context", "DmtzError", "Network", "Opts", "Report", "cell_counts", "load_library"]
 
 _lib = None
 
@@ -52,7 +52,8 @@ class Report(ctypes.Structure):
     def as_dict(self):
         return dict(outer_iterations=self.outer_iterations, cp_rounds=self.cp_rounds, path_rounds=self.path_rounds,
                     initial_mismatch=list(self.initial_mismatch), final_mismatch=list(self.final_mismatch),
-                    final_paths=list(self.final_paths), converged=bool(self.converged),
+                    final_paths=list(self.final_paths), edited_vertices=self.edited_vertices,
+                    converged=bool(self.converged),
                     error_flags=self.error_flags, seconds=self.seconds, kernel_launches=self.kernel_launches,
                     phase_ms=dict(zip(self.PHASES, [round(x, 4) for x in self.phase_ms])))
 
@@ -94,6 +95,29 @@ def load_library(build_if_missing: bool = True):
     L.dmtz_get_tuning.argtypes = [_vp, ctypes.POINTER(_int), ctypes.POINTER(_int)]
     L.dmtz_autotune.argtypes = [_vp, _int, _int, _int, _vp, _vp, _int, ctypes.POINTER(_int), ctypes.POINTER(ctypes.c_double)]
     L.dmtz_device_name.argtypes = [_vp, ctypes.c_char_p, _int]
+    # learned proposal
+    L.dmtz_cnn_num_params.argtypes = []
+    L.dmtz_cnn_num_params.restype = ctypes.c_int64
+    L.dmtz_cnn_create.argtypes = [ctypes.POINTER(_vp), _int, ctypes.c_uint64]
+    L.dmtz_cnn_destroy.argtypes = [_vp]
+    L.dmtz_cnn_destroy.restype = None
+    L.dmtz_cnn_last_error.argtypes = [_vp]
+    L.dmtz_cnn_last_error.restype = ctypes.c_char_p
+    _f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+    L.dmtz_cnn_set_params.argtypes = [_vp, _f32p]
+    L.dmtz_cnn_get_params.argtypes = [_vp, _f32p]
+    L.dmtz_cnn_get_grads.argtypes = [_vp, _f32p]
+    L.dmtz_cnn_forward.argtypes = [_vp, _int, _int, _int, _vp, _vp, _int]
+    L.dmtz_cnn_backward.argtypes = [_vp, _int, _int, _int, _vp, _vp, ctypes.POINTER(ctypes.c_double)]
+    L.dmtz_cnn_step.argtypes = [_vp, ctypes.c_float]
+    L.dmtz_cnn_profile.argtypes = [_vp, _int, _int, _int, _vp, _vp, _vp, _vp, _int, _f64p]
+    L.dmtz_cnn_profile.restype = _int
+    L.dmtz_features.argtypes = [_vp, _int, _int, _int, _vp, _vp, _int, ctypes.c_double, _vp, _vp]
+    L.dmtz_correct_learned.argtypes = [_vp, _vp, _int, _int, _int, _vp, _vp, _int, ctypes.c_double,
+                                       ctypes.POINTER(Opts), ctypes.POINTER(Report), _vp]
+    for fn in ("dmtz_cnn_create", "dmtz_cnn_set_params", "dmtz_cnn_get_params", "dmtz_cnn_get_grads",
+               "dmtz_cnn_forward", "dmtz_cnn_backward", "dmtz_cnn_step", "dmtz_features", "dmtz_correct_learned"):
+        getattr(L, fn).restype = _int
     for fn in ("dmtz_correct_batch", "dmtz_set_tuning", "dmtz_get_tuning", "dmtz_autotune", "dmtz_device_name"):
         getattr(L, fn).restype = _int
     for fn in ("dmtz_ctx_create", "dmtz_cell_counts", "dmtz_extract", "dmtz_mismatch", "dmtz_fix_round",
@@ -154,8 +178,8 @@ class Context:
         except Exception:
             pass
 
-    def _check(self, rc):
-        if rc:
+    def _check(self, rc, allow=()):
+        if rc and rc not in allow:
             raise DmtzError(rc, self._L.dmtz_last_error(self._h).decode())
 
     # ------------------------------------------------------------------ stages
@@ -275,13 +299,16 @@ class Context:
         return best[0], best[1], ms.value
 
     def correct_ptr(self, f_ptr: int, g_ptr: int, dims, rel_eps, flags=(1, 1, 1, 0, 0, 0, 0), on_device=True,
-                    max_rounds=0, use_graph=0):
+                    max_rounds=0, use_graph=0, allow_nonconverged=False):
         """Correction on raw float64 buffers (device pointers when on_device, else host
-        pointers, e.g. pinned memory); g is edited in place."""
+        pointers, e.g. pinned memory); g is edited in place.  With
+        allow_nonconverged, hitting max_rounds returns the report (converged
+        False) instead of raising."""
         o = Opts(*[int(x) for x in flags], int(max_rounds), int(use_graph))
         r = Report()
         self._check(self._L.dmtz_correct(self._h, *dims, _vp(f_ptr), _vp(g_ptr), int(bool(on_device)),
-                                         float(rel_eps), ctypes.byref(o), ctypes.byref(r), None))
+                                         float(rel_eps), ctypes.byref(o), ctypes.byref(r), None),
+                    allow=(4,) if allow_nonconverged else ())
         return r.as_dict()
 
     def profile_sweep(self, f_ptr: int, g_ptr: int, dims, reps=10, on_device=True):
@@ -290,3 +317,104 @@ class Context:
         self._check(self._L.dmtz_profile_sweep(self._h, *dims, _vp(f_ptr), _vp(g_ptr), int(bool(on_device)),
                                                int(reps), ms))
         return ms
+
+    # --------------------------------------------------------- learned proposal
+    def features(self, f_ptr: int, g_ptr: int, dims, rel_eps, feat_ptr: int, active_ptr: int, on_device=True):
+        """Network input (V x 16 bf16) and active mask (V bytes) of (f, g) into
+        device buffers feat_ptr / active_ptr."""
+        self._check(self._L.dmtz_features(self._h, *dims, _vp(f_ptr), _vp(g_ptr), int(bool(on_device)),
+                                          float(rel_eps), _vp(feat_ptr), _vp(active_ptr)))
+
+    def correct_learned(self, net, f, g, rel_eps, flags=(1, 1, 1, 0, 0, 0, 0), dims=None, max_rounds=0,
+                        use_graph=0):
+        """Correction started from the network's proposal (host arrays).
+        Returns (corrected g, report dict)."""
+        dims = _dims_of(np.asarray(f), dims)
+        ff = _flat(f)
+        gg = np.array(_flat(g), copy=True)
+        o = Opts(*[int(x) for x in flags], int(max_rounds), int(use_graph))
+        r = Report()
+        self._check(self._L.dmtz_correct_learned(self._h, net._h, *dims, ff.ctypes.data, gg.ctypes.data, 0,
+                                                 float(rel_eps), ctypes.byref(o), ctypes.byref(r), None))
+        return gg, r.as_dict()
+
+    def correct_learned_ptr(self, net, f_ptr: int, g_ptr: int, dims, rel_eps, flags=(1, 1, 1, 0, 0, 0, 0),
+                            on_device=True, max_rounds=0, use_graph=0, allow_nonconverged=False):
+        """correct_learned on raw float64 buffers (g edited in place)."""
+        o = Opts(*[int(x) for x in flags], int(max_rounds), int(use_graph))
+        r = Report()
+        self._check(self._L.dmtz_correct_learned(self._h, net._h, *dims, _vp(f_ptr), _vp(g_ptr),
+                                                 int(bool(on_device)), float(rel_eps), ctypes.byref(o),
+                                                 ctypes.byref(r), None),
+                    allow=(4,) if allow_nonconverged else ())
+        return r.as_dict()
+
+
+class Network:
+    """The learned-proposal network (dmtz_cnn): 3x3x3 convolutions 16 -> 32 ->
+    32 -> 32 -> 1 with bf16 tensor-core kernels.  Buffers passed by pointer are
+    device buffers (e.g. torch tensors' data_ptr())."""
+
+    def __init__(self, device: int = 0, seed: int = 0):
+        self._L = load_library()
+        h = _vp()
+        rc = self._L.dmtz_cnn_create(ctypes.byref(h), int(device), ctypes.c_uint64(int(seed) & (2**64 - 1)))
+        if rc:
+            raise DmtzError(rc, "cannot create the network (no CUDA device?)")
+        self._h = h
+        self.n_params = int(self._L.dmtz_cnn_num_params())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.dmtz_cnn_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc:
+            raise DmtzError(rc, self._L.dmtz_cnn_last_error(self._h).decode())
+
+    def get_params(self):
+        out = np.empty(self.n_params, np.float32)
+        self._check(self._L.dmtz_cnn_get_params(self._h, out))
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        if p.size != self.n_params:
+            raise ValueError(f"expected {self.n_params} parameters")
+        self._check(self._L.dmtz_cnn_set_params(self._h, p))
+
+    def get_grads(self):
+        out = np.empty(self.n_params, np.float32)
+        self._check(self._L.dmtz_cnn_get_grads(self._h, out))
+        return out
+
+    def forward(self, feat_ptr: int, out_ptr: int, dims, train=False):
+        self._check(self._L.dmtz_cnn_forward(self._h, *dims, _vp(feat_ptr), _vp(out_ptr), int(bool(train))))
+
+    def backward(self, target_ptr: int, active_ptr: int, dims) -> float:
+        loss = ctypes.c_double()
+        self._check(self._L.dmtz_cnn_backward(self._h, *dims, _vp(target_ptr), _vp(active_ptr), ctypes.byref(loss)))
+        return loss.value
+
+    def step(self, lr: float):
+        self._check(self._L.dmtz_cnn_step(self._h, ctypes.c_float(lr)))
+
+    def profile(self, feat_ptr: int, out_ptr: int, target_ptr: int, active_ptr: int, dims, reps=5):
+        """ms of: forward, training step, one 32->32 conv launch, one 32x32 weight-gradient launch."""
+        ms = np.zeros(4, np.float64)
+        self._check(self._L.dmtz_cnn_profile(self._h, *dims, _vp(feat_ptr), _vp(out_ptr), _vp(target_ptr),
+                                             _vp(active_ptr), int(reps), ms))
+        return ms
+
+    def save(self, path):
+        np.save(path, self.get_params())
+
+    def load(self, path):
+        self.set_params(np.load(path))

@@ -1,8 +1,10 @@
 """Build recipe for libdmtz (sm_103a) and the drop-in `dmtz` executable.
 
-nvcc is called directly (no cmake, no torch extension machinery): one
-translation unit for the library and one small host file for the executable,
-linked against it.  Outputs go to dmtz_gb300/_lib/ (git-ignored).
+nvcc is called directly (no cmake, no torch extension machinery): two
+translation units for the library (the correction path, dmtz.cu, and the
+learned-proposal network, cnn.cu), compiled in parallel and linked into one
+shared object, and one small host file for the executable, linked against it.
+Outputs go to dmtz_gb300/_lib/ (git-ignored).
 """
 from __future__ import annotations
 
@@ -46,9 +48,22 @@ def build(force: bool = False, verbose: bool = False) -> str:
     deps = _sources()
     jobs = []
     if force or _stale(LIB, deps):
-        jobs.append([NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
-                     *(["-Xptxas", "-v"] if verbose else []),
-                     "-o", LIB, os.path.join(CSRC, "dmtz.cu")])
+        objs = []
+        procs = []
+        for tu in ("dmtz.cu", "cnn.cu"):
+            obj = os.path.join(LIBDIR, tu.replace(".cu", ".o"))
+            objs.append(obj)
+            cmd = [NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-c",
+                   *(["-Xptxas", "-v"] if verbose else []), "-o", obj, os.path.join(CSRC, tu)]
+            procs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)))
+        for cmd, p in procs:
+            out, err = p.communicate()
+            if p.returncode != 0:
+                sys.stderr.write(out + err)
+                raise RuntimeError("build failed: " + " ".join(cmd))
+            if verbose:
+                sys.stdout.write(out + err)
+        jobs.append([NVCC, *ARCH, "-shared", "-o", LIB, *objs])
     for job in jobs:
         r = _run(job)
         if verbose:

@@ -1,0 +1,871 @@
+// cnn.cu — the learned proposal: a 4-layer 3x3x3 convolutional network with
+// BF16 weights/activations and FP32 accumulation on the tensor cores, its
+// backward pass, and the loss / optimiser kernels.  No counterpart in the
+// reference; it only produces a starting point for the exact correction loop.
+//
+// Layout: activations channels-last bf16, [vertex][channel], vertex =
+// x + W*(y + H*z).  Layers (in -> out channels): 16 -> 32 -> 32 -> 32 -> 16,
+// ReLU after the first three; only output channel 0 is used (the other 15
+// have zero weights and zero gradients, so they stay zero).  Parameters (f32
+// master copy), per layer: weights [27 taps][out][in], then bias [out];
+// tap = (dz+1)*9 + (dy+1)*3 + (dx+1).
+//
+// Kernels (all persistent: one or two blocks per SM loop over tiles):
+//   k_conv   implicit-GEMM convolution on mma.sync.m16n8k16 (bf16 in, f32
+//            accumulate).  A block keeps all 27 x out x in weights in shared
+//            memory and streams 8x8x4-vertex tiles (+1 halo) through a
+//            cp.async double buffer; operands reach registers by ldmatrix.
+//            The data gradient is the same kernel with transposed weights,
+//            mirrored taps and a ReLU-derivative epilogue.
+//   k_wgrad  weight + bias gradient: per tile, all 27 taps x out x in
+//            products reduced over the tile's 256 vertices on the same MMA
+//            (operands by ldmatrix.trans from the channels-last tiles);
+//            per-block partial sums, then a fixed-order reduction
+//            (deterministic).
+//   k_loss, k_loss_final, k_reduce, k_adam, k_pack: loss, gradient scaling,
+//            Adam, bf16 weight refresh.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "cnn.cuh"
+
+typedef __nv_bfloat16 bf16;
+typedef long long i64;
+
+namespace {
+
+constexpr int TX = 8, TY = 8, TZ = 4, TV = TX * TY * TZ;  // output tile (256 vertices)
+constexpr int HX = TX + 2, HY = TY + 2, HZ = TZ + 2, HALO = HX * HY * HZ;
+constexpr int NLAYER = 4;
+constexpr int LCIN[NLAYER] = {16, 32, 32, 32};
+constexpr int LCOUT[NLAYER] = {32, 32, 32, 16};
+
+constexpr i64 layer_params(int l) { return 27LL * LCOUT[l] * LCIN[l] + LCOUT[l]; }
+constexpr i64 layer_offset(int l) { return l == 0 ? 0 : layer_offset(l - 1) + layer_params(l - 1); }
+constexpr i64 kParams = layer_offset(NLAYER);
+
+// ------------------------------------------------------------------ PTX helpers
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+// 16-byte async copy global -> shared; src_bytes = 0 writes zeros (the source
+// address is not read then, but is kept valid anyway)
+__device__ __forceinline__ void cp16(void *dst, const void *src, int src_bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(smem_addr(dst)), "l"(src), "r"(src_bytes));
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
+}
+__device__ __forceinline__ void ldm4(uint32_t r[4], const void *p) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(smem_addr(p)));
+}
+__device__ __forceinline__ void ldm4t(uint32_t r[4], const void *p) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(smem_addr(p)));
+}
+__device__ __forceinline__ void mma16816(float c[4], const uint32_t a[4], uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+struct Dims {
+    int W, H, D, ntx, nty, ntz;
+    i64 ntiles;
+};
+inline Dims make_dims(int W, int H, int D) {
+    Dims d{W, H, D, (W + TX - 1) / TX, (H + TY - 1) / TY, (D + TZ - 1) / TZ, 0};
+    d.ntiles = (i64)d.ntx * d.nty * d.ntz;
+    return d;
+}
+
+// Box of EX x EY x EZ vertices starting at (x0, y0, z0) (may stick out of the
+// grid: zeros there) of a channels-last tensor with C channels, into shared
+// rows of CP = C + 8 bf16 (the 16-byte pad makes ldmatrix conflict-free).
+template <int C, int EX, int EY, int EZ>
+__device__ __forceinline__ void load_box(bf16 *dst, const bf16 *__restrict__ src, const Dims &d, int x0, int y0,
+                                         int z0) {
+    constexpr int CP = C + 8, PIECES = C / 8;
+    for (int i = threadIdx.x; i < EX * EY * EZ * PIECES; i += blockDim.x) {
+        const int row = i / PIECES, piece = i - row * PIECES;
+        const int hx = row % EX, hy = (row / EX) % EY, hz = row / (EX * EY);
+        const int gx = x0 + hx, gy = y0 + hy, gz = z0 + hz;
+        const bool in = gx >= 0 && gx < d.W && gy >= 0 && gy < d.H && gz >= 0 && gz < d.D;
+        const bf16 *s = in ? src + ((i64)gx + (i64)gy * d.W + (i64)gz * d.W * d.H) * C + piece * 8 : src;
+        cp16(dst + row * CP + piece * 8, s, in ? 16 : 0);
+    }
+}
+
+__device__ __forceinline__ void tile_origin(const Dims &d, i64 tile, int &x0, int &y0, int &z0) {
+    x0 = (int)(tile % d.ntx) * TX;
+    y0 = (int)((tile / d.ntx) % d.nty) * TY;
+    z0 = (int)(tile / ((i64)d.ntx * d.nty)) * TZ;
+}
+
+}  // namespace
+
+namespace {
+
+// ---------------------------------------------------------------- convolution
+// out[v][n] = sum_tap sum_c W[tap][n][c] * in[v + off(tap)][c]   (FLIP: v - off)
+// MODE 0: + bias, ReLU, bf16 out.  MODE 1: + bias, channel 0 as f32 (the
+// proposal).  MODE 2 (data gradient): no bias; zero where aux, the stored
+// activation that fed the layer, is not positive (ReLU derivative).
+// 8 warps; warp w owns tile vertices 32w..32w+31 (two m16 tiles), all COUT.
+template <int CIN, int COUT, int MODE, bool FLIP>
+__global__ void __launch_bounds__(256, 1) k_conv(Dims d, const bf16 *__restrict__ in, const bf16 *__restrict__ wt,
+                                              const float *__restrict__ bias, void *out,
+                                              const bf16 *__restrict__ aux) {
+    constexpr int CP = CIN + 8, NT = COUT / 8, KC = CIN / 16;
+    static_assert(NT % 2 == 0 && CIN % 16 == 0, "tile shapes");
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    bf16 *ws = reinterpret_cast<bf16 *>(smem_raw);  // [27*COUT][CP]
+    bf16 *xs0 = ws + 27 * COUT * CP;                 // 2 x [HALO][CP]
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
+    for (int i = tid; i < 27 * COUT * (CIN / 8); i += blockDim.x) {
+        const int row = i / (CIN / 8), piece = i - row * (CIN / 8);
+        cp16(ws + row * CP + piece * 8, wt + (i64)row * CIN + piece * 8, 16);
+    }
+    // ldmatrix roles.  A (vertices x channels): lane supplies row
+    // (lane&7) + 8*((lane>>3)&1) of the m-tile, channel half 8*(lane>>4).
+    // B (weights, rows = output channel): n = 8*(lane>>4) + (lane&7) within a
+    // pair of n-tiles, channel half 8*((lane>>3)&1).
+    int hbase[2];
+#pragma unroll
+    for (int m = 0; m < 2; m++) {
+        const int li = warp * 32 + m * 16 + (lane & 7) + 8 * ((lane >> 3) & 1);
+        hbase[m] = (((li >> 6) + 1) * HY + ((li >> 3) & 7) + 1) * HX + (li & 7) + 1;
+    }
+    const int akofs = 8 * (lane >> 4);
+    const int bn = 8 * (lane >> 4) + (lane & 7), bkofs = 8 * ((lane >> 3) & 1);
+
+    i64 tile = blockIdx.x;
+    int buf = 0;
+    if (tile < d.ntiles) {
+        int x0, y0, z0;
+        tile_origin(d, tile, x0, y0, z0);
+        load_box<CIN, HX, HY, HZ>(xs0, in, d, x0 - 1, y0 - 1, z0 - 1);
+    }
+    cp_commit();
+    for (; tile < d.ntiles; tile += gridDim.x, buf ^= 1) {
+        const i64 next = tile + gridDim.x;
+        if (next < d.ntiles) {
+            int x0, y0, z0;
+            tile_origin(d, next, x0, y0, z0);
+            load_box<CIN, HX, HY, HZ>(xs0 + (buf ^ 1) * HALO * CP, in, d, x0 - 1, y0 - 1, z0 - 1);
+        }
+        cp_commit();
+        cp_wait<1>();
+        __syncthreads();
+        const bf16 *xs = xs0 + buf * HALO * CP;
+        float acc[2][NT][4];
+#pragma unroll
+        for (int m = 0; m < 2; m++)
+#pragma unroll
+            for (int n = 0; n < NT; n++)
+#pragma unroll
+                for (int k = 0; k < 4; k++) acc[m][n][k] = 0.f;
+#pragma unroll 1
+        for (int tap = 0; tap < 27; tap++) {
+            const int dx = tap % 3 - 1, dy = (tap / 3) % 3 - 1, dzz = tap / 9 - 1;
+            const int toff = FLIP ? -((dzz * HY + dy) * HX + dx) : (dzz * HY + dy) * HX + dx;
+            const bf16 *wtap = ws + tap * COUT * CP;
+#pragma unroll
+            for (int kc = 0; kc < KC; kc++) {
+                uint32_t a0[4], a1[4];
+                ldm4(a0, xs + (hbase[0] + toff) * CP + kc * 16 + akofs);
+                ldm4(a1, xs + (hbase[1] + toff) * CP + kc * 16 + akofs);
+#pragma unroll
+                for (int j = 0; j < NT; j += 2) {
+                    uint32_t b[4];
+                    ldm4(b, wtap + (j * 8 + bn) * CP + kc * 16 + bkofs);
+                    mma16816(acc[0][j], a0, b[0], b[1]);
+                    mma16816(acc[1][j], a1, b[0], b[1]);
+                    mma16816(acc[0][j + 1], a0, b[2], b[3]);
+                    mma16816(acc[1][j + 1], a1, b[2], b[3]);
+                }
+            }
+        }
+        // accumulator (m, n, k): vertex row g + 8*(k>>1), channel n*8 + 2t + (k&1)
+        int x0, y0, z0;
+        tile_origin(d, tile, x0, y0, z0);
+#pragma unroll
+        for (int m = 0; m < 2; m++)
+#pragma unroll
+            for (int r = 0; r < 2; r++) {
+                const int li = warp * 32 + m * 16 + g + 8 * r;
+                const int gx = x0 + (li & 7), gy = y0 + ((li >> 3) & 7), gz = z0 + (li >> 6);
+                if (gx >= d.W || gy >= d.H || gz >= d.D) continue;
+                const i64 v = gx + (i64)gy * d.W + (i64)gz * d.W * d.H;
+                if constexpr (MODE == 1) {
+                    if (t == 0) reinterpret_cast<float *>(out)[v] = acc[m][0][2 * r] + bias[0];
+                } else {
+#pragma unroll
+                for (int n = 0; n < NT; n++) {
+                    const int ch = n * 8 + 2 * t;
+                    float v0 = acc[m][n][2 * r], v1 = acc[m][n][2 * r + 1];
+                    if constexpr (MODE == 0) {
+                        v0 = fmaxf(v0 + bias[ch], 0.f);
+                        v1 = fmaxf(v1 + bias[ch + 1], 0.f);
+                    } else {
+                        const __nv_bfloat162 a2 = *reinterpret_cast<const __nv_bfloat162 *>(aux + v * COUT + ch);
+                        if (!(__bfloat162float(a2.x) > 0.f)) v0 = 0.f;
+                        if (!(__bfloat162float(a2.y) > 0.f)) v1 = 0.f;
+                    }
+                    *reinterpret_cast<__nv_bfloat162 *>(reinterpret_cast<bf16 *>(out) + v * COUT + ch) =
+                        __floats2bfloat162_rn(v0, v1);
+                }
+                }
+            }
+        __syncthreads();  // buffer `buf` is refilled two iterations on
+    }
+    cp_wait<0>();
+}
+
+// ------------------------------------------------------------ weight gradient
+// dW[tap][n][c] = sum_v dz[v][n] * act[v + off(tap)][c]; db[n] = sum_v dz[v][n].
+// GEMM per tap with M = n, N = c, K = vertices of the tile.  Both operands are
+// read transposed from the channels-last tiles by ldmatrix.trans.  16 warps
+// share the 27 x (COUT/16) (tap, m-tile) units; each keeps its units'
+// accumulators in registers across all tiles of the block, and the block
+// writes one partial sum of every parameter of the layer to part[blockIdx.x].
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(512, 1) k_wgrad(Dims d, const bf16 *__restrict__ act, const bf16 *__restrict__ dz,
+                                                  float *__restrict__ part) {
+    constexpr int AP = CIN + 8, DP = COUT + 8, NT = CIN / 8, MT = COUT / 16, UNITS = 27 * MT, NW = 16;
+    constexpr int UPW = (UNITS + NW - 1) / NW;
+    constexpr i64 NPAR = 27LL * COUT * CIN + COUT;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    bf16 *as0 = reinterpret_cast<bf16 *>(smem_raw);  // 2 x [HALO][AP]
+    bf16 *ds0 = as0 + 2 * HALO * AP;                  // 2 x [TV][DP]
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
+    float acc[UPW][NT][4];
+#pragma unroll
+    for (int u = 0; u < UPW; u++)
+#pragma unroll
+        for (int n = 0; n < NT; n++)
+#pragma unroll
+            for (int k = 0; k < 4; k++) acc[u][n][k] = 0.f;
+    float bacc = 0.f;
+    // ldmatrix.trans roles.  A (dz^T: rows = out channel, k = vertex): lane
+    // gives vertex (lane&7) + 8*(lane>>4), channel block 8*((lane>>3)&1).
+    // B (act: k = vertex, n = in channel): vertex (lane&7) + 8*((lane>>3)&1),
+    // channel block 8*(lane>>4) within a pair of n-tiles.
+    const int va = (lane & 7) + 8 * (lane >> 4), ca = 8 * ((lane >> 3) & 1);
+    const int vb = (lane & 7) + 8 * ((lane >> 3) & 1), cb = 8 * (lane >> 4);
+
+    i64 tile = blockIdx.x;
+    int buf = 0;
+    if (tile < d.ntiles) {
+        int x0, y0, z0;
+        tile_origin(d, tile, x0, y0, z0);
+        load_box<CIN, HX, HY, HZ>(as0, act, d, x0 - 1, y0 - 1, z0 - 1);
+        load_box<COUT, TX, TY, TZ>(ds0, dz, d, x0, y0, z0);
+    }
+    cp_commit();
+    for (; tile < d.ntiles; tile += gridDim.x, buf ^= 1) {
+        const i64 next = tile + gridDim.x;
+        if (next < d.ntiles) {
+            int x0, y0, z0;
+            tile_origin(d, next, x0, y0, z0);
+            load_box<CIN, HX, HY, HZ>(as0 + (buf ^ 1) * HALO * AP, act, d, x0 - 1, y0 - 1, z0 - 1);
+            load_box<COUT, TX, TY, TZ>(ds0 + (buf ^ 1) * TV * DP, dz, d, x0, y0, z0);
+        }
+        cp_commit();
+        cp_wait<1>();
+        __syncthreads();
+        const bf16 *as = as0 + buf * HALO * AP, *ds = ds0 + buf * TV * DP;
+        if (lane < COUT)
+            for (int v = warp * (TV / NW); v < (warp + 1) * (TV / NW); v++) bacc += __bfloat162float(ds[v * DP + lane]);
+#pragma unroll
+        for (int u = 0; u < UPW; u++) {
+            const int unit = warp + u * NW;
+            if (unit >= UNITS) continue;
+            const int tap = unit / MT, mt = unit - tap * MT;
+            const int dx = tap % 3 - 1, dy = (tap / 3) % 3 - 1, dzz = tap / 9 - 1;
+            const int toff = (dzz * HY + dy) * HX + dx;
+#pragma unroll 4
+            for (int ks = 0; ks < TV / 16; ks++) {
+                uint32_t a[4];
+                ldm4t(a, ds + (ks * 16 + va) * DP + mt * 16 + ca);
+                const int lb = ks * 16 + vb;
+                const int hb = (((lb >> 6) + 1) * HY + ((lb >> 3) & 7) + 1) * HX + (lb & 7) + 1 + toff;
+#pragma unroll
+                for (int nt = 0; nt < NT; nt += 2) {
+                    uint32_t b[4];
+                    ldm4t(b, as + hb * AP + nt * 8 + cb);
+                    mma16816(acc[u][nt], a, b[0], b[1]);
+                    mma16816(acc[u][nt + 1], a, b[2], b[3]);
+                }
+            }
+        }
+        __syncthreads();
+    }
+    cp_wait<0>();
+    float *p = part + (i64)blockIdx.x * NPAR;
+#pragma unroll
+    for (int u = 0; u < UPW; u++) {
+        const int unit = warp + u * NW;
+        if (unit >= UNITS) continue;
+        const int tap = unit / MT, mt = unit - tap * MT;
+#pragma unroll
+        for (int nt = 0; nt < NT; nt++) {
+            const int n0 = mt * 16 + g, c0 = nt * 8 + 2 * t;
+            float *q = p + ((i64)tap * COUT + n0) * CIN + c0;
+            q[0] = acc[u][nt][0];
+            q[1] = acc[u][nt][1];
+            q[8 * CIN] = acc[u][nt][2];
+            q[8 * CIN + 1] = acc[u][nt][3];
+        }
+    }
+    // bias: fixed-order sum of the 16 warps' partials
+    __syncthreads();
+    float *red = reinterpret_cast<float *>(smem_raw);
+    if (lane < COUT) red[warp * COUT + lane] = bacc;
+    __syncthreads();
+    if (tid < COUT) {
+        float s = 0.f;
+        for (int w = 0; w < NW; w++) s += red[w * COUT + tid];
+        p[27LL * COUT * CIN + tid] = s;
+    }
+}
+
+// grad[i] = scale * sum over blocks (in block order) of part[b][i]
+__global__ void k_reduce(const float *__restrict__ part, int nblk, i64 n, const float *__restrict__ scale,
+                         float *__restrict__ grad) {
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+        float s = 0.f;
+        for (int b = 0; b < nblk; b++) s += part[(i64)b * n + i];
+        grad[i] = s * *scale;
+    }
+}
+
+// ------------------------------------------------------------------- the loss
+// Over active vertices: L = mean (tanh(o) - target)^2.  Writes dL/do without
+// the 1/count factor (applied by k_reduce) into channel 0 of dz (16 channels,
+// the others 0), and per-block (sum, count) partials.
+constexpr int kLossBlocks = 1024;
+__global__ void k_loss(i64 V, const float *__restrict__ o, const float *__restrict__ target,
+                       const uint8_t *__restrict__ active, bf16 *__restrict__ dz, double *__restrict__ part) {
+    double ls = 0.0, cnt = 0.0;
+    for (i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (i64)gridDim.x * blockDim.x) {
+        float gval = 0.f;
+        if (active[v]) {
+            const float y = tanhf(o[v]);
+            const float e = y - target[v];
+            ls += (double)e * e;
+            cnt += 1.0;
+            gval = 2.f * e * (1.f - y * y);
+        }
+        const __nv_bfloat162 lo = __floats2bfloat162_rn(gval, 0.f);
+        uint4 first = make_uint4(*reinterpret_cast<const uint32_t *>(&lo), 0u, 0u, 0u);
+        reinterpret_cast<uint4 *>(dz + v * 16)[0] = first;
+        reinterpret_cast<uint4 *>(dz + v * 16)[1] = make_uint4(0u, 0u, 0u, 0u);
+    }
+    __shared__ double sl[32], sc[32];
+    for (int off = 16; off > 0; off >>= 1) {
+        ls += __shfl_down_sync(0xffffffffu, ls, off);
+        cnt += __shfl_down_sync(0xffffffffu, cnt, off);
+    }
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+        sl[w] = ls;
+        sc[w] = cnt;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) {
+            a += sl[i];
+            b += sc[i];
+        }
+        part[2 * blockIdx.x] = a;
+        part[2 * blockIdx.x + 1] = b;
+    }
+}
+// res[0] = mean loss, res[1] = active count; scale = 1 / count (0 if none)
+__global__ void k_loss_final(const double *__restrict__ part, int nblk, double *__restrict__ res,
+                             float *__restrict__ scale) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double a = 0.0, b = 0.0;
+    for (int i = 0; i < nblk; i++) {
+        a += part[2 * i];
+        b += part[2 * i + 1];
+    }
+    res[0] = b > 0 ? a / b : 0.0;
+    res[1] = b;
+    *scale = b > 0 ? (float)(1.0 / b) : 0.f;
+}
+
+// ------------------------------------------------------------ Adam + weights
+__global__ void k_adam(i64 n, float *__restrict__ w, const float *__restrict__ gr, float *__restrict__ m1,
+                       float *__restrict__ m2, float lr, float b1, float b2, float eps, float c1, float c2) {
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+        const float gv = gr[i];
+        const float a = b1 * m1[i] + (1.f - b1) * gv;
+        const float b = b2 * m2[i] + (1.f - b2) * gv * gv;
+        m1[i] = a;
+        m2[i] = b;
+        w[i] -= lr * (a / c1) / (sqrtf(b / c2) + eps);
+    }
+}
+// bf16 copies of one layer's weights: forward [tap][n][c] and transposed
+// [tap][c][n] (for the data gradient)
+__global__ void k_pack(const float *__restrict__ w, int cin, int cout, bf16 *__restrict__ wf, bf16 *__restrict__ wt) {
+    const int n = 27 * cin * cout;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int c = i % cin, no = (i / cin) % cout, tap = i / (cin * cout);
+        const bf16 b = __float2bfloat16_rn(w[i]);
+        wf[i] = b;
+        wt[((i64)tap * cin + c) * cout + no] = b;
+    }
+}
+
+}  // namespace
+
+// ====================================================================== host
+struct dmtz_cnn {
+    int device = 0;
+    int nsm = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    float *w = nullptr, *grad = nullptr, *m1 = nullptr, *m2 = nullptr;  // kParams each
+    bf16 *wf = nullptr, *wt = nullptr;  // bf16 weights, forward and transposed, per layer at woff[l]
+    float *part = nullptr;              // weight-gradient partials, part_blocks x (largest layer)
+    int part_blocks = 0;
+    double *lpart = nullptr, *lres = nullptr;
+    float *scale = nullptr;
+    i64 step = 0;
+    // activations of the last forward pass (a[2] aliases a[0] unless kept for training)
+    i64 capV = 0;
+    bool cap_train = false;
+    bf16 *a[3] = {nullptr, nullptr, nullptr};
+    bf16 *dz4 = nullptr, *gA = nullptr, *gB = nullptr;
+    int lastW = 0, lastH = 0, lastD = 0, last_train = 0;
+    const bf16 *last_feat = nullptr;
+    const float *last_out = nullptr;
+    // warm-start scratch
+    i64 capS = 0;
+    bf16 *feat = nullptr;
+    uint8_t *active = nullptr;
+    float *out = nullptr;
+};
+
+namespace {
+
+i64 woff(int l) {
+    i64 o = 0;
+    for (int k = 0; k < l; k++) o += 27LL * LCIN[k] * LCOUT[k];
+    return o;
+}
+constexpr i64 kWeights = 27LL * (16 * 32 + 32 * 32 + 32 * 32 + 32 * 16);
+
+dmtz_status nfail(dmtz_cnn *n, dmtz_status s, const std::string &m) {
+    if (n) n->err = m;
+    return s;
+}
+#define NCK(call)                                                                                 \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess)                                                                    \
+            return nfail(net, DMTZ_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+template <class T>
+cudaError_t nalloc(T **p, i64 n) {
+    return cudaMalloc((void **)p, sizeof(T) * (size_t)std::max<i64>(n, 1));
+}
+
+uint64_t splitmix(uint64_t &s) {
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+template <int CIN, int COUT, int MODE, bool FLIP>
+constexpr size_t conv_smem() {
+    return (size_t)(27 * COUT * (CIN + 8) + 2 * HALO * (CIN + 8)) * sizeof(bf16);
+}
+template <int CIN, int COUT>
+constexpr size_t wgrad_smem() {
+    return (size_t)(2 * HALO * (CIN + 8) + 2 * TV * (COUT + 8)) * sizeof(bf16);
+}
+
+// launches a persistent kernel with as many blocks as fit on the GPU (at most
+// one per tile); the dynamic shared-memory limit is raised once per kernel
+template <class K>
+dmtz_status launch_persistent(dmtz_cnn *net, K kernel, int threads, size_t smem, i64 ntiles, int cap_blocks,
+                              int *used_blocks, cudaStream_t st, void **args) {
+    NCK(cudaFuncSetAttribute((const void *)kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    NCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem));
+    if (per_sm < 1) return nfail(net, DMTZ_ERR_CUDA, "convolution kernel does not fit on an SM");
+    i64 blocks = std::min<i64>(ntiles, (i64)per_sm * net->nsm);
+    if (cap_blocks > 0) blocks = std::min<i64>(blocks, cap_blocks);
+    blocks = std::max<i64>(blocks, 1);
+    if (used_blocks) *used_blocks = (int)blocks;
+    NCK(cudaLaunchKernel((const void *)kernel, dim3((unsigned)blocks), dim3(threads), args, smem, st));
+    return DMTZ_OK;
+}
+
+template <int CIN, int COUT, int MODE, bool FLIP>
+dmtz_status conv(dmtz_cnn *net, const Dims &d, const bf16 *in, const bf16 *w, const float *bias, void *out,
+                 const bf16 *aux, cudaStream_t st) {
+    Dims dd = d;
+    void *args[] = {&dd, &in, &w, &bias, &out, &aux};
+    return launch_persistent(net, k_conv<CIN, COUT, MODE, FLIP>, 256, conv_smem<CIN, COUT, MODE, FLIP>(), d.ntiles, 0,
+                             nullptr, st, args);
+}
+
+template <int CIN, int COUT>
+dmtz_status wgrad(dmtz_cnn *net, const Dims &d, const bf16 *act, const bf16 *dz, float *grad_out, cudaStream_t st) {
+    Dims dd = d;
+    float *part = net->part;
+    void *args[] = {&dd, &act, &dz, &part};
+    int used = 0;
+    dmtz_status s = launch_persistent(net, k_wgrad<CIN, COUT>, 512, wgrad_smem<CIN, COUT>(), d.ntiles,
+                                      net->part_blocks, &used, st, args);
+    if (s != DMTZ_OK) return s;
+    const i64 n = 27LL * COUT * CIN + COUT;
+    k_reduce<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(net->part, used, n, net->scale, grad_out);
+    NCK(cudaGetLastError());
+    return DMTZ_OK;
+}
+
+dmtz_status pack(dmtz_cnn *net, cudaStream_t st) {
+    for (int l = 0; l < NLAYER; l++) {
+        k_pack<<<64, 256, 0, st>>>(net->w + layer_offset(l), LCIN[l], LCOUT[l], net->wf + woff(l), net->wt + woff(l));
+    }
+    NCK(cudaGetLastError());
+    return DMTZ_OK;
+}
+
+dmtz_status ensure_act(dmtz_cnn *net, i64 V, bool train) {
+    if (V <= net->capV && (!train || net->cap_train)) return DMTZ_OK;
+    cudaFree(net->a[0]);
+    cudaFree(net->a[1]);
+    if (net->cap_train) cudaFree(net->a[2]);
+    cudaFree(net->dz4);
+    cudaFree(net->gA);
+    cudaFree(net->gB);
+    net->a[0] = net->a[1] = net->a[2] = net->dz4 = net->gA = net->gB = nullptr;
+    net->capV = 0;
+    net->cap_train = false;
+    const i64 cap = std::max(V, net->capV);
+    NCK(nalloc(&net->a[0], cap * 32));
+    NCK(nalloc(&net->a[1], cap * 32));
+    if (train) {
+        NCK(nalloc(&net->a[2], cap * 32));
+        NCK(nalloc(&net->dz4, cap * 16));
+        NCK(nalloc(&net->gA, cap * 32));
+        NCK(nalloc(&net->gB, cap * 32));
+    } else {
+        net->a[2] = net->a[0];
+    }
+    net->capV = cap;
+    net->cap_train = train;
+    return DMTZ_OK;
+}
+
+dmtz_status check_grid(dmtz_cnn *net, int W, int H, int D) {
+    if (!net) return DMTZ_ERR_ARG;
+    if (W < 1 || H < 1 || D < 1) return nfail(net, DMTZ_ERR_ARG, "grid dimensions must be >= 1");
+    if ((i64)W * H * D > (1LL << 40)) return nfail(net, DMTZ_ERR_ARG, "grid too large");
+    return DMTZ_OK;
+}
+
+}  // namespace
+
+namespace dmtz_cnn_impl {
+
+const std::string &error_of(const dmtz_cnn *net) { return net->err; }
+int device_of(const dmtz_cnn *net) { return net->device; }
+
+dmtz_status forward_on(dmtz_cnn *net, int W, int H, int D, const bf16 *feat, float *out, int train,
+                       cudaStream_t st) {
+    dmtz_status s = check_grid(net, W, H, D);
+    if (s != DMTZ_OK) return s;
+    if (!feat || !out || ((uintptr_t)feat & 15)) return nfail(net, DMTZ_ERR_ARG, "features must be 16-byte aligned");
+    NCK(cudaSetDevice(net->device));
+    const Dims d = make_dims(W, H, D);
+    const i64 V = (i64)W * H * D;
+    if ((s = ensure_act(net, V, train != 0)) != DMTZ_OK) return s;
+    bf16 *a1 = net->a[0], *a2 = net->a[1], *a3 = net->a[2];
+    const float *w = net->w;
+    if ((s = conv<16, 32, 0, false>(net, d, feat, net->wf + woff(0), w + layer_offset(0) + 27 * 32 * 16, a1, nullptr,
+                                    st)) != DMTZ_OK)
+        return s;
+    if ((s = conv<32, 32, 0, false>(net, d, a1, net->wf + woff(1), w + layer_offset(1) + 27 * 32 * 32, a2, nullptr,
+                                    st)) != DMTZ_OK)
+        return s;
+    if ((s = conv<32, 32, 0, false>(net, d, a2, net->wf + woff(2), w + layer_offset(2) + 27 * 32 * 32, a3, nullptr,
+                                    st)) != DMTZ_OK)
+        return s;
+    if ((s = conv<32, 16, 1, false>(net, d, a3, net->wf + woff(3), w + layer_offset(3) + 27 * 16 * 32, out, nullptr,
+                                    st)) != DMTZ_OK)
+        return s;
+    net->lastW = W;
+    net->lastH = H;
+    net->lastD = D;
+    net->last_train = train != 0;
+    net->last_feat = feat;
+    net->last_out = out;
+    return DMTZ_OK;
+}
+
+dmtz_status scratch(dmtz_cnn *net, int64_t V, bf16 **feat, uint8_t **active, float **out) {
+    if (V > net->capS) {
+        cudaFree(net->feat);
+        cudaFree(net->active);
+        cudaFree(net->out);
+        net->feat = nullptr;
+        net->active = nullptr;
+        net->out = nullptr;
+        net->capS = 0;
+        NCK(nalloc(&net->feat, V * kFeat));
+        NCK(nalloc(&net->active, V));
+        NCK(nalloc(&net->out, V));
+        net->capS = V;
+    }
+    *feat = net->feat;
+    *active = net->active;
+    *out = net->out;
+    return DMTZ_OK;
+}
+
+}  // namespace dmtz_cnn_impl
+
+using dmtz_cnn_impl::forward_on;
+
+extern "C" {
+
+int64_t dmtz_cnn_num_params(void) { return kParams; }
+
+dmtz_status dmtz_cnn_create(dmtz_cnn **out, int device, uint64_t seed) {
+    if (!out) return DMTZ_ERR_ARG;
+    *out = nullptr;
+    dmtz_cnn *net = new dmtz_cnn();
+    net->device = device;
+    auto bail = [&](dmtz_status s) {
+        dmtz_cnn_destroy(net);
+        return s;
+    };
+    if (cudaSetDevice(device) != cudaSuccess) return bail(DMTZ_ERR_CUDA);
+    if (cudaDeviceGetAttribute(&net->nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
+        return bail(DMTZ_ERR_CUDA);
+    if (cudaStreamCreateWithFlags(&net->stream, cudaStreamNonBlocking) != cudaSuccess) return bail(DMTZ_ERR_CUDA);
+    net->part_blocks = 2 * net->nsm;
+    i64 largest = 0;
+    for (int l = 0; l < NLAYER; l++) largest = std::max(largest, layer_params(l));
+    if (nalloc(&net->w, kParams) || nalloc(&net->grad, kParams) || nalloc(&net->m1, kParams) ||
+        nalloc(&net->m2, kParams) || nalloc(&net->wf, kWeights) || nalloc(&net->wt, kWeights) ||
+        nalloc(&net->part, (i64)net->part_blocks * largest) || nalloc(&net->lpart, 2 * kLossBlocks) ||
+        nalloc(&net->lres, 2) || nalloc(&net->scale, 1))
+        return bail(DMTZ_ERR_CUDA);
+    // He-uniform weights (bound sqrt(6 / fan_in)); the output layer 0.1x and
+    // only its channel 0 nonzero; zero biases
+    std::vector<float> h((size_t)kParams, 0.f);
+    uint64_t s = seed ^ 0x6A09E667F3BCC909ull;
+    for (int l = 0; l < NLAYER; l++) {
+        const double b = std::sqrt(6.0 / (27.0 * LCIN[l])) * (l == NLAYER - 1 ? 0.1 : 1.0);
+        float *p = h.data() + layer_offset(l);
+        for (int tap = 0; tap < 27; tap++)
+            for (int n = 0; n < LCOUT[l]; n++)
+                for (int c = 0; c < LCIN[l]; c++) {
+                    const double u = (double)(splitmix(s) >> 11) * (1.0 / 9007199254740992.0);
+                    const bool live = l < NLAYER - 1 || n == 0;
+                    p[((i64)tap * LCOUT[l] + n) * LCIN[l] + c] = live ? (float)((2.0 * u - 1.0) * b) : 0.f;
+                }
+    }
+    if (dmtz_cnn_set_params(net, h.data()) != DMTZ_OK) return bail(DMTZ_ERR_CUDA);
+    *out = net;
+    return DMTZ_OK;
+}
+
+void dmtz_cnn_destroy(dmtz_cnn *net) {
+    if (!net) return;
+    cudaSetDevice(net->device);
+    if (net->stream) cudaStreamSynchronize(net->stream);
+    for (void *p : {(void *)net->w, (void *)net->grad, (void *)net->m1, (void *)net->m2, (void *)net->wf,
+                    (void *)net->wt, (void *)net->part, (void *)net->lpart, (void *)net->lres, (void *)net->scale,
+                    (void *)net->a[0], (void *)net->a[1], (void *)net->dz4, (void *)net->gA, (void *)net->gB,
+                    (void *)net->feat, (void *)net->active, (void *)net->out})
+        cudaFree(p);
+    if (net->cap_train) cudaFree(net->a[2]);
+    if (net->stream) cudaStreamDestroy(net->stream);
+    delete net;
+}
+
+const char *dmtz_cnn_last_error(const dmtz_cnn *net) { return net ? net->err.c_str() : "null network"; }
+
+dmtz_status dmtz_cnn_set_params(dmtz_cnn *net, const float *host) {
+    if (!net || !host) return DMTZ_ERR_ARG;
+    NCK(cudaSetDevice(net->device));
+    NCK(cudaMemcpyAsync(net->w, host, sizeof(float) * kParams, cudaMemcpyHostToDevice, net->stream));
+    NCK(cudaMemsetAsync(net->m1, 0, sizeof(float) * kParams, net->stream));
+    NCK(cudaMemsetAsync(net->m2, 0, sizeof(float) * kParams, net->stream));
+    NCK(cudaMemsetAsync(net->grad, 0, sizeof(float) * kParams, net->stream));
+    net->step = 0;
+    dmtz_status s = pack(net, net->stream);
+    if (s != DMTZ_OK) return s;
+    NCK(cudaStreamSynchronize(net->stream));
+    return DMTZ_OK;
+}
+
+dmtz_status dmtz_cnn_get_params(dmtz_cnn *net, float *host) {
+    if (!net || !host) return DMTZ_ERR_ARG;
+    NCK(cudaSetDevice(net->device));
+    NCK(cudaMemcpyAsync(host, net->w, sizeof(float) * kParams, cudaMemcpyDeviceToHost, net->stream));
+    NCK(cudaStreamSynchronize(net->stream));
+    return DMTZ_OK;
+}
+
+dmtz_status dmtz_cnn_get_grads(dmtz_cnn *net, float *host) {
+    if (!net || !host) return DMTZ_ERR_ARG;
+    NCK(cudaSetDevice(net->device));
+    NCK(cudaMemcpyAsync(host, net->grad, sizeof(float) * kParams, cudaMemcpyDeviceToHost, net->stream));
+    NCK(cudaStreamSynchronize(net->stream));
+    return DMTZ_OK;
+}
+
+dmtz_status dmtz_cnn_forward(dmtz_cnn *net, int W, int H, int D, const void *feat, float *out, int train) {
+    if (!net) return DMTZ_ERR_ARG;
+    dmtz_status s = forward_on(net, W, H, D, static_cast<const bf16 *>(feat), out, train, net->stream);
+    if (s != DMTZ_OK) return s;
+    NCK(cudaStreamSynchronize(net->stream));
+    return DMTZ_OK;
+}
+
+dmtz_status dmtz_cnn_backward(dmtz_cnn *net, int W, int H, int D, const float *target, const uint8_t *active,
+                              double *loss) {
+    dmtz_status s = check_grid(net, W, H, D);
+    if (s != DMTZ_OK) return s;
+    if (!target || !active) return nfail(net, DMTZ_ERR_ARG, "null target or mask");
+    if (!net->last_train || net->lastW != W || net->lastH != H || net->lastD != D)
+        return nfail(net, DMTZ_ERR_ARG, "backward needs a training forward pass on the same grid");
+    NCK(cudaSetDevice(net->device));
+    cudaStream_t st = net->stream;
+    const Dims d = make_dims(W, H, D);
+    const i64 V = (i64)W * H * D;
+    k_loss<<<kLossBlocks, 256, 0, st>>>(V, net->last_out, target, active, net->dz4, net->lpart);
+    k_loss_final<<<1, 32, 0, st>>>(net->lpart, kLossBlocks, net->lres, net->scale);
+    NCK(cudaGetLastError());
+    bf16 *a1 = net->a[0], *a2 = net->a[1], *a3 = net->a[2];
+    float *gr = net->grad;
+    // layer 4: data gradient into a3's space (ReLU mask of a3), weight gradient
+    if ((s = conv<16, 32, 2, true>(net, d, net->dz4, net->wt + woff(3), nullptr, net->gA, a3, st)) != DMTZ_OK) return s;
+    if ((s = wgrad<32, 16>(net, d, a3, net->dz4, gr + layer_offset(3), st)) != DMTZ_OK) return s;
+    // layer 3
+    if ((s = conv<32, 32, 2, true>(net, d, net->gA, net->wt + woff(2), nullptr, net->gB, a2, st)) != DMTZ_OK) return s;
+    if ((s = wgrad<32, 32>(net, d, a2, net->gA, gr + layer_offset(2), st)) != DMTZ_OK) return s;
+    // layer 2
+    if ((s = conv<32, 32, 2, true>(net, d, net->gB, net->wt + woff(1), nullptr, net->gA, a1, st)) != DMTZ_OK) return s;
+    if ((s = wgrad<32, 32>(net, d, a1, net->gB, gr + layer_offset(1), st)) != DMTZ_OK) return s;
+    // layer 1 (no data gradient of the features)
+    if ((s = wgrad<16, 32>(net, d, net->last_feat, net->gA, gr + layer_offset(0), st)) != DMTZ_OK) return s;
+    double res[2] = {0, 0};
+    NCK(cudaMemcpyAsync(res, net->lres, sizeof(res), cudaMemcpyDeviceToHost, st));
+    NCK(cudaStreamSynchronize(st));
+    if (loss) *loss = res[0];
+    return DMTZ_OK;
+}
+
+dmtz_status dmtz_cnn_step(dmtz_cnn *net, float lr) {
+    if (!net) return DMTZ_ERR_ARG;
+    if (!(lr >= 0.f) || !std::isfinite(lr)) return nfail(net, DMTZ_ERR_ARG, "learning rate must be finite, >= 0");
+    NCK(cudaSetDevice(net->device));
+    net->step++;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = (float)(1.0 - std::pow((double)b1, (double)net->step));
+    const float c2 = (float)(1.0 - std::pow((double)b2, (double)net->step));
+    k_adam<<<(unsigned)((kParams + 255) / 256), 256, 0, net->stream>>>(kParams, net->w, net->grad, net->m1, net->m2,
+                                                                       lr, b1, b2, 1e-8f, c1, c2);
+    NCK(cudaGetLastError());
+    dmtz_status s = pack(net, net->stream);
+    if (s != DMTZ_OK) return s;
+    NCK(cudaStreamSynchronize(net->stream));
+    return DMTZ_OK;
+}
+
+}  // extern "C"
+
+extern "C" dmtz_status dmtz_cnn_profile(dmtz_cnn *net, int W, int H, int D, const void *feat, float *out,
+                                        const float *target, const uint8_t *active, int reps, double ms[4]) {
+    dmtz_status s = check_grid(net, W, H, D);
+    if (s != DMTZ_OK) return s;
+    if (!ms || reps < 1 || !target || !active) return nfail(net, DMTZ_ERR_ARG, "bad profile arguments");
+    NCK(cudaSetDevice(net->device));
+    cudaStream_t st = net->stream;
+    const bf16 *fb = static_cast<const bf16 *>(feat);
+    cudaEvent_t e[2];
+    NCK(cudaEventCreate(&e[0]));
+    NCK(cudaEventCreate(&e[1]));
+    float t = 0.f;
+    auto timed = [&](auto &&body, double &acc) -> dmtz_status {
+        NCK(cudaEventRecord(e[0], st));
+        for (int r = 0; r < reps; r++) {
+            dmtz_status q = body();
+            if (q != DMTZ_OK) return q;
+        }
+        NCK(cudaEventRecord(e[1], st));
+        NCK(cudaEventSynchronize(e[1]));
+        NCK(cudaEventElapsedTime(&t, e[0], e[1]));
+        acc = (double)t / reps;
+        return DMTZ_OK;
+    };
+    // the training steps are undone afterwards: weights, Adam moments and step count
+    float *keep = nullptr;
+    NCK(nalloc(&keep, 3 * kParams));
+    NCK(cudaMemcpyAsync(keep, net->w, sizeof(float) * kParams, cudaMemcpyDeviceToDevice, st));
+    NCK(cudaMemcpyAsync(keep + kParams, net->m1, sizeof(float) * kParams, cudaMemcpyDeviceToDevice, st));
+    NCK(cudaMemcpyAsync(keep + 2 * kParams, net->m2, sizeof(float) * kParams, cudaMemcpyDeviceToDevice, st));
+    const i64 step0 = net->step;
+    const Dims d = make_dims(W, H, D);
+    if ((s = forward_on(net, W, H, D, fb, out, 1, st)) != DMTZ_OK) return s;  // warm-up, sizes buffers
+    NCK(cudaStreamSynchronize(st));
+    s = timed([&]() { return forward_on(net, W, H, D, fb, out, 0, st); }, ms[0]);
+    if (s == DMTZ_OK)
+        s = timed(
+            [&]() {
+                dmtz_status q = forward_on(net, W, H, D, fb, out, 1, st);
+                if (q == DMTZ_OK) q = dmtz_cnn_backward(net, W, H, D, target, active, nullptr);
+                if (q == DMTZ_OK) q = dmtz_cnn_step(net, 0.f);
+                return q;
+            },
+            ms[1]);
+    if (s == DMTZ_OK)
+        s = timed(
+            [&]() {
+                return conv<32, 32, 0, false>(net, d, net->a[0], net->wf + woff(1),
+                                              net->w + layer_offset(1) + 27 * 32 * 32, net->a[1], nullptr, st);
+            },
+            ms[2]);
+    if (s == DMTZ_OK)
+        s = timed([&]() { return wgrad<32, 32>(net, d, net->a[1], net->gB, net->grad + layer_offset(2), st); },
+                  ms[3]);
+    cudaEventDestroy(e[0]);
+    cudaEventDestroy(e[1]);
+    cudaMemcpyAsync(net->w, keep, sizeof(float) * kParams, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(net->m1, keep + kParams, sizeof(float) * kParams, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(net->m2, keep + 2 * kParams, sizeof(float) * kParams, cudaMemcpyDeviceToDevice, st);
+    net->step = step0;
+    const dmtz_status sp = pack(net, st);
+    NCK(cudaStreamSynchronize(st));
+    cudaFree(keep);
+    return s != DMTZ_OK ? s : sp;
+}

@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "../../include/dmtz.h"
+#include "cnn.cuh"
 #include "dmtz_common.cuh"
 #include "pairing.cuh"
 #include "pairing_fast.cuh"
@@ -461,6 +462,12 @@ __global__ void k_minmax(const double *a, i64 n, unsigned long long *kmin, unsig
     }
 }
 
+__global__ void k_count_u8(const uint8_t *a, i64 n, unsigned long long *out) {
+    unsigned long long c = 0;
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) c += a[i] != 0;
+    for (int off = 16; off > 0; off >>= 1) c += __shfl_down_sync(0xffffffffu, c, off);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
+}
 __global__ void k_fill_i32(int *p, int val, i64 n) {
     i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) p[i] = val;
@@ -475,6 +482,72 @@ __global__ void k_check_finite(const double *a, i64 n, int *bad) {
 // =============================================================================
 // host side
 // =============================================================================
+// ----------------------------------------------------- learned-proposal glue
+// Network input per vertex (layout in cnn.cuh) and the mismatch byte mm[v]
+// (criticality of v's own cells differs between the two gradients).
+__global__ void k_features(Grid g, const double *f, const double *gv, const uint32_t *critP, const uint32_t *critQ,
+                           double bound, __nv_bfloat16 *feat, uint8_t *mm) {
+    for (i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x; v < g.V; v += (i64)gridDim.x * blockDim.x) {
+        int x, y, z;
+        decode_v(g, v, x, y, z);
+        const double fv = f[v];
+        const bool mis = critP[v] != critQ[v];
+        mm[v] = mis;
+        float c[16];
+        c[0] = bound > 0 ? fminf(fmaxf((float)((gv[v] - fv) / bound), -1.f), 1.f) : 0.f;
+        c[1] = mis ? 1.f : 0.f;
+#pragma unroll
+        for (int k = 0; k < 14; k++) {
+            const int nx = x + TOPO_DIRS[k][0], ny = y + TOPO_DIRS[k][1], nz = z + TOPO_DIRS[k][2];
+            float cv = 0.f;
+            if (bound > 0 && nx >= 0 && nx < g.W && ny >= 0 && ny < g.H && nz >= 0 && nz < g.D)
+                cv = tanhf((float)((f[v + g.doff[k]] - fv) / (4.0 * bound)));
+            c[2 + k] = cv;
+        }
+        uint32_t packed[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const __nv_bfloat162 b = __floats2bfloat162_rn(c[2 * k], c[2 * k + 1]);
+            packed[k] = *reinterpret_cast<const uint32_t *>(&b);
+        }
+        uint4 *dst = reinterpret_cast<uint4 *>(feat + v * 16);
+        dst[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+        dst[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+    }
+}
+// dst[v] = max of src over v + k*step, |k| <= 2, along one axis (in-grid)
+__global__ void k_dilate(Grid g, int axis, const uint8_t *src, uint8_t *dst) {
+    const i64 step = axis == 0 ? 1 : axis == 1 ? (i64)g.W : g.WH;
+    for (i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x; v < g.V; v += (i64)gridDim.x * blockDim.x) {
+        int c[3];
+        decode_v(g, v, c[0], c[1], c[2]);
+        const int n = axis == 0 ? g.W : axis == 1 ? g.H : g.D;
+        uint8_t m = 0;
+        for (int k = -2; k <= 2; k++) {
+            const int q = c[axis] + k;
+            if (q >= 0 && q < n) m |= src[v + k * step];
+        }
+        dst[v] = m;
+    }
+}
+// Proposal at active vertices: g <- min(g, f + bound * tanh(o)); a value that
+// the reference's own bound test |f - g| <= bound would reject becomes
+// f - bound, the value the reference falls back to (main_3d.cu:1133-1141).
+__global__ void k_propose(i64 V, const double *f, double *gv, const float *o, const uint8_t *active, double bound,
+                          uint8_t *changed) {
+    for (i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (i64)gridDim.x * blockDim.x) {
+        if (!active[v]) continue;
+        const double fv = f[v], old = gv[v];
+        const double p = __dadd_rn(fv, __dmul_rn(bound, (double)tanhf(o[v])));
+        double nv = p < old ? p : old;
+        if (fabs(__dsub_rn(fv, nv)) > bound) nv = __dsub_rn(fv, bound);
+        if (nv != old) {
+            gv[v] = nv;
+            changed[v] = 1;
+        }
+    }
+}
+
 struct DevField {
     uint64_t *key = nullptr;
     uint16_t *low = nullptr;
@@ -506,13 +579,16 @@ struct dmtz_ctx {
     uint32_t *brick_list = nullptr;   // their compacted list (counters[11])
     i64 *sad2 = nullptr;      // original 2-saddle triangles
     unsigned long long *counters = nullptr;  // [0..3] cp lists, [4] requests, [5,6] paths, [8,9] min/max
-                                             // keys, [10] original 2-saddles, [11] dirty bricks
+                                             // keys, [10] original 2-saddles, [11] dirty bricks,
+                                             // [12] edited vertices
     int *errword = nullptr;
     uint8_t *changed = nullptr;
     int64_t launches = 0;  // kernels launched by the current call
     int tune_shape = 0;    // brick shape (DMTZ_SHAPES) chosen by dmtz_autotune
     int tune_bps = 16;     // sweep blocks per SM
     std::vector<dmtz_ctx *> pool;  // worker contexts of dmtz_correct_batch
+    uint8_t *mm = nullptr;         // mismatch bytes of the learned proposal's features
+    i64 capMM = 0;
 };
 
 namespace {
@@ -791,6 +867,7 @@ void dmtz_ctx_destroy(dmtz_ctx *ctx) {
     ctx->pool.clear();
     cudaSetDevice(ctx->device);
     free_all(ctx);
+    cudaFree(ctx->mm);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -1149,8 +1226,49 @@ static dmtz_status run_graph_loop(dmtz_ctx *ctx, const Grid &g, const RuleCtx &r
 }
 
 // ----------------------------------------------------------------------------- the correction loop
-dmtz_status dmtz_correct(dmtz_ctx *ctx, int W, int H, int D, const double *orig, double *decp, int on_device,
-                         double rel_eps, const dmtz_opts *opts, dmtz_report *rep, int32_t *edit_counter_out) {
+// features of (ctx->f, ctx->g) from the current gradients ctx->P / ctx->Q
+static dmtz_status features_into(dmtz_ctx *ctx, const Grid &g, double bound, __nv_bfloat16 *feat, uint8_t *active) {
+    if (g.V > ctx->capMM) {
+        cudaFree(ctx->mm);
+        ctx->mm = nullptr;
+        ctx->capMM = 0;
+        CK(dalloc(&ctx->mm, g.V));
+        ctx->capMM = g.V;
+    }
+    cudaStream_t st = ctx->stream;
+    const unsigned grid = persistent_grid();
+    k_features<<<grid, kBlock, 0, st>>>(g, ctx->f, ctx->g, ctx->P.crit, ctx->Q.crit, bound, feat, ctx->mm);
+    k_dilate<<<grid, kBlock, 0, st>>>(g, 0, ctx->mm, active);
+    k_dilate<<<grid, kBlock, 0, st>>>(g, 1, active, ctx->mm);
+    k_dilate<<<grid, kBlock, 0, st>>>(g, 2, ctx->mm, active);
+    ctx->launches += 4;
+    CK(cudaGetLastError());
+    return DMTZ_OK;
+}
+
+// Learned warm start: features, network, proposal, then the gradient of the
+// edited field and its mismatch lists again.
+static dmtz_status learned_start(dmtz_ctx *ctx, dmtz_cnn *net, const Grid &g, double bound) {
+    using namespace dmtz_cnn_impl;
+    if (device_of(net) != ctx->device) return fail(ctx, DMTZ_ERR_ARG, "network and context on different devices");
+    __nv_bfloat16 *feat;
+    uint8_t *active;
+    float *out;
+    dmtz_status s = scratch(net, g.V, &feat, &active, &out);
+    if (s != DMTZ_OK) return fail(ctx, s, "network: " + error_of(net));
+    if ((s = features_into(ctx, g, bound, feat, active)) != DMTZ_OK) return s;
+    s = forward_on(net, g.W, g.H, g.D, feat, out, 0, ctx->stream);
+    if (s != DMTZ_OK) return fail(ctx, s, "network: " + error_of(net));
+    k_propose<<<persistent_grid(), kBlock, 0, ctx->stream>>>(g.V, ctx->f, ctx->g, out, active, bound, ctx->changed);
+    ctx->launches += 5;
+    run_pairing(ctx, g, view(ctx->Q, ctx->g), ctx->P.crit, 1);
+    CK(cudaGetLastError());
+    return DMTZ_OK;
+}
+
+static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int D, const double *orig, double *decp,
+                                int on_device, double rel_eps, const dmtz_opts *opts, dmtz_report *rep,
+                                int32_t *edit_counter_out) {
     Grid g;
     dmtz_status s = check_dims(ctx, W, H, D, g);
     if (s != DMTZ_OK) return s;
@@ -1203,6 +1321,12 @@ dmtz_status dmtz_correct(dmtz_ctx *ctx, int W, int H, int D, const double *orig,
     dmtz_report R;
     memset(&R, 0, sizeof(R));
     for (int k = 0; k < 4; k++) R.initial_mismatch[k] = (int64_t)hc[k];
+    if (net) {
+        pt_.begin(PH_SETUP);
+        if ((s = learned_start(ctx, net, g, bound)) != DMTZ_OK) return s;
+        pt_.end();
+        if ((s = read_counts()) != DMTZ_OK) return s;
+    }
     i64 cc[4] = {(i64)hc[0], (i64)hc[1], (i64)hc[2], (i64)hc[3]};
     i64 n_as = 1, n_ds = 1, n_wall = 1;
     i64 rounds = 0;
@@ -1301,6 +1425,10 @@ dmtz_status dmtz_correct(dmtz_ctx *ctx, int W, int H, int D, const double *orig,
         }
     }
     CK(cudaEventRecord(e1, st));
+    CK(cudaMemsetAsync(ctx->counters + 12, 0, sizeof(unsigned long long), st));
+    k_count_u8<<<persistent_grid(), kBlock, 0, st>>>(ctx->changed, g.V, ctx->counters + 12);
+    unsigned long long n_edited = 0;
+    CK(cudaMemcpyAsync(&n_edited, ctx->counters + 12, sizeof(n_edited), cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(decp, ctx->g, sizeof(double) * (size_t)g.V,
                        on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
     if (edit_counter_out)
@@ -1317,6 +1445,7 @@ dmtz_status dmtz_correct(dmtz_ctx *ctx, int W, int H, int D, const double *orig,
     R.final_paths[0] = n_as;
     R.final_paths[1] = n_ds;
     R.converged = converged;
+    R.edited_vertices = (int64_t)n_edited;
     R.error_flags = err;
     R.seconds = ms * 1e-3;
     R.kernel_launches = ctx->launches;
@@ -1325,6 +1454,39 @@ dmtz_status dmtz_correct(dmtz_ctx *ctx, int W, int H, int D, const double *orig,
     if (err & ERR_OOB) return fail(ctx, DMTZ_ERR_OOB, "a fix rule indexed out of range");
     if (err & ERR_WALK) return fail(ctx, DMTZ_ERR_CYCLE, "ascending path walk exceeded its step cap");
     if (!converged) return fail(ctx, DMTZ_ERR_NONCONVERGED, "round cap reached before the complexes agree");
+    return DMTZ_OK;
+}
+
+dmtz_status dmtz_correct(dmtz_ctx *ctx, int W, int H, int D, const double *orig, double *decp, int on_device,
+                         double rel_eps, const dmtz_opts *opts, dmtz_report *rep, int32_t *edit_counter_out) {
+    return correct_impl(ctx, nullptr, W, H, D, orig, decp, on_device, rel_eps, opts, rep, edit_counter_out);
+}
+
+dmtz_status dmtz_correct_learned(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int D, const double *orig,
+                                 double *decp, int on_device, double rel_eps, const dmtz_opts *opts,
+                                 dmtz_report *rep, int32_t *edit_counter_out) {
+    if (!net) return fail(ctx, DMTZ_ERR_ARG, "null network");
+    return correct_impl(ctx, net, W, H, D, orig, decp, on_device, rel_eps, opts, rep, edit_counter_out);
+}
+
+dmtz_status dmtz_features(dmtz_ctx *ctx, int W, int H, int D, const double *orig, const double *decp, int on_device,
+                          double rel_eps, void *feat, uint8_t *active) {
+    Grid g;
+    dmtz_status s = check_dims(ctx, W, H, D, g);
+    if (s != DMTZ_OK) return s;
+    if (!feat || !active || ((uintptr_t)feat & 15)) return fail(ctx, DMTZ_ERR_ARG, "feat must be 16-byte aligned");
+    if (!(rel_eps >= 0.0) || !std::isfinite(rel_eps)) return fail(ctx, DMTZ_ERR_ARG, "rel_eps must be finite and >= 0");
+    CK(cudaSetDevice(ctx->device));
+    if ((s = ensure(ctx, g)) != DMTZ_OK) return s;
+    if ((s = upload(ctx, ctx->f, orig, g.V, on_device)) != DMTZ_OK) return s;
+    if ((s = upload(ctx, ctx->g, decp, g.V, on_device)) != DMTZ_OK) return s;
+    double mn, mx;
+    if ((s = device_minmax(ctx, ctx->f, g.V, mn, mx)) != DMTZ_OK) return s;
+    run_pairing(ctx, g, view(ctx->P, ctx->f), nullptr, 1);
+    run_pairing(ctx, g, view(ctx->Q, ctx->g), nullptr, 1);
+    if ((s = features_into(ctx, g, (mx - mn) * rel_eps, static_cast<__nv_bfloat16 *>(feat), active)) != DMTZ_OK)
+        return s;
+    CK(cudaStreamSynchronize(ctx->stream));
     return DMTZ_OK;
 }
 

@@ -66,7 +66,8 @@ typedef struct {
     int64_t initial_mismatch[4];/* min, 1-saddle, 2-saddle, max before correction */
     int64_t final_mismatch[4];
     int64_t final_paths[2];     /* ascending, descending separatrix records */
-    int64_t edited_vertices;    /* vertices whose value changed */
+    int64_t edited_vertices;    /* vertices the correction wrote at least once (a
+                                   vertex written back to its input value counts) */
     int32_t converged;
     int32_t error_flags;        /* bit 0: out-of-range index met by a fix rule,
                                    bit 1: path-walk step cap reached */
@@ -188,6 +189,64 @@ dmtz_status dmtz_autotune(dmtz_ctx *ctx, int W, int H, int D, const double *orig
  * No counterpart call in the reference (measurement only). */
 dmtz_status dmtz_profile_sweep(dmtz_ctx *ctx, int W, int H, int D, const double *orig, const double *decp,
                                int on_device, int reps, double ms[7]);
+
+/* ---- learned proposal (no counterpart in the reference) ----
+ * A small convolutional network proposes corrected values near mismatches;
+ * the exact correction loop then starts from that proposal instead of the
+ * decompressed field.  Network: 3x3x3 convolutions 16 -> 32 -> 32 -> 32 -> 1
+ * channels, ReLU between layers, bf16 weights and activations with fp32
+ * accumulation on the tensor cores.  Proposed value at an active vertex:
+ * min(g, f + bound * tanh(o)), kept within the bound.
+ *
+ * Features (dmtz_features): per vertex 16 bf16 channels, channels-last:
+ *   0 (g - f) / bound; 1 = 1 where the vertex's own cells differ in
+ *   criticality between the two gradients; 2..15 tanh((f(u) - f(v)) /
+ *   (4 bound)) for the 14 Freudenthal neighbours u (0 outside the grid).
+ * active[v] = 1 within 2 vertices (per axis) of such a mismatch.
+ *
+ * Network buffers (feat, out, target, active) are DEVICE pointers on the
+ * network's device; feat must be 16-byte aligned.  Calls are synchronous. */
+typedef struct dmtz_cnn dmtz_cnn;
+#define DMTZ_CNN_FEATURES 16
+/* number of float parameters (get/set/grad layout: per layer, weights
+ * [27 taps][out][in] (tap = (dz+1)*9 + (dy+1)*3 + dx+1), then bias [out];
+ * layers 16->32, 32->32, 32->32, 32->16 of which only output 0 is used) */
+int64_t dmtz_cnn_num_params(void);
+dmtz_status dmtz_cnn_create(dmtz_cnn **out, int device, uint64_t seed);
+void dmtz_cnn_destroy(dmtz_cnn *net);
+const char *dmtz_cnn_last_error(const dmtz_cnn *net);
+dmtz_status dmtz_cnn_set_params(dmtz_cnn *net, const float *host);  /* also resets Adam */
+dmtz_status dmtz_cnn_get_params(dmtz_cnn *net, float *host);
+dmtz_status dmtz_cnn_get_grads(dmtz_cnn *net, float *host);
+/* out (V floats) = pre-tanh output o; train != 0 keeps the activations for
+ * dmtz_cnn_backward */
+dmtz_status dmtz_cnn_forward(dmtz_cnn *net, int W, int H, int D, const void *feat, float *out, int train);
+/* loss = mean over active vertices of (tanh(o) - target)^2; the parameter
+ * gradient of that loss goes into the network's gradient buffer */
+dmtz_status dmtz_cnn_backward(dmtz_cnn *net, int W, int H, int D, const float *target, const uint8_t *active,
+                              double *loss);
+/* one Adam step (beta 0.9 / 0.999, eps 1e-8) with learning rate lr */
+dmtz_status dmtz_cnn_step(dmtz_cnn *net, float lr);
+/* Timing of the network kernels on a W x H x D grid (CUDA events on the
+ * network's stream, `reps` repetitions each; measurement only): ms[0] = one
+ * forward pass (inference), ms[1] = one training step (forward, backward,
+ * Adam with learning rate 0; parameters and Adam state are restored
+ * afterwards), ms[2] = one
+ * 32 -> 32 convolution launch, ms[3] = one 32 x 32 weight-gradient launch
+ * (with its reduction). */
+dmtz_status dmtz_cnn_profile(dmtz_cnn *net, int W, int H, int D, const void *feat, float *out, const float *target,
+                             const uint8_t *active, int reps, double ms[4]);
+/* features and active mask of (orig, decp); feat / active are device
+ * pointers (V x 16 bf16, V bytes); orig / decp as in dmtz_correct */
+dmtz_status dmtz_features(dmtz_ctx *ctx, int W, int H, int D, const double *orig, const double *decp, int on_device,
+                          double rel_eps, void *feat, uint8_t *active);
+/* dmtz_correct started from the network's proposal.  The result keeps the
+ * reference loop's guarantees (gradients agree, |decp - orig| <= bound) but
+ * is not the reference's output, which starts from the unedited field.
+ * report->seconds includes features, network and proposal (phase "set-up"). */
+dmtz_status dmtz_correct_learned(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int D, const double *orig,
+                                 double *decp, int on_device, double rel_eps, const dmtz_opts *opts,
+                                 dmtz_report *report, int32_t *edit_counter_out);
 
 /* Allocation-free variant of dmtz_extract, for callers that cannot call
  * cudaMalloc: applications whose device memory is owned by their own pool

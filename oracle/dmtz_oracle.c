@@ -734,6 +734,21 @@ int orc_pair(int W, int H, int D, const double *data, int *PV, int *PE, int *PF,
  * ------------------------------------------------------------------------- */
 static int xor_crit(int p, int q) { return (q == -1 && p != -1) || (q != -1 && p == -1); }
 
+/* vertex at the componentwise minimum of n vertices */
+static int anchor_of(const grid_t *G, const int *vs, int n) {
+    int mx = 1 << 30, my = 1 << 30, mz = 1 << 30;
+    for (int i = 0; i < n; i++) {
+        int x, y, z;
+        x = vs[i] % G->W;
+        y = (vs[i] / G->W) % G->H;
+        z = vs[i] / (G->W * G->H);
+        if (x < mx) mx = x;
+        if (y < my) my = y;
+        if (z < mz) mz = z;
+    }
+    return mx + my * G->W + mz * G->W * G->H;
+}
+
 void orc_cp_mismatch(int W, int H, int D, const int *PV, const int *PE, const int *PF, const int *PT,
                      const int *QV, const int *QE, const int *QF, const int *QT, int counts[4], int *lmin,
                      int *lsad, int *l2sad, int *lmax) {
@@ -1580,4 +1595,31 @@ void orc_edge_verts(int W, int H, int D, int n, const int *edges, int *out2) {
     grid_t G;
     grid_init(&G, W, H, D);
     for (int i = 0; i < n; i++) edge_verts(&G, edges[i], &out2[2 * i], &out2[2 * i + 1]);
+}
+
+/* Mismatch anchors of the learned proposal's features: mask[v] = 1 when some
+ * cell whose componentwise-minimum vertex is v is critical in exactly one of
+ * the two pairings (the same per-cell test as get_false_*, main_3d.cu:
+ * 2492-2550, gathered per anchor vertex instead of listed). */
+void orc_mismatch_anchors(int W, int H, int D, const int *PV, const int *PE, const int *PF, const int *PT,
+                          const int *QV, const int *QE, const int *QF, const int *QT, unsigned char *mask) {
+    grid_t G;
+    grid_init(&G, W, H, D);
+    for (int i = 0; i < G.V; i++) mask[i] = (unsigned char)xor_crit(PV[i], QV[i]);
+    int vs[4];
+    for (int e = 0; e < G.E; e++)
+        if (xor_crit(PE[e], QE[e])) {
+            edge_verts(&G, e, &vs[0], &vs[1]);
+            mask[anchor_of(&G, vs, 2)] = 1;
+        }
+    for (int t = 0; t < G.F; t++)
+        if (xor_crit(PF[t], QF[t])) {
+            tri_verts(&G, t, &vs[0], &vs[1], &vs[2]);
+            mask[anchor_of(&G, vs, 3)] = 1;
+        }
+    for (int t = 0; t < G.T; t++)
+        if (xor_crit(PT[t], QT[t])) {
+            tet_verts(&G, t, &vs[0], &vs[1], &vs[2], &vs[3]);
+            mask[anchor_of(&G, vs, 4)] = 1;
+        }
 }

@@ -92,6 +92,12 @@ int orc_labels(int W, int H, int D, const double *data, int *desc, int *asc, int
 void orc_face_cofaces(int W, int H, int D, int n, const int *faces, int *out2);
 void orc_edge_verts(int W, int H, int D, int n, const int *edges, int *out2);
 
+/* mask[v] (V bytes) = 1 when a cell anchored at v (componentwise-minimum
+ * vertex) is critical in exactly one of the two pairings */
+void orc_mismatch_anchors(int W, int H, int D,
+                          const int *PV, const int *PE, const int *PF, const int *PT,
+                          const int *QV, const int *QE, const int *QF, const int *QT, unsigned char *mask);
+
 #ifdef __cplusplus
 }
 #endif

@@ -53,6 +53,9 @@ def lib():
         L.orc_labels.restype = ctypes.c_int
         L.orc_face_cofaces.argtypes = [ctypes.c_int] * 4 + [_i32p, _i32p]
         L.orc_edge_verts.argtypes = [ctypes.c_int] * 4 + [_i32p, _i32p]
+        L.orc_mismatch_anchors.argtypes = [ctypes.c_int] * 3 + [_i32p] * 8 + [
+            np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")]
+        L.orc_mismatch_anchors.restype = None
         _lib = L
     return _lib
 
@@ -161,3 +164,11 @@ def edge_verts(edges, dims):
     out = np.empty(2 * max(e.size, 1), np.int32)
     lib().orc_edge_verts(*dims, int(e.size), e if e.size else np.zeros(1, np.int32), out)
     return out[: 2 * e.size].reshape(-1, 2)
+
+
+def mismatch_anchors(P, Q, dims):
+    """uint8 per vertex: 1 where a cell anchored there is critical in exactly one pairing."""
+    W, H, D = dims
+    out = np.zeros(W * H * D, np.uint8)
+    lib().orc_mismatch_anchors(W, H, D, *P, *Q, out)
+    return out
