@@ -355,21 +355,23 @@ __global__ void k_reduce(const float *__restrict__ part, int nblk, i64 n, const 
 }
 
 // ------------------------------------------------------------------- the loss
-// Over active vertices: L = mean (tanh(o) - target)^2.  Writes dL/do without
-// the 1/count factor (applied by k_reduce) into channel 0 of dz (16 channels,
-// the others 0), and per-block (sum, count) partials.
+// Weighted over vertices (weight = the byte active[v], 0 = ignored):
+// L = sum w (tanh(o) - target)^2 / sum w.  Writes dL/do without the 1/sum w
+// factor (applied by k_reduce) into channel 0 of dz (16 channels, the others
+// 0), and per-block (weighted sum, sum of weights) partials.
 constexpr int kLossBlocks = 1024;
 __global__ void k_loss(i64 V, const float *__restrict__ o, const float *__restrict__ target,
                        const uint8_t *__restrict__ active, bf16 *__restrict__ dz, double *__restrict__ part) {
     double ls = 0.0, cnt = 0.0;
     for (i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (i64)gridDim.x * blockDim.x) {
         float gval = 0.f;
-        if (active[v]) {
+        const float w = (float)active[v];
+        if (w > 0.f) {
             const float y = tanhf(o[v]);
             const float e = y - target[v];
-            ls += (double)e * e;
-            cnt += 1.0;
-            gval = 2.f * e * (1.f - y * y);
+            ls += (double)w * e * e;
+            cnt += w;
+            gval = 2.f * w * e * (1.f - y * y);
         }
         const __nv_bfloat162 lo = __floats2bfloat162_rn(gval, 0.f);
         uint4 first = make_uint4(*reinterpret_cast<const uint32_t *>(&lo), 0u, 0u, 0u);
@@ -397,7 +399,7 @@ __global__ void k_loss(i64 V, const float *__restrict__ o, const float *__restri
         part[2 * blockIdx.x + 1] = b;
     }
 }
-// res[0] = mean loss, res[1] = active count; scale = 1 / count (0 if none)
+// res[0] = mean loss, res[1] = sum of weights; scale = 1 / that (0 if none)
 __global__ void k_loss_final(const double *__restrict__ part, int nblk, double *__restrict__ res,
                              float *__restrict__ scale) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
@@ -439,6 +441,7 @@ __global__ void k_pack(const float *__restrict__ w, int cin, int cout, bf16 *__r
 
 // ====================================================================== host
 struct dmtz_cnn {
+    float min_drop = 0.5f;  // proposal applied only where it lowers g by >= min_drop * bound
     int device = 0;
     int nsm = 0;
     cudaStream_t stream = nullptr;
@@ -595,6 +598,7 @@ namespace dmtz_cnn_impl {
 
 const std::string &error_of(const dmtz_cnn *net) { return net->err; }
 int device_of(const dmtz_cnn *net) { return net->device; }
+float min_drop_of(const dmtz_cnn *net) { return net->min_drop; }
 
 dmtz_status forward_on(dmtz_cnn *net, int W, int H, int D, const bf16 *feat, float *out, int train,
                        cudaStream_t st) {
@@ -712,6 +716,13 @@ void dmtz_cnn_destroy(dmtz_cnn *net) {
 }
 
 const char *dmtz_cnn_last_error(const dmtz_cnn *net) { return net ? net->err.c_str() : "null network"; }
+
+dmtz_status dmtz_cnn_set_min_drop(dmtz_cnn *net, float min_drop) {
+    if (!net) return DMTZ_ERR_ARG;
+    if (!(min_drop >= 0.f) || !(min_drop <= 2.f)) return nfail(net, DMTZ_ERR_ARG, "min_drop must be in [0, 2]");
+    net->min_drop = min_drop;
+    return DMTZ_OK;
+}
 
 dmtz_status dmtz_cnn_set_params(dmtz_cnn *net, const float *host) {
     if (!net || !host) return DMTZ_ERR_ARG;

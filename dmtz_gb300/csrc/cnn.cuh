@@ -31,5 +31,6 @@ dmtz_status scratch(dmtz_cnn *net, int64_t V, __nv_bfloat16 **feat, uint8_t **ac
 
 const std::string &error_of(const dmtz_cnn *net);
 int device_of(const dmtz_cnn *net);
+float min_drop_of(const dmtz_cnn *net);
 
 }  // namespace dmtz_cnn_impl

@@ -530,16 +530,18 @@ __global__ void k_dilate(Grid g, int axis, const uint8_t *src, uint8_t *dst) {
         dst[v] = m;
     }
 }
-// Proposal at active vertices: g <- min(g, f + bound * tanh(o)); a value that
+// Proposal at active vertices: g <- f + bound * tanh(o) where that lowers g by
+// at least min_drop (absolute; the network's min_drop x bound); a value that
 // the reference's own bound test |f - g| <= bound would reject becomes
 // f - bound, the value the reference falls back to (main_3d.cu:1133-1141).
 __global__ void k_propose(i64 V, const double *f, double *gv, const float *o, const uint8_t *active, double bound,
-                          uint8_t *changed) {
+                          double min_drop, uint8_t *changed) {
     for (i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (i64)gridDim.x * blockDim.x) {
         if (!active[v]) continue;
         const double fv = f[v], old = gv[v];
         const double p = __dadd_rn(fv, __dmul_rn(bound, (double)tanhf(o[v])));
-        double nv = p < old ? p : old;
+        if (!(old - p >= min_drop)) continue;  // keep g unless the proposal lowers it enough
+        double nv = p;
         if (fabs(__dsub_rn(fv, nv)) > bound) nv = __dsub_rn(fv, bound);
         if (nv != old) {
             gv[v] = nv;
@@ -1259,7 +1261,8 @@ static dmtz_status learned_start(dmtz_ctx *ctx, dmtz_cnn *net, const Grid &g, do
     if ((s = features_into(ctx, g, bound, feat, active)) != DMTZ_OK) return s;
     s = forward_on(net, g.W, g.H, g.D, feat, out, 0, ctx->stream);
     if (s != DMTZ_OK) return fail(ctx, s, "network: " + error_of(net));
-    k_propose<<<persistent_grid(), kBlock, 0, ctx->stream>>>(g.V, ctx->f, ctx->g, out, active, bound, ctx->changed);
+    k_propose<<<persistent_grid(), kBlock, 0, ctx->stream>>>(g.V, ctx->f, ctx->g, out, active, bound,
+                                                              (double)min_drop_of(net) * bound, ctx->changed);
     ctx->launches += 5;
     run_pairing(ctx, g, view(ctx->Q, ctx->g), ctx->P.crit, 1);
     CK(cudaGetLastError());

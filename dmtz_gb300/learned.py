@@ -9,8 +9,9 @@ A trace is what the exact correction did to one field:
     target  (g_final - f) / bound in [-1, 1], g_final = the corrected field.
 Training minimises mean (tanh(o) - target)^2 over active vertices with Adam.
 
-At inference dmtz_correct_learned lowers every active vertex to
-min(g, f + bound * tanh(o)) and then runs the exact loop, so the output keeps
+At inference dmtz_correct_learned sets an active vertex to f + bound * tanh(o)
+where that lowers g by at least min_drop x bound, then runs the exact loop, so
+the output keeps
 the loop's guarantees whatever the network predicts; the network can only
 change how many rounds the loop needs.
 """
@@ -38,7 +39,7 @@ def _torch():
 class Trace:
     dims: tuple
     feat: object      # torch bf16 (V, 16), device
-    active: object    # torch uint8 (V,), device
+    active: object    # torch uint8 (V,), device: loss weight, 0 outside the active mask
     target: object    # torch float32 (V,), device
     n_active: int
     report: dict = field(default_factory=dict)
@@ -51,9 +52,11 @@ def trace_fields(dims, seed, rel_eps, kind="powerlaw"):
     return f, g
 
 
-def make_trace(ctx: Context, f, g, rel_eps, flags=FULL_MSC, max_rounds=2000, use_graph=1):
+def make_trace(ctx: Context, f, g, rel_eps, flags=FULL_MSC, max_rounds=2000, use_graph=1, edit_weight=8):
     """Trace of one field, or None when the exact loop does not converge
-    within max_rounds (the reference's loop can stall on such fields)."""
+    within max_rounds (the reference's loop can stall on such fields).  The
+    loss weight of an active vertex is 1, or edit_weight where the loop
+    changed its value (those are rare and are what the proposal must find)."""
     torch = _torch()
     f = np.ascontiguousarray(f, np.float64)
     D, H, W = f.shape
@@ -74,7 +77,8 @@ def make_trace(ctx: Context, f, g, rel_eps, flags=FULL_MSC, max_rounds=2000, use
     bound = rel_eps * float(f.max() - f.min())
     target = ((gfix - fd) / bound).clamp_(-1.0, 1.0).float() if bound > 0 else torch.zeros_like(gfix).float()
     n_active = int(active.sum().item())
-    return Trace(dims, feat, active, target, n_active, rep)
+    weight = active * torch.where(gfix != gd, int(edit_weight), 1).to(torch.uint8)
+    return Trace(dims, feat, weight, target, n_active, rep)
 
 
 def make_traces(ctx: Context, n, dims=(128, 128, 128), seed0=1000, rel_eps=1e-4, flags=FULL_MSC, log=None):

@@ -195,8 +195,10 @@ dmtz_status dmtz_profile_sweep(dmtz_ctx *ctx, int W, int H, int D, const double 
  * the exact correction loop then starts from that proposal instead of the
  * decompressed field.  Network: 3x3x3 convolutions 16 -> 32 -> 32 -> 32 -> 1
  * channels, ReLU between layers, bf16 weights and activations with fp32
- * accumulation on the tensor cores.  Proposed value at an active vertex:
- * min(g, f + bound * tanh(o)), kept within the bound.
+ * accumulation on the tensor cores.  At an active vertex the proposal
+ * p = f + bound * tanh(o) replaces g where it lowers g by at least
+ * min_drop * bound (dmtz_cnn_set_min_drop, default 0.5); values stay within
+ * the bound.
  *
  * Features (dmtz_features): per vertex 16 bf16 channels, channels-last:
  *   0 (g - f) / bound; 1 = 1 where the vertex's own cells differ in
@@ -221,10 +223,14 @@ dmtz_status dmtz_cnn_get_grads(dmtz_cnn *net, float *host);
 /* out (V floats) = pre-tanh output o; train != 0 keeps the activations for
  * dmtz_cnn_backward */
 dmtz_status dmtz_cnn_forward(dmtz_cnn *net, int W, int H, int D, const void *feat, float *out, int train);
-/* loss = mean over active vertices of (tanh(o) - target)^2; the parameter
- * gradient of that loss goes into the network's gradient buffer */
+/* loss = sum_v w_v (tanh(o_v) - target_v)^2 / sum_v w_v with the weight
+ * w_v = active[v] (0..255; a 0/1 mask gives the mean over active vertices);
+ * the parameter gradient of that loss goes into the network's gradient
+ * buffer */
 dmtz_status dmtz_cnn_backward(dmtz_cnn *net, int W, int H, int D, const float *target, const uint8_t *active,
                               double *loss);
+/* proposal threshold in units of the bound, 0..2 */
+dmtz_status dmtz_cnn_set_min_drop(dmtz_cnn *net, float min_drop);
 /* one Adam step (beta 0.9 / 0.999, eps 1e-8) with learning rate lr */
 dmtz_status dmtz_cnn_step(dmtz_cnn *net, float lr);
 /* Timing of the network kernels on a W x H x D grid (CUDA events on the

@@ -2,8 +2,8 @@
 
 Restates, in numpy, what the GPU kernels compute: 3x3x3 zero-padded
 convolutions 16 -> 32 -> 32 -> 32 -> 16 (output channel 0 used), ReLU between
-layers, the tanh-MSE loss over active vertices and its parameter gradient.
-The arithmetic is float64; `bf16=True` rounds to bfloat16 (round to nearest
+layers, the weighted tanh-MSE loss and its parameter gradient.
+The arithmetic is float64; `emulate=True` rounds to bfloat16 (round to nearest
 even) exactly where the GPU stores bfloat16: weights, features, the three
 activations and the three data gradients and the loss gradient.  With that
 emulation the only difference left is the order of the fp32 accumulations
@@ -101,17 +101,18 @@ def forward(feat, params, emulate=True):
 
 
 def loss_and_grad(feat, params, target, active, emulate=True):
-    """Mean (tanh(o) - target)^2 over active vertices and its flat gradient."""
+    """Weighted mean sum w (tanh(o) - target)^2 / sum w (w = active, a 0/1 mask
+    or byte weights) and its flat gradient."""
     q = bf16 if emulate else (lambda a: np.asarray(a, np.float64))
     layers = split(params)
     o, acts = forward(feat, params, emulate)
     y = np.tanh(o)
-    act = np.asarray(active, bool)
-    cnt = max(int(act.sum()), 1)
+    w = np.asarray(active, np.float64)
+    cnt = w.sum() if w.sum() > 0 else 1.0
     e = y - target
-    loss = float((e[act] ** 2).sum() / act.sum()) if act.any() else 0.0
+    loss = float((w * e ** 2).sum() / w.sum()) if w.sum() > 0 else 0.0
     dz4 = np.zeros(o.shape + (16,))
-    dz4[..., 0] = np.where(act, 2.0 * e * (1.0 - y * y), 0.0)
+    dz4[..., 0] = 2.0 * w * e * (1.0 - y * y)
     dz = q(dz4)
     ins = [q(feat)] + acts
     grads = [None] * 4

@@ -73,8 +73,8 @@ def test_forward_matches_reference(net, dims):
     assert _rel(got, ref64) < 3e-2
 
 
-@pytest.mark.parametrize("dims", [(13, 11, 9), (16, 16, 8)])
-def test_backward_matches_reference(net, dims):
+@pytest.mark.parametrize("dims,weighted", [((13, 11, 9), False), ((16, 16, 8), False), ((13, 11, 9), True)])
+def test_backward_matches_reference(net, dims, weighted):
     W, H, D = dims
     V = W * H * D
     p = _params(3)
@@ -83,6 +83,8 @@ def test_backward_matches_reference(net, dims):
     rng = np.random.default_rng(5)
     target = rng.uniform(-0.9, 0.9, (D, H, W))
     active = rng.random((D, H, W)) < 0.3
+    if weighted:
+        active = active * rng.integers(1, 9, (D, H, W))
     out = torch.empty(V, dtype=torch.float32, device="cuda")
     tgt = torch.from_numpy(target.reshape(-1).astype(np.float32)).cuda()
     act = torch.from_numpy(active.reshape(-1).astype(np.uint8)).cuda()
