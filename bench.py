@@ -149,6 +149,23 @@ def cpu_sample(f, g, threads: int):
     return SAMPLE ** 3 / dt / 1e6, dt, st
 
 
+def max_over_ranks(values, dist=None, device="cpu"):
+    """Element-wise maximum of per-rank floats over the process group (the
+    slowest rank sets the job time); the values themselves without one."""
+    if dist is None:
+        return [float(x) for x in values]
+    import torch
+
+    t = torch.tensor([float(x) for x in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t]
+
+
+def job_value(world: int, voxels_per_rank: int, seconds: float) -> float:
+    """Whole-job Mvox/s: every rank corrects its own field of voxels_per_rank."""
+    return world * voxels_per_rank / seconds / 1e6
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
@@ -224,12 +241,8 @@ def run_ours(args, rank, world, local_rank):
     if dist:
         dist.barrier()
     clk = clocks.stop()
-    t_step = float(np.mean(dev_s))
-    if dist:
-        tt = torch.tensor([t_step, wall], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_step, wall = float(tt[0]), float(tt[1])
-    value = world * V / t_step / 1e6
+    t_step, wall = max_over_ranks([float(np.mean(dev_s)), wall], dist, "cuda")
+    value = job_value(world, V, t_step)
 
     # end to end through the public API from pinned host buffers
     f_pin = torch.from_numpy(f).pin_memory()
@@ -244,11 +257,7 @@ def run_ours(args, rank, world, local_rank):
         ctx.correct_ptr(f_pin.data_ptr(), g_pin.data_ptr(), dims, REL_EPS, FLAGS, on_device=False,
                         use_graph=args.graph)
         e2e_t.append(time.perf_counter() - t1)
-    e2e_step = float(np.mean(e2e_t))
-    if dist:
-        tt = torch.tensor([e2e_step], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_step = float(tt[0])
+    e2e_step = max_over_ranks([float(np.mean(e2e_t))], dist, "cuda")[0]
 
     # roofline of the dominant kernel group: the gradient sweep run every round
     ms = ctx.profile_sweep(f_dev.data_ptr(), g0_dev.data_ptr(), dims, reps=20, on_device=True)
@@ -273,7 +282,7 @@ def run_ours(args, rank, world, local_rank):
                            "within_bound": ok_bound, "wall_s_per_step": wall / args.steps,
                            "phase_ms": rep["phase_ms"]},
                 "time_to_match_s": t_step,
-                "e2e": {"value": world * V / e2e_step / 1e6, "unit": "Mvox/s", "seconds_per_step": e2e_step,
+                "e2e": {"value": job_value(world, V, e2e_step), "unit": "Mvox/s", "seconds_per_step": e2e_step,
                         "h2d_bytes_per_step": 2 * V * 8, "d2h_bytes_per_step": V * 8 + 4},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,

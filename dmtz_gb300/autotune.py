@@ -1,7 +1,7 @@
 """Autotuner front end: a JSON cache of sweep configurations.
 
 The library measures (`Context.autotune`): for each brick shape (8x4x4,
-16x4x2, 32x2x2 anchors) and 4/8/16/32 blocks per SM it times a full gradient
+16x4x2, 32x2x2 anchors) and 8/16/32/64 blocks per SM it times a full gradient
 sweep and keeps the fastest.  This module remembers the answer per
 (GPU name, grid size class, dtype) in a JSON file, so later runs on the same
 kind of input skip the measurement:

@@ -587,7 +587,7 @@ struct dmtz_ctx {
     uint8_t *changed = nullptr;
     int64_t launches = 0;  // kernels launched by the current call
     int tune_shape = 0;    // brick shape (DMTZ_SHAPES) chosen by dmtz_autotune
-    int tune_bps = 16;     // sweep blocks per SM
+    int tune_bps = 32;     // sweep blocks per SM
     std::vector<dmtz_ctx *> pool;  // worker contexts of dmtz_correct_batch
     uint8_t *mm = nullptr;         // mismatch bytes of the learned proposal's features
     i64 capMM = 0;
@@ -1579,9 +1579,9 @@ dmtz_status dmtz_autotune(dmtz_ctx *ctx, int W, int H, int D, const double *orig
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
-    static const int bps_opts[4] = {4, 8, 16, 32};
+    static const int bps_opts[4] = {8, 16, 32, 64};
     double best_t = 1e30;
-    int bs = 0, bb = 16;
+    int bs = 0, bb = 32;
     for (int sh = 0; sh < DMTZ_NSHAPES; sh++) {
         if (!shape_fits(g, sh)) continue;
         for (int bi = 0; bi < 4; bi++) {

@@ -32,6 +32,12 @@ struct Grid {
     i64 bxy, byz, bxz;  // first ids of yz-plane, xz-plane, interior triangles
     i64 doff[14];  // linear offset of each stencil direction
     i64 coff[8];   // linear offset of each cube corner
+    // 32-bit copies for grids of fewer than 2^31 vertices (small != 0): the
+    // interior fast path indexes with 32-bit integers there
+    int small;
+    int WHi;
+    int doff32[14];
+    int coff32[8];
 };
 
 static inline Grid make_grid(int W, int H, int D) {
@@ -55,6 +61,10 @@ static inline Grid make_grid(int W, int H, int D) {
                                     {-1, 0, 1}, {1, 0, -1}, {-1, 1, 1}, {1, -1, -1}};
     for (int i = 0; i < 14; i++) g.doff[i] = dirs[i][0] + dirs[i][1] * w + dirs[i][2] * w * h;
     for (int c8 = 0; c8 < 8; c8++) g.coff[c8] = (c8 & 1) + ((c8 >> 1) & 1) * w + ((c8 >> 2) & 1) * w * h;
+    g.small = g.V < (1LL << 31) ? 1 : 0;
+    g.WHi = g.small ? (int)g.WH : 0;
+    for (int i = 0; i < 14; i++) g.doff32[i] = g.small ? (int)g.doff[i] : 0;
+    for (int c8 = 0; c8 < 8; c8++) g.coff32[c8] = g.small ? (int)g.coff[c8] : 0;
     return g;
 }
 

@@ -2,6 +2,9 @@
 //
 // An anchor at 1 <= x,y,z <= dim-2 owns all 26 of its cells and every vertex
 // its passes look at (offsets -1..2) exists, so no bounds test is needed.
+// Vertex indices are 32-bit here (grids below 2^31 vertices, Grid::small):
+// half the integer work of 64-bit ids in the address and tie-break
+// arithmetic, which dominates these instruction-bound passes.
 // These versions unroll every loop over edge families, triangle slots and
 // cofaces at compile time: the topology tables become immediates and each
 // "is n below u" test is one shift of a 14-bit mask by a constant.  They
@@ -40,8 +43,12 @@ __host__ __device__ constexpr int tet_corner_index(int ts, int x, int y, int z) 
 
 // linear offset of a compile-time displacement
 template <int DX, int DY, int DZ>
-__device__ __forceinline__ i64 off(const Grid &g) {
-    return (i64)DX + (i64)DY * g.W + (i64)DZ * g.WH;
+__device__ __forceinline__ int off(const Grid &g) {
+    return DX + DY * g.W + DZ * g.WHi;
+}
+
+__device__ __forceinline__ bool key_less32(uint64_t ka, int a, uint64_t kb, int b) {
+    return ka < kb || (ka == kb && a < b);
 }
 
 template <int... Is, class F>
@@ -53,19 +60,19 @@ __device__ __forceinline__ void static_for(std::integer_sequence<int, Is...>, F 
 __device__ __forceinline__ bool bit(uint32_t m, int d) { return (m >> d) & 1u; }
 
 // ---------------------------------------------------------------- pass 1
-__device__ __forceinline__ void fast_vertex(const Grid &g, const FieldState &s, i64 v) {
+__device__ __forceinline__ void fast_vertex(const Grid &g, const FieldState &s, int v) {
     const uint64_t kv = okey(s.val[v]);
     uint64_t bk = DMTZ_KEY_DBL_MAX;
-    i64 bid = -1;
+    int bid = -1;
     int bdir = 15;
     uint32_t lm = 0;
 #pragma unroll
     for (int i = 0; i < 14; i++) {
-        const i64 nb = v + g.doff[i];
+        const int nb = v + g.doff32[i];
         const uint64_t kn = okey(s.val[nb]);
-        if (key_less(kn, nb, kv, v)) {
+        if (key_less32(kn, nb, kv, v)) {
             lm |= 1u << i;
-            if (key_less(kn, nb, bk, bid)) {
+            if (key_less32(kn, nb, bk, bid)) {
                 bk = kn;
                 bid = nb;
                 bdir = i;
@@ -80,17 +87,17 @@ __device__ __forceinline__ void fast_vertex(const Grid &g, const FieldState &s, 
 // ---------------------------------------------------------------- pass 2 / 4 (edges)
 // A2 = true: candidates below both endpoints (pass 2); false: between them (pass 4)
 template <int K, bool A2>
-__device__ __forceinline__ int fast_edge_choice(const Grid &g, const FieldState &s, i64 v, bool &claimed) {
+__device__ __forceinline__ int fast_edge_choice(const Grid &g, const FieldState &s, int v, bool &claimed) {
     constexpr int cp = cxt::TOPO_EDGE_V[K][0], cq = cxt::TOPO_EDGE_V[K][1];
     constexpr int dpq = cxt::TOPO_CORNER_DIR[cp][cq], dqp = cxt::TOPO_CORNER_DIR[cq][cp];
-    const i64 p = v + g.coff[cp], q = v + g.coff[cq];
+    const int p = v + g.coff32[cp], q = v + g.coff32[cq];
     const uint32_t lp = s.low[p], lq = s.low[q];
     const bool qb = bit(lp, dpq);  // q below p: p is the higher endpoint
     claimed = qb ? (s.pv[p] == dpq) : (s.pv[q] == dqp);
     if (claimed) return -1;
     const uint32_t lhi = qb ? lp : lq, llo = qb ? lq : lp;
     uint64_t bk = DMTZ_KEY_DBL_MAX;
-    i64 bid = INT_MAX;
+    int bid = INT_MAX;
     int bj = -1;
     DMTZ_FOR(cxt::TOPO_EDGE_NCOF[K], J, {
         constexpr int j = decltype(J)::value;
@@ -100,9 +107,9 @@ __device__ __forceinline__ int fast_edge_choice(const Grid &g, const FieldState 
         const int dlo = qb ? dq : dp, dhi = qb ? dp : dq;
         const bool ok = A2 ? bit(llo, dlo) : (bit(lhi, dhi) && !bit(llo, dlo));
         if (ok) {
-            const i64 nb = v + off<tx, ty, tz>(g);
+            const int nb = v + off<tx, ty, tz>(g);
             const uint64_t kn = s.key[nb];
-            if (key_less(kn, nb, bk, bid)) {
+            if (key_less32(kn, nb, bk, bid)) {
                 bk = kn;
                 bid = nb;
                 bj = j;
@@ -112,7 +119,7 @@ __device__ __forceinline__ int fast_edge_choice(const Grid &g, const FieldState 
     return bj;
 }
 
-__device__ __forceinline__ void fast_edge_a2(const Grid &g, const FieldState &s, i64 v) {
+__device__ __forceinline__ void fast_edge_a2(const Grid &g, const FieldState &s, int v) {
     uint32_t out = 0;
     DMTZ_FOR(7, K, {
         constexpr int k = decltype(K)::value;
@@ -125,13 +132,13 @@ __device__ __forceinline__ void fast_edge_a2(const Grid &g, const FieldState &s,
 
 // is the face (anchor offset, slot) paired after pass 3?
 template <int K, int J>
-__device__ __forceinline__ bool cof_face_paired3(const Grid &g, const FieldState &s, i64 v) {
+__device__ __forceinline__ bool cof_face_paired3(const Grid &g, const FieldState &s, int v) {
     constexpr int fx = cxt::TOPO_EDGE_COF[K][J][0], fy = cxt::TOPO_EDGE_COF[K][J][1],
                   fz = cxt::TOPO_EDGE_COF[K][J][2], fs = cxt::TOPO_EDGE_COF[K][J][3];
     return bit(s.fp3[v + off<fx, fy, fz>(g)], fs);
 }
 
-__device__ __forceinline__ void fast_edge_a4(const Grid &g, const FieldState &s, i64 v) {
+__device__ __forceinline__ void fast_edge_a4(const Grid &g, const FieldState &s, int v) {
     const uint32_t a2 = s.ea2[v];
     uint32_t out = a2;
     DMTZ_FOR(7, K, {
@@ -168,7 +175,7 @@ __device__ __forceinline__ void fast_tri_order(const FieldState &s, const uint32
 
 // does the edge of slot S opposite corner j point (through `arr`) to this triangle?
 template <int S>
-__device__ __forceinline__ bool edge_points_to_face(const Grid &g, const uint32_t *arr, i64 v, int j) {
+__device__ __forceinline__ bool edge_points_to_face(const Grid &g, const uint32_t *arr, int v, int j) {
     bool r = false;
     DMTZ_FOR(3, J, {
         constexpr int jj = decltype(J)::value;
@@ -183,13 +190,13 @@ __device__ __forceinline__ bool edge_points_to_face(const Grid &g, const uint32_
 // argmin over the triangle's cofaces of the fourth vertex, among those with
 // "below lo" (A3) or "below mid and above lo" (A5)
 template <int S, bool A3>
-__device__ __forceinline__ int fast_face_choice(const Grid &g, const FieldState &s, i64 v, const uint32_t l[3], int jlo,
+__device__ __forceinline__ int fast_face_choice(const Grid &g, const FieldState &s, int v, const uint32_t l[3], int jlo,
                                                 int jmid) {
     constexpr int c0 = cxt::TOPO_FACE_V[S][0], c1 = cxt::TOPO_FACE_V[S][1], c2 = cxt::TOPO_FACE_V[S][2];
     const uint32_t llo = jlo == 0 ? l[0] : (jlo == 1 ? l[1] : l[2]);
     const uint32_t lmid = jmid == 0 ? l[0] : (jmid == 1 ? l[1] : l[2]);
     uint64_t bk = DMTZ_KEY_DBL_MAX;
-    i64 bid = INT_MAX;
+    int bid = INT_MAX;
     int bj = -1;
     DMTZ_FOR(cxt::TOPO_FACE_NCOF[S], J, {
         constexpr int j = decltype(J)::value;
@@ -201,9 +208,9 @@ __device__ __forceinline__ int fast_face_choice(const Grid &g, const FieldState 
         const int dmid = jmid == 0 ? d0 : (jmid == 1 ? d1 : d2);
         const bool ok = A3 ? bit(llo, dlo) : (bit(lmid, dmid) && !bit(llo, dlo));
         if (ok) {
-            const i64 nb = v + off<nx, ny, nz>(g);
+            const int nb = v + off<nx, ny, nz>(g);
             const uint64_t kn = s.key[nb];
-            if (key_less(kn, nb, bk, bid)) {
+            if (key_less32(kn, nb, bk, bid)) {
                 bk = kn;
                 bid = nb;
                 bj = j;
@@ -214,14 +221,14 @@ __device__ __forceinline__ int fast_face_choice(const Grid &g, const FieldState 
 }
 
 template <int S>
-__device__ __forceinline__ void load_corner_lows(const Grid &g, const FieldState &s, i64 v, uint32_t l[3]) {
+__device__ __forceinline__ void load_corner_lows(const Grid &g, const FieldState &s, int v, uint32_t l[3]) {
     constexpr int c0 = cxt::TOPO_FACE_V[S][0], c1 = cxt::TOPO_FACE_V[S][1], c2 = cxt::TOPO_FACE_V[S][2];
     l[0] = s.low[v + off<cxt::ccx(c0), cxt::ccy(c0), cxt::ccz(c0)>(g)];
     l[1] = s.low[v + off<cxt::ccx(c1), cxt::ccy(c1), cxt::ccz(c1)>(g)];
     l[2] = s.low[v + off<cxt::ccx(c2), cxt::ccy(c2), cxt::ccz(c2)>(g)];
 }
 
-__device__ __forceinline__ void fast_face_a3(const Grid &g, const FieldState &s, i64 v) {
+__device__ __forceinline__ void fast_face_a3(const Grid &g, const FieldState &s, int v) {
     uint32_t out = 0, paired = 0;
     DMTZ_FOR(12, S, {
         constexpr int sl = decltype(S)::value;
@@ -246,7 +253,7 @@ __device__ __forceinline__ void fast_face_a3(const Grid &g, const FieldState &s,
 // was coface tet J of slot S claimed in pass 3?  Its claimer there is its
 // triangle opposite its lowest vertex, which is corner jlo of the triangle.
 template <int S, int J>
-__device__ __forceinline__ bool cof_tet_claimed3(const Grid &g, const FieldState &s, i64 v, int jlo) {
+__device__ __forceinline__ bool cof_tet_claimed3(const Grid &g, const FieldState &s, int v, int jlo) {
     constexpr int tx = cxt::TOPO_FACE_COF[S][J][0], ty = cxt::TOPO_FACE_COF[S][J][1], tz = cxt::TOPO_FACE_COF[S][J][2],
                   ts = cxt::TOPO_FACE_COF[S][J][3];
     bool r = false;
@@ -263,7 +270,7 @@ __device__ __forceinline__ bool cof_tet_claimed3(const Grid &g, const FieldState
     return r;
 }
 
-__device__ __forceinline__ void fast_face_a5(const Grid &g, const FieldState &s, i64 v) {
+__device__ __forceinline__ void fast_face_a5(const Grid &g, const FieldState &s, int v) {
     const uint32_t a3 = s.fa3[v];
     const uint32_t p3 = s.fp3[v];
     uint32_t out = a3;
@@ -293,15 +300,15 @@ __device__ __forceinline__ void fast_face_a5(const Grid &g, const FieldState &s,
 }
 
 // ---------------------------------------------------------------- criticality
-__device__ __forceinline__ void fast_crit(const Grid &g, const FieldState &s, i64 v) {
+__device__ __forceinline__ void fast_crit(const Grid &g, const FieldState &s, int v) {
     uint32_t m = s.pv[v] == 15 ? 1u : 0u;
     const uint32_t eu = s.eup[v], fu = s.fup[v];
     DMTZ_FOR(7, K, {
         constexpr int k = decltype(K)::value;
         constexpr int cp = cxt::TOPO_EDGE_V[k][0], cq = cxt::TOPO_EDGE_V[k][1];
         if (!eup_get(eu, k)) {
-            const bool vp = s.pv[v + g.coff[cp]] == cxt::TOPO_CORNER_DIR[cp][cq] ||
-                            s.pv[v + g.coff[cq]] == cxt::TOPO_CORNER_DIR[cq][cp];
+            const bool vp = s.pv[v + g.coff32[cp]] == cxt::TOPO_CORNER_DIR[cp][cq] ||
+                            s.pv[v + g.coff32[cq]] == cxt::TOPO_CORNER_DIR[cq][cp];
             if (!vp) m |= 1u << (1 + k);
         }
     });
@@ -334,8 +341,16 @@ __device__ __forceinline__ void fast_crit(const Grid &g, const FieldState &s, i6
 // ---------------------------------------------------------------- brick sweep
 enum { PASS_VERTEX = 0, PASS_E2, PASS_F3, PASS_E4, PASS_F5, PASS_CRIT };
 
+// minimum resident blocks per SM the sweep kernels are compiled for: 16
+// blocks of 128 threads fill an SM and cap the kernels at 32 registers.  The
+// passes are latency- and issue-bound; full occupancy beats the few spills
+// this causes (sweep 6.9 -> 5.9 ms at 256^3 on GB300).
+#ifndef DMTZ_SWEEP_MINB
+#define DMTZ_SWEEP_MINB 16
+#endif
+
 template <int PASS, int SX, int SY, int SZ>
-__global__ void __launch_bounds__(DMTZ_BRICK) k_sweep(Grid g, FieldState s, BrickList bl) {
+__global__ void __launch_bounds__(DMTZ_BRICK, DMTZ_SWEEP_MINB) k_sweep(Grid g, FieldState s, BrickList bl) {
     static_assert(SX * SY * SZ == DMTZ_BRICK, "a brick is one block");
     const i64 nb = brick_count(bl);
     const int lx = threadIdx.x % SX, ly = (threadIdx.x / SX) % SY, lz = threadIdx.x / (SX * SY);
@@ -345,25 +360,27 @@ __global__ void __launch_bounds__(DMTZ_BRICK) k_sweep(Grid g, FieldState s, Bric
         const int x = bx * SX + lx, y = by * SY + ly, z = bz * SZ + lz;
         if (x >= g.W || y >= g.H || z >= g.D) continue;
         const i64 v = x + (i64)y * g.W + (i64)z * g.WH;
-        const bool interior = x >= 1 && y >= 1 && z >= 1 && x <= g.W - 2 && y <= g.H - 2 && z <= g.D - 2;
+        const bool interior =
+            g.small && x >= 1 && y >= 1 && z >= 1 && x <= g.W - 2 && y <= g.H - 2 && z <= g.D - 2;
+        const int v32 = (int)v;  // used only when g.small
         if (PASS == PASS_VERTEX) {
-            if (interior) fast_vertex(g, s, v);
+            if (interior) fast_vertex(g, s, v32);
             else pass_vertex_at(g, s, v, x, y, z);
         } else if (PASS == PASS_E2) {
-            if (interior) fast_edge_a2(g, s, v);
+            if (interior) fast_edge_a2(g, s, v32);
             else pass_edge_a2_at(g, s, v, x, y, z);
         } else if (PASS == PASS_F3) {
-            if (interior) fast_face_a3(g, s, v);
+            if (interior) fast_face_a3(g, s, v32);
             else pass_face_a3_at(g, s, v, x, y, z);
         } else if (PASS == PASS_E4) {
-            if (interior) fast_edge_a4(g, s, v);
+            if (interior) fast_edge_a4(g, s, v32);
             else pass_edge_a4_at(g, s, v, x, y, z);
         } else if (PASS == PASS_F5) {
-            if (interior) fast_face_a5(g, s, v);
+            if (interior) fast_face_a5(g, s, v32);
             else pass_face_a5_at(g, s, v, x, y, z);
         } else {
             if (interior) {
-                fast_crit(g, s, v);
+                fast_crit(g, s, v32);
             } else {
                 uint32_t tc;
                 s.crit[v] = crit_mask(g, s, v, x, y, z, &tc);

@@ -172,7 +172,7 @@ dmtz_status dmtz_correct_batch(dmtz_ctx *ctx, int n, const dmtz_instance *inst, 
 
 /* Brick shape (0: 8x4x4, 1: 16x4x2, 2: 32x2x2 anchors) and blocks per SM of
  * the gradient sweeps.  Results do not depend on them, only speed.
- * dmtz_autotune times a full sweep of `decp` for every shape and 4, 8, 16, 32
+ * dmtz_autotune times a full sweep of `decp` for every shape and 8, 16, 32, 64
  * blocks per SM, keeps the fastest in the context and returns it in best[2]. */
 dmtz_status dmtz_set_tuning(dmtz_ctx *ctx, int shape, int blocks_per_sm);
 /* name of the context's device (for keying tuning caches) */

@@ -45,7 +45,7 @@ def test_tuning_does_not_change_results(gpu_ctx):
                 out, _ = gpu_ctx.correct(f, g, 1e-3, dims=dims)
                 assert np.array_equal(out, base), (shape, bps)
         shape, bps, ms = gpu_ctx.autotune(f, g, dims)
-        assert 0 <= shape < 3 and bps in (4, 8, 16, 32) and ms > 0
+        assert 0 <= shape < 3 and bps in (8, 16, 32, 64) and ms > 0
         out, _ = gpu_ctx.correct(f, g, 1e-3, dims=dims)
         assert np.array_equal(out, base)
     finally:
