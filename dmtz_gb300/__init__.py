@@ -95,6 +95,8 @@ def load_library(build_if_missing: bool = True):
     L.dmtz_get_tuning.argtypes = [_vp, ctypes.POINTER(_int), ctypes.POINTER(_int)]
     L.dmtz_autotune.argtypes = [_vp, _int, _int, _int, _vp, _vp, _int, ctypes.POINTER(_int), ctypes.POINTER(ctypes.c_double)]
     L.dmtz_device_name.argtypes = [_vp, ctypes.c_char_p, _int]
+    L.dmtz_set_list_reserve.argtypes = [_vp, ctypes.c_double, ctypes.c_int64]
+    L.dmtz_set_list_reserve.restype = _int
     # learned proposal
     L.dmtz_cnn_num_params.argtypes = []
     L.dmtz_cnn_num_params.restype = ctypes.c_int64
@@ -284,6 +286,11 @@ class Context:
 
     def set_tuning(self, shape, blocks_per_sm):
         self._check(self._L.dmtz_set_tuning(self._h, int(shape), int(blocks_per_sm)))
+
+    def set_list_reserve(self, fraction=1.0 / 16, min_entries=1 << 20):
+        """Initial room of the mismatch lists (fraction of cells, at least
+        min_entries); they grow on demand, results do not depend on it."""
+        self._check(self._L.dmtz_set_list_reserve(self._h, float(fraction), int(min_entries)))
 
     def get_tuning(self):
         a, b = _int(), _int()

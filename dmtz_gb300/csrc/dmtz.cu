@@ -41,11 +41,13 @@ static inline unsigned grid_for(i64 n) { return (unsigned)std::max<i64>(1, (n + 
 struct Lists {
     i64 *l[4];                  // min, 1-saddle, 2-saddle, max (reference cell ids)
     unsigned long long *n;      // 4 counters
+    i64 cap[4];                 // capacities; a counter above its capacity = overflow,
+                                // the host grows the list and scans again
 };
 
 __device__ __forceinline__ void push_list(const Lists &L, int k, i64 id) {
     const unsigned long long at = atomicAdd(&L.n[k], 1ull);
-    L.l[k][at] = id;
+    if ((i64)at < L.cap[k]) L.l[k][at] = id;
 }
 
 // mismatch between the decompressed and the original critical cells
@@ -160,12 +162,15 @@ __global__ void k_export(Grid g, FieldState s, int32_t *PV, int32_t *PE, int32_t
 struct CpLists {
     const i64 *l[4];
     const unsigned long long *n;
+    i64 cap[4];
 };
 
 // fix_minimum, [fix_saddle, fix_2saddle], fix_maximum over the current lists
+// (the host never runs this on an overflowed list; the clamp only keeps
+// every read inside the allocation)
 __global__ void k_fix_cp(RuleCtx c, CpLists L, int preserve_saddles) {
-    const i64 n0 = (i64)L.n[0], n1 = preserve_saddles ? (i64)L.n[1] : 0, n2 = preserve_saddles ? (i64)L.n[2] : 0,
-              n3 = (i64)L.n[3];
+    const i64 n0 = min((i64)L.n[0], L.cap[0]), n1 = preserve_saddles ? min((i64)L.n[1], L.cap[1]) : 0,
+              n2 = preserve_saddles ? min((i64)L.n[2], L.cap[2]) : 0, n3 = min((i64)L.n[3], L.cap[3]);
     const i64 total = n0 + n1 + n2 + n3;
     for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (i64)gridDim.x * blockDim.x) {
         if (i < n0) rule_min(c, L.l[0][i]);
@@ -179,6 +184,7 @@ __global__ void k_fix_cp(RuleCtx c, CpLists L, int preserve_saddles) {
 struct PathRec {
     i64 *as_tet, *as_cur, *ds_edge, *ds_vert;
     unsigned long long *n;  // [0] ascending, [1] descending
+    i64 cap_as, cap_ds;     // at most one record per original 2-saddle / 1-saddle
 };
 
 // Original ascending paths (is_false, main_3d.cu:4437-4497) step from a
@@ -213,14 +219,33 @@ __global__ void k_path_succ(Grid g, const uint32_t *tcodeP, uint8_t *succ) {
 }
 
 // compact list of the original 2-saddle triangles (anchor * 12 + slot)
-__global__ void k_sad2_list(Grid g, const uint32_t *critP, i64 *list, unsigned long long *n) {
+__global__ void k_sad2_list(Grid g, const uint32_t *critP, i64 *list, i64 cap, unsigned long long *n) {
     i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= g.V) return;
     uint32_t m = (critP[v] >> 8) & 0xFFFu;
     while (m) {
         const int sl = __ffs(m) - 1;
         m &= m - 1;
-        list[atomicAdd(n, 1ull)] = v * 12 + sl;
+        const unsigned long long at = atomicAdd(n, 1ull);
+        if ((i64)at < cap) list[at] = v * 12 + sl;
+    }
+}
+
+// numbers of original 1-saddle edges (out[0]) and 2-saddle triangles (out[1])
+__global__ void k_count_saddles(i64 V, const uint32_t *critP, unsigned long long *out) {
+    unsigned long long a = 0, b = 0;
+    for (i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (i64)gridDim.x * blockDim.x) {
+        const uint32_t m = critP[v];
+        a += __popc((m >> 1) & 0x7Fu);
+        b += __popc((m >> 8) & 0xFFFu);
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, off);
+        b += __shfl_down_sync(0xffffffffu, b, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (a) atomicAdd(&out[0], a);
+        if (b) atomicAdd(&out[1], b);
     }
 }
 
@@ -250,8 +275,10 @@ __global__ void k_path_as(Grid g, const i64 *sad2, const unsigned long long *nsa
                 if (p == 7) break;  // an original maximum ends the path
                 if (p != (int)((tcQ[ci] >> (3 * cs)) & 7)) {
                     const unsigned long long at = atomicAdd(&R.n[0], 1ull);
-                    R.as_tet[at] = tet_ref(g, sx, sy, sz, ss);
-                    R.as_cur[at] = tet_ref(g, cx, cy, cz, cs);
+                    if ((i64)at < R.cap_as) {
+                        R.as_tet[at] = tet_ref(g, sx, sy, sz, ss);
+                        R.as_cur[at] = tet_ref(g, cx, cy, cz, cs);
+                    }
                     found = true;
                     break;
                 }
@@ -292,8 +319,10 @@ __global__ void k_path_ds(RuleCtx c, PathRec R) {
                 if (po == 15) continue;
                 if (po != c.Q.pv[e]) {
                     const unsigned long long at = atomicAdd(&R.n[1], 1ull);
-                    R.ds_edge[at] = edge_ref(g, x, y, z, k);
-                    R.ds_vert[at] = e;
+                    if ((i64)at < R.cap_ds) {
+                        R.ds_edge[at] = edge_ref(g, x, y, z, k);
+                        R.ds_vert[at] = e;
+                    }
                     break;
                 }
             }
@@ -302,7 +331,7 @@ __global__ void k_path_ds(RuleCtx c, PathRec R) {
 }
 
 __global__ void k_fix_path(RuleCtx c, PathRec R) {
-    const i64 na = (i64)R.n[0], nd = (i64)R.n[1];
+    const i64 na = min((i64)R.n[0], R.cap_as), nd = min((i64)R.n[1], R.cap_ds);
     for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < na + nd; i += (i64)gridDim.x * blockDim.x) {
         if (i < na) rule_as_path(c, R.as_cur[i]);
         else rule_ds_path(c, R.ds_vert[i - na]);
@@ -574,8 +603,17 @@ struct dmtz_ctx {
     int *cnt = nullptr;
     uint32_t *reqbits = nullptr;
     i64 *reqlist = nullptr;
+    // Mismatch lists and separatrix records.  Sized for the counts that occur,
+    // not for every cell: the mismatch lists start at list_frac x cells (at
+    // least list_min entries, at most all cells) and grow when a scan
+    // overflows them; the path records and the 2-saddle list are sized from
+    // the original gradient's saddle counts, which bound them.
     i64 *lists[4] = {nullptr, nullptr, nullptr, nullptr};
+    i64 capL[4] = {0, 0, 0, 0};
+    double list_frac = 1.0 / 16;
+    i64 list_min = 1 << 20;
     i64 *as_tet = nullptr, *as_cur = nullptr, *ds_edge = nullptr, *ds_vert = nullptr;
+    i64 capAS = 0, capDS = 0, capSad2 = 0;
     uint8_t *succ = nullptr;  // original ascending-path successor of each tetrahedron
     uint8_t *brick_flags = nullptr;   // bricks to re-pair in the next sweep
     uint32_t *brick_list = nullptr;   // their compacted list (counters[11])
@@ -619,6 +657,8 @@ void free_all(dmtz_ctx *c) {
     cudaFree(c->f); cudaFree(c->g); free_field(c->P); free_field(c->Q);
     cudaFree(c->cnt); cudaFree(c->reqbits); cudaFree(c->reqlist);
     for (auto &l : c->lists) { cudaFree(l); l = nullptr; }
+    for (auto &k : c->capL) k = 0;
+    c->capAS = c->capDS = c->capSad2 = 0;
     cudaFree(c->as_tet); cudaFree(c->as_cur); cudaFree(c->ds_edge); cudaFree(c->ds_vert);
     cudaFree(c->counters); cudaFree(c->errword); cudaFree(c->changed);
     cudaFree(c->succ); cudaFree(c->sad2); cudaFree(c->brick_flags); cudaFree(c->brick_list);
@@ -638,11 +678,29 @@ dmtz_status alloc_field(dmtz_ctx *ctx, DevField &d, i64 V) {
 
 i64 bricks_of(const Grid &g, int shape, int &nbx, int &nby, int &nbz);
 
+// capacity a mismatch list of a dimension with `cells` cells starts with
+i64 lean_cap(const dmtz_ctx *ctx, i64 cells) {
+    const i64 want = std::max<i64>(ctx->list_min, (i64)((double)cells * ctx->list_frac));
+    return std::max<i64>(1, std::min<i64>(cells, want));
+}
+
+dmtz_status ensure_lists(dmtz_ctx *ctx, const Grid &g) {
+    const i64 cells[4] = {g.V, g.E, g.F, g.T};
+    for (int k = 0; k < 4; k++) {
+        if (ctx->lists[k]) continue;
+        const i64 cap = lean_cap(ctx, cells[k]);
+        CK(dalloc(&ctx->lists[k], cap));
+        ctx->capL[k] = cap;
+    }
+    return DMTZ_OK;
+}
+
 dmtz_status ensure(dmtz_ctx *ctx, const Grid &g) {
     int nbx, nby, nbz;
     i64 nbr = 0;
     for (int sh = 0; sh < DMTZ_NSHAPES; sh++) nbr = std::max(nbr, bricks_of(g, sh, nbx, nby, nbz));
-    if (g.V <= ctx->capV && g.E <= ctx->capE && g.F <= ctx->capF && g.T <= ctx->capT && nbr <= ctx->capB) return DMTZ_OK;
+    if (g.V <= ctx->capV && g.E <= ctx->capE && g.F <= ctx->capF && g.T <= ctx->capT && nbr <= ctx->capB)
+        return ensure_lists(ctx, g);
     free_all(ctx);
     const i64 V = g.V;
     CK(dalloc(&ctx->f, V)); CK(dalloc(&ctx->g, V));
@@ -653,16 +711,25 @@ dmtz_status ensure(dmtz_ctx *ctx, const Grid &g) {
     CK(dalloc(&ctx->reqbits, (V + 31) / 32 + 1));
     CK(cudaMemset(ctx->reqbits, 0, sizeof(uint32_t) * (size_t)((V + 31) / 32 + 1)));
     CK(dalloc(&ctx->reqlist, V));
-    CK(dalloc(&ctx->lists[0], g.V)); CK(dalloc(&ctx->lists[1], g.E));
-    CK(dalloc(&ctx->lists[2], g.F)); CK(dalloc(&ctx->lists[3], g.T));
-    CK(dalloc(&ctx->as_tet, g.F)); CK(dalloc(&ctx->as_cur, g.F));
-    CK(dalloc(&ctx->ds_edge, g.E)); CK(dalloc(&ctx->ds_vert, g.E));
-    CK(dalloc(&ctx->succ, 6 * V)); CK(dalloc(&ctx->sad2, g.F));
+    CK(dalloc(&ctx->succ, 6 * V));
     CK(dalloc(&ctx->brick_flags, nbr)); CK(dalloc(&ctx->brick_list, nbr));
     CK(cudaMemset(ctx->brick_flags, 0, (size_t)nbr));
     ctx->capB = nbr;
     CK(dalloc(&ctx->counters, 16)); CK(dalloc(&ctx->errword, 1)); CK(dalloc(&ctx->changed, V));
     ctx->capV = g.V; ctx->capE = g.E; ctx->capF = g.F; ctx->capT = g.T;
+    return ensure_lists(ctx, g);
+}
+
+// grow mismatch list k to hold `need` entries; its contents are lost, so the
+// caller scans again
+dmtz_status grow_list(dmtz_ctx *ctx, const Grid &g, int k, i64 need) {
+    const i64 cells[4] = {g.V, g.E, g.F, g.T};
+    const i64 cap = std::max<i64>(need, std::min<i64>(cells[k], std::max<i64>(need + need / 2, 2 * ctx->capL[k])));
+    cudaFree(ctx->lists[k]);
+    ctx->lists[k] = nullptr;
+    ctx->capL[k] = 0;
+    CK(dalloc(&ctx->lists[k], cap));
+    ctx->capL[k] = cap;
     return DMTZ_OK;
 }
 
@@ -719,7 +786,10 @@ BrickList all_bricks(const Grid &g, int shape, i64 &nb) {
 // mismatch lists of the decompressed gradient against crit_o
 void scan_mismatch(dmtz_ctx *ctx, const Grid &g, const uint32_t *crit_d, const uint32_t *crit_o, int want_saddles) {
     Lists L;
-    for (int k = 0; k < 4; k++) L.l[k] = ctx->lists[k];
+    for (int k = 0; k < 4; k++) {
+        L.l[k] = ctx->lists[k];
+        L.cap[k] = ctx->capL[k];
+    }
     L.n = ctx->counters;
     cudaMemsetAsync(ctx->counters, 0, 4 * sizeof(unsigned long long), ctx->stream);
     k_mismatch_scan<<<persistent_grid(), kBlock, 0, ctx->stream>>>(g, crit_d, crit_o, L, want_saddles);
@@ -795,12 +865,84 @@ RuleCtx rule_ctx(dmtz_ctx *ctx, const Grid &g, double bound, int edit_type) {
     return c;
 }
 
-// static data of the original ascending paths (after the original pairing)
-void prep_paths(dmtz_ctx *ctx, const Grid &g) {
-    cudaMemsetAsync(ctx->counters + 10, 0, sizeof(unsigned long long), ctx->stream);
-    k_path_succ<<<grid_for(g.V), kBlock, 0, ctx->stream>>>(g, ctx->P.tcode, ctx->succ);
-    k_sad2_list<<<grid_for(g.V), kBlock, 0, ctx->stream>>>(g, ctx->P.crit, ctx->sad2, ctx->counters + 10);
-    ctx->launches += 2;
+// After a scan that left its counts in hc[0..3]: grow every overflowed list
+// and scan again (same masks, so the same counts, which now fit).
+dmtz_status fit_lists(dmtz_ctx *ctx, const Grid &g, int want_saddles, unsigned long long *hc) {
+    bool over = false;
+    for (int k = 0; k < 4; k++) {
+        if ((i64)hc[k] <= ctx->capL[k]) continue;
+        dmtz_status s = grow_list(ctx, g, k, (i64)hc[k]);
+        if (s != DMTZ_OK) return s;
+        over = true;
+    }
+    if (!over) return DMTZ_OK;
+    scan_mismatch(ctx, g, ctx->Q.crit, ctx->P.crit, want_saddles);
+    CK(cudaMemcpyAsync(hc, ctx->counters, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return DMTZ_OK;
+}
+
+CpLists cp_lists(const dmtz_ctx *ctx) {
+    CpLists L;
+    for (int k = 0; k < 4; k++) {
+        L.l[k] = ctx->lists[k];
+        L.cap[k] = ctx->capL[k];
+    }
+    L.n = ctx->counters;
+    return L;
+}
+
+PathRec path_rec(const dmtz_ctx *ctx) {
+    return PathRec{ctx->as_tet, ctx->as_cur, ctx->ds_edge, ctx->ds_vert, ctx->counters + 5, ctx->capAS, ctx->capDS};
+}
+
+// static data of the original ascending paths (after the original pairing),
+// and record buffers sized by the original saddle counts (each original
+// 2-saddle gives at most one ascending record, each 1-saddle at most one
+// descending record)
+dmtz_status prep_paths(dmtz_ctx *ctx, const Grid &g) {
+    cudaStream_t st = ctx->stream;
+    CK(cudaMemsetAsync(ctx->counters + 13, 0, 2 * sizeof(unsigned long long), st));
+    k_count_saddles<<<persistent_grid(), kBlock, 0, st>>>(g.V, ctx->P.crit, ctx->counters + 13);
+    unsigned long long n[2] = {0, 0};
+    CK(cudaMemcpyAsync(n, ctx->counters + 13, sizeof(n), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if ((i64)n[0] > ctx->capDS) {
+        cudaFree(ctx->ds_edge);
+        cudaFree(ctx->ds_vert);
+        ctx->ds_edge = ctx->ds_vert = nullptr;
+        ctx->capDS = 0;
+        CK(dalloc(&ctx->ds_edge, (i64)n[0]));
+        CK(dalloc(&ctx->ds_vert, (i64)n[0]));
+        ctx->capDS = (i64)n[0];
+    }
+    if ((i64)n[1] > ctx->capAS) {
+        cudaFree(ctx->as_tet);
+        cudaFree(ctx->as_cur);
+        cudaFree(ctx->sad2);
+        ctx->as_tet = ctx->as_cur = ctx->sad2 = nullptr;
+        ctx->capAS = ctx->capSad2 = 0;
+        CK(dalloc(&ctx->as_tet, (i64)n[1]));
+        CK(dalloc(&ctx->as_cur, (i64)n[1]));
+        CK(dalloc(&ctx->sad2, (i64)n[1]));
+        ctx->capAS = ctx->capSad2 = (i64)n[1];
+    }
+    // buffers exist even when a count is 0 (kernels take their addresses)
+    if (!ctx->ds_edge) {
+        CK(dalloc(&ctx->ds_edge, 1));
+        CK(dalloc(&ctx->ds_vert, 1));
+    }
+    if (!ctx->as_tet) {
+        CK(dalloc(&ctx->as_tet, 1));
+        CK(dalloc(&ctx->as_cur, 1));
+        CK(dalloc(&ctx->sad2, 1));
+    }
+    CK(cudaMemsetAsync(ctx->counters + 10, 0, sizeof(unsigned long long), st));
+    k_path_succ<<<grid_for(g.V), kBlock, 0, st>>>(g, ctx->P.tcode, ctx->succ);
+    k_sad2_list<<<grid_for(g.V), kBlock, 0, st>>>(g, ctx->P.crit, ctx->sad2, ctx->capSad2, ctx->counters + 10);
+    ctx->launches += 3;
+    CK(cudaGetLastError());
+    return DMTZ_OK;
 }
 
 // separatrix detection (ascending and descending) into the path records
@@ -916,7 +1058,10 @@ static dmtz_status setup_pair(dmtz_ctx *ctx, const Grid &g, const double *orig, 
     run_pairing(ctx, g, view(ctx->P, ctx->f), nullptr, 1);
     run_pairing(ctx, g, view(ctx->Q, ctx->g), ctx->P.crit, 1);
     CK(cudaGetLastError());
-    return DMTZ_OK;
+    unsigned long long hc[4];
+    CK(cudaMemcpyAsync(hc, ctx->counters, sizeof(hc), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return fit_lists(ctx, g, 1, hc);
 }
 
 dmtz_status dmtz_mismatch(dmtz_ctx *ctx, int W, int H, int D, const double *orig, const double *decp,
@@ -964,10 +1109,7 @@ dmtz_status dmtz_fix_round(dmtz_ctx *ctx, int W, int H, int D, const double *ori
     CK(cudaMemsetAsync(ctx->counters + 4, 0, sizeof(unsigned long long), ctx->stream));
     CK(cudaMemsetAsync(ctx->errword, 0, sizeof(int), ctx->stream));
     RuleCtx rc = rule_ctx(ctx, g, bound, edit_type);
-    CpLists L;
-    for (int k = 0; k < 4; k++) L.l[k] = ctx->lists[k];
-    L.n = ctx->counters;
-    k_fix_cp<<<persistent_grid(), kBlock, 0, ctx->stream>>>(rc, L, preserve_saddles);
+    k_fix_cp<<<persistent_grid(), kBlock, 0, ctx->stream>>>(rc, cp_lists(ctx), preserve_saddles);
     double *dd = nullptr;
     CK(dalloc(&dd, g.V));
     const double sentinel = -2000.0 * range;
@@ -995,9 +1137,8 @@ dmtz_status dmtz_path_detect(dmtz_ctx *ctx, int W, int H, int D, const double *o
     if ((s = setup_pair(ctx, g, orig, decp)) != DMTZ_OK) return s;
     CK(cudaMemsetAsync(ctx->errword, 0, sizeof(int), ctx->stream));
     RuleCtx rc = rule_ctx(ctx, g, 0.0, 0);
-    PathRec R{ctx->as_tet, ctx->as_cur, ctx->ds_edge, ctx->ds_vert, ctx->counters + 5};
-    prep_paths(ctx, g);
-    detect_paths(ctx, g, rc, R, persistent_grid());
+    if ((s = prep_paths(ctx, g)) != DMTZ_OK) return s;
+    detect_paths(ctx, g, rc, path_rec(ctx), persistent_grid());
     unsigned long long hc[2];
     CK(cudaMemcpyAsync(hc, ctx->counters + 5, sizeof(hc), cudaMemcpyDeviceToHost, ctx->stream));
     int err = 0;
@@ -1045,6 +1186,9 @@ struct LoopCtl {
     long long cc[4];
     long long n_as, n_ds;
     long long runs[4];  // body executions per state
+    long long cap[4];   // mismatch list capacities
+    int overflow;       // a scan overflowed a list: stop, grow, scan again, resume at `state`
+    int last;           // state of the last body run
 };
 }  // namespace
 
@@ -1088,9 +1232,13 @@ __global__ void k_loop_ctl(LoopCtl *ctl, const unsigned long long *counters, cud
         c.converged = 0;
         next = LS_DONE;
     }
+    c.last = st;
+    if (next != LS_DONE && st != LS_PCHECK)
+        for (int k = 0; k < 4; k++)
+            if (c.cc[k] > c.cap[k]) c.overflow = 1;
     c.state = next;
     *ctl = c;
-    cudaGraphSetConditional(hwhile, next != LS_DONE ? 1u : 0u);
+    cudaGraphSetConditional(hwhile, (next != LS_DONE && !c.overflow) ? 1u : 0u);
 }
 
 // ----------------------------------------------------------------------------- phase timers
@@ -1305,7 +1453,7 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
     CK(cudaMemsetAsync(ctx->counters, 0, 8 * sizeof(unsigned long long), st));
     const FieldState Ps = view(ctx->P, ctx->f), Qs = view(ctx->Q, ctx->g);
     run_pairing(ctx, g, Ps, nullptr, 1);
-    if (pvp == 1) prep_paths(ctx, g);
+    if (pvp == 1 && (s = prep_paths(ctx, g)) != DMTZ_OK) return s;
     if (filt == 1) {
         k_filter<<<grid_for(g.V), kBlock, 0, st>>>(g, ctx->P.crit, ctx->f, ctx->g, bound);
         ctx->launches++;
@@ -1320,7 +1468,12 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
         CK(cudaStreamSynchronize(st));
         return DMTZ_OK;
     };
-    if ((s = read_counts()) != DMTZ_OK) return s;
+    // counts after a mismatch scan; lists that overflowed grow and are rebuilt
+    auto read_fit = [&](int want_saddles) -> dmtz_status {
+        dmtz_status q = read_counts();
+        return q != DMTZ_OK ? q : fit_lists(ctx, g, want_saddles, hc);
+    };
+    if ((s = read_fit(1)) != DMTZ_OK) return s;
     dmtz_report R;
     memset(&R, 0, sizeof(R));
     for (int k = 0; k < 4; k++) R.initial_mismatch[k] = (int64_t)hc[k];
@@ -1328,7 +1481,7 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
         pt_.begin(PH_SETUP);
         if ((s = learned_start(ctx, net, g, bound)) != DMTZ_OK) return s;
         pt_.end();
-        if ((s = read_counts()) != DMTZ_OK) return s;
+        if ((s = read_fit(1)) != DMTZ_OK) return s;
     }
     i64 cc[4] = {(i64)hc[0], (i64)hc[1], (i64)hc[2], (i64)hc[3]};
     i64 n_as = 1, n_ds = 1, n_wall = 1;
@@ -1336,10 +1489,7 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
     int converged = 1;
     const unsigned pgrid = persistent_grid();
     RuleCtx rc = rule_ctx(ctx, g, bound, et);
-    CpLists L;
-    for (int k = 0; k < 4; k++) L.l[k] = ctx->lists[k];
-    L.n = ctx->counters;
-    PathRec PR{ctx->as_tet, ctx->as_cur, ctx->ds_edge, ctx->ds_vert, ctx->counters + 5};
+    const PathRec PR = path_rec(ctx);
     auto cp_any = [&]() { return cc[0] > 0 || cc[1] > 0 || cc[2] > 0 || cc[3] > 0; };
     if (opts->use_graph) {
         // same loop, decided on the device (see run_graph_loop)
@@ -1354,7 +1504,19 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
         LoopCtl fin = c;
         if (c.state != LS_DONE) {
             pt_.begin(PH_PAIR);
-            if ((s = run_graph_loop(ctx, g, rc, L, PR, Qs, range, ps, pt, c, &fin)) != DMTZ_OK) return s;
+            LoopCtl cur = c;
+            while (true) {
+                for (int k = 0; k < 4; k++) cur.cap[k] = ctx->capL[k];
+                if ((s = run_graph_loop(ctx, g, rc, cp_lists(ctx), PR, Qs, range, ps, pt, cur, &fin)) != DMTZ_OK)
+                    return s;
+                if (!fin.overflow) break;
+                // a scan outgrew a list: grow it, rebuild the lists and resume
+                unsigned long long h4[4];
+                for (int k = 0; k < 4; k++) h4[k] = (unsigned long long)fin.cc[k];
+                if ((s = fit_lists(ctx, g, fin.last == LS_CP ? (ps == 1) : 1, h4)) != DMTZ_OK) return s;
+                cur = fin;
+                cur.overflow = 0;
+            }
             pt_.end();
             // kernels per body run: switch + control, plus each state's own
             ctx->launches += 2 * (fin.runs[0] + fin.runs[1] + fin.runs[2] + fin.runs[3]) + 11 * fin.runs[LS_CP] +
@@ -1369,6 +1531,8 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
         n_wall = 0;
         converged = fin.converged;
     }
+    // separatrix records of the last re-check, still valid while no round ran since
+    bool paths_fresh = false;
     while (!opts->use_graph && (n_as > 0 || n_ds > 0 || n_wall > 0 || cp_any())) {
         if (rounds >= max_rounds) {
             converged = 0;
@@ -1379,9 +1543,10 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
             if (rounds >= max_rounds) break;
             rounds++;
             R.cp_rounds++;
+            paths_fresh = false;
             CK(cudaMemsetAsync(ctx->counters + 4, 0, sizeof(unsigned long long), st));
             pt_.begin(PH_FIXCP);
-            k_fix_cp<<<pgrid, kBlock, 0, st>>>(rc, L, ps);
+            k_fix_cp<<<pgrid, kBlock, 0, st>>>(rc, cp_lists(ctx), ps);
             pt_.end();
             pt_.begin(PH_APPLY);
             k_apply<<<pgrid, kBlock, 0, st>>>(rc, range, pt, 1, ctx->changed, nullptr);
@@ -1390,7 +1555,7 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
             pt_.begin(PH_PAIR);
             repair_dirty(ctx, g, Qs, ctx->P.crit, ps == 1);
             pt_.end();
-            if ((s = read_counts()) != DMTZ_OK) return s;
+            if ((s = read_fit(ps == 1)) != DMTZ_OK) return s;
             for (int k = 0; k < 4; k++) cc[k] = (i64)hc[k];
         }
         if (rounds >= max_rounds) {
@@ -1401,9 +1566,12 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
         // separatrix phase (main_3d.cu:6943-7148)
         rounds++;
         R.path_rounds++;
-        pt_.begin(PH_PATH);
-        detect_paths(ctx, g, rc, PR, pgrid);
-        pt_.end();
+        if (!paths_fresh) {  // else the last re-check ran on this same state
+            pt_.begin(PH_PATH);
+            detect_paths(ctx, g, rc, PR, pgrid);
+            pt_.end();
+        }
+        paths_fresh = false;
         CK(cudaMemsetAsync(ctx->counters + 4, 0, sizeof(unsigned long long), st));
         pt_.begin(PH_FIXPATH);
         k_fix_path<<<pgrid, kBlock, 0, st>>>(rc, PR);
@@ -1415,7 +1583,7 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
         pt_.begin(PH_PAIR);
         repair_dirty(ctx, g, Qs, ctx->P.crit, 1);
         pt_.end();
-        if ((s = read_counts()) != DMTZ_OK) return s;
+        if ((s = read_fit(1)) != DMTZ_OK) return s;
         for (int k = 0; k < 4; k++) cc[k] = (i64)hc[k];
         n_as = n_ds = n_wall = 0;
         if (!cp_any()) {
@@ -1425,6 +1593,7 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
             if ((s = read_counts()) != DMTZ_OK) return s;
             n_as = (i64)hc[5];
             n_ds = (i64)hc[6];
+            paths_fresh = true;
         }
     }
     CK(cudaEventRecord(e1, st));
@@ -1557,6 +1726,19 @@ dmtz_status dmtz_set_tuning(dmtz_ctx *ctx, int shape, int blocks_per_sm) {
     return DMTZ_OK;
 }
 
+dmtz_status dmtz_set_list_reserve(dmtz_ctx *ctx, double fraction, int64_t min_entries) {
+    if (!ctx || !(fraction >= 0.0 && fraction <= 1.0) || min_entries < 1) return DMTZ_ERR_ARG;
+    ctx->list_frac = fraction;
+    ctx->list_min = min_entries;
+    cudaSetDevice(ctx->device);
+    for (int k = 0; k < 4; k++) {  // reallocated with the new reserve by the next call
+        cudaFree(ctx->lists[k]);
+        ctx->lists[k] = nullptr;
+        ctx->capL[k] = 0;
+    }
+    return DMTZ_OK;
+}
+
 dmtz_status dmtz_get_tuning(const dmtz_ctx *ctx, int *shape, int *blocks_per_sm) {
     if (!ctx) return DMTZ_ERR_ARG;
     if (shape) *shape = ctx->tune_shape;
@@ -1634,6 +1816,8 @@ dmtz_status dmtz_correct_batch(dmtz_ctx *ctx, int n, const dmtz_instance *inst, 
     auto work = [&](dmtz_ctx *w) {
         w->tune_shape = ctx->tune_shape;
         w->tune_bps = ctx->tune_bps;
+        w->list_frac = ctx->list_frac;
+        w->list_min = ctx->list_min;
         std::vector<double> fo, go;
         for (int i = next++; i < n; i = next++) {
             const dmtz_instance &I = inst[i];

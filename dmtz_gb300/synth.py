@@ -121,3 +121,41 @@ def batch_workload(n: int = 64, seed: int = 2024, lo: int = 32, hi: int = 192):
         dt = np.float32 if i % 2 == 0 else np.float64
         out.append((f.astype(dt), g.astype(dt), rel))
     return out
+
+
+def power_law_device(dims, seed: int, rel_eps: float, slope: float = -3.0, frac: float = 0.05):
+    """Large synthetic case generated on the GPU (torch is used only as a
+    seeded random-number and FFT toolbox here, for fields too big to build in
+    host memory quickly): the same recipe as power_law + decompress_sz, with
+    torch's CUDA generator instead of numpy's, so the values differ from the
+    host recipe's for the same seed.  Returns (f, g) as float64 device
+    tensors of shape (D*H*W,) and the bound eps = rel_eps x range."""
+    import torch
+
+    W, H, D = dims
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(int(seed))
+    white = torch.randn((D, H, W), generator=gen, device="cuda", dtype=torch.float32)
+    spec = torch.fft.rfftn(white)
+    del white
+    kz = torch.fft.fftfreq(D, device="cuda")[:, None, None]
+    ky = torch.fft.fftfreq(H, device="cuda")[None, :, None]
+    kx = torch.fft.rfftfreq(W, device="cuda")[None, None, :]
+    k2 = kx * kx + ky * ky + kz * kz
+    amp = torch.where(k2 > 0, k2.clamp_min(1e-30) ** (slope / 4.0), torch.zeros_like(k2))
+    spec *= amp
+    del amp, k2
+    f = torch.fft.irfftn(spec, s=(D, H, W))
+    del spec
+    f = ((f - f.min()) / (f.max() - f.min())).reshape(-1)  # float32 values, as the host recipe
+    f = f.double()
+    eps = rel_eps * float(f.max() - f.min())
+    fmin = float(f.min())
+    g = fmin + 2.0 * eps * torch.round((f - fmin) / (2.0 * eps))
+    sel = torch.rand(f.shape, generator=gen, device="cuda", dtype=torch.float32) < frac
+    noise = (torch.rand(f.shape, generator=gen, device="cuda", dtype=torch.float64) * 2.0 - 1.0) * eps
+    g += torch.where(sel, noise, torch.zeros_like(noise))
+    del sel, noise
+    g = torch.minimum(torch.maximum(g, f - eps), f + eps)
+    torch.cuda.synchronize()
+    return f, g, eps

@@ -175,6 +175,14 @@ dmtz_status dmtz_correct_batch(dmtz_ctx *ctx, int n, const dmtz_instance *inst, 
  * dmtz_autotune times a full sweep of `decp` for every shape and 8, 16, 32, 64
  * blocks per SM, keeps the fastest in the context and returns it in best[2]. */
 dmtz_status dmtz_set_tuning(dmtz_ctx *ctx, int shape, int blocks_per_sm);
+/* Memory of the mismatch lists (critical cells that differ between the two
+ * gradients).  Each of the four lists starts with room for `fraction` of the
+ * cells of its dimension, at least `min_entries` (defaults 1/16 and 2^20),
+ * and grows when a round produces more mismatches; results never depend on
+ * it.  The separatrix records are sized from the original field's saddle
+ * counts.  Together this keeps a correction near 125 bytes of device memory
+ * per vertex, so a 1024^3 field fits on one GPU. */
+dmtz_status dmtz_set_list_reserve(dmtz_ctx *ctx, double fraction, int64_t min_entries);
 /* name of the context's device (for keying tuning caches) */
 dmtz_status dmtz_device_name(const dmtz_ctx *ctx, char *buf, int len);
 dmtz_status dmtz_get_tuning(const dmtz_ctx *ctx, int *shape, int *blocks_per_sm);
