@@ -71,32 +71,56 @@ __global__ void k_mismatch_scan(Grid g, const uint32_t *crit_d, const uint32_t *
     }
 }
 
-// bricks whose anchors lie within 5 anchors of a changed vertex: the gradient
-// state of an anchor depends on values no further away (vertex pass +-1, edge
-// pass +-2, first triangle pass -3..2, second edge pass +-3, second triangle
-// pass +-4, criticality -5..4)
+// Dirty bricks, per pass.  The gradient state of an anchor depends on values
+// at most r_p anchors away in pass p: r = 1 (vertex pass), 2 (edge pass),
+// 3 (first triangle pass, -3..2), 3 (second edge pass), 4 (second triangle
+// pass), 5 (criticality, -5..4).  For every changed vertex, each brick within
+// 5 anchors gets bit r-1 for every r >= its distance (the largest per-axis gap
+// between the vertex and the brick's anchors); pass p re-pairs the bricks with
+// bit r_p - 1.  Flags are bytes packed four to a word (atomicOr on the word).
+constexpr int kRadii = 5;
 __global__ void k_mark_dirty(Grid g, int nbx, int nby, int nbz, int sx, int sy, int sz, const i64 *verts,
-                             const unsigned long long *nverts, uint8_t *flags) {
+                             const unsigned long long *nverts, uint32_t *flags) {
     const i64 n = (i64)*nverts;
     for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
         int x, y, z;
         decode_v(g, verts[i], x, y, z);
-        const int x0 = max(x - 5, 0) / sx, x1 = min(x + 5, g.W - 1) / sx;
-        const int y0 = max(y - 5, 0) / sy, y1 = min(y + 5, g.H - 1) / sy;
-        const int z0 = max(z - 5, 0) / sz, z1 = min(z + 5, g.D - 1) / sz;
-        for (int bz = z0; bz <= z1; bz++)
-            for (int by = y0; by <= y1; by++)
-                for (int bx = x0; bx <= x1; bx++) flags[bx + (i64)nbx * (by + (i64)nby * bz)] = 1;
+        const int x0 = max(x - kRadii, 0) / sx, x1 = min(x + kRadii, g.W - 1) / sx;
+        const int y0 = max(y - kRadii, 0) / sy, y1 = min(y + kRadii, g.H - 1) / sy;
+        const int z0 = max(z - kRadii, 0) / sz, z1 = min(z + kRadii, g.D - 1) / sz;
+        for (int bz = z0; bz <= z1; bz++) {
+            const int dz = max(0, max(bz * sz - z, z - (bz * sz + sz - 1)));
+            for (int by = y0; by <= y1; by++) {
+                const int dy = max(0, max(by * sy - y, y - (by * sy + sy - 1)));
+                for (int bx = x0; bx <= x1; bx++) {
+                    const int dx = max(0, max(bx * sx - x, x - (bx * sx + sx - 1)));
+                    const int d = max(dx, max(dy, dz));  // <= kRadii by the loop bounds
+                    const uint32_t mask = 0x1Fu & ~((1u << max(d - 1, 0)) - 1u);
+                    const i64 b = bx + (i64)nbx * (by + (i64)nby * bz);
+                    atomicOr(&flags[b >> 2], mask << (8 * (b & 3)));
+                }
+            }
+        }
     }
 }
-
-__global__ void k_compact_bricks(int nbx, int nby, int nbz, uint8_t *flags, uint32_t *list, unsigned long long *n) {
+// one compacted brick list per radius (list r-1 holds the bricks with bit
+// r-1), and the flags cleared for the next round
+__global__ void k_compact_bricks(int nbx, int nby, int nbz, uint32_t *flags, uint32_t *lists, i64 stride,
+                                 unsigned long long *n) {
     const i64 nb = (i64)nbx * nby * nbz;
-    for (i64 b = (i64)blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += (i64)gridDim.x * blockDim.x) {
-        if (!flags[b]) continue;
-        flags[b] = 0;
-        const int bx = (int)(b % nbx), by = (int)((b / nbx) % nby), bz = (int)(b / ((i64)nbx * nby));
-        list[atomicAdd(n, 1ull)] = (uint32_t)bx | ((uint32_t)by << 11) | ((uint32_t)bz << 22);
+    for (i64 w = (i64)blockIdx.x * blockDim.x + threadIdx.x; w < (nb + 3) / 4; w += (i64)gridDim.x * blockDim.x) {
+        const uint32_t word = flags[w];
+        if (!word) continue;
+        flags[w] = 0;
+        for (int q = 0; q < 4; q++) {
+            const uint32_t m = (word >> (8 * q)) & 0xFFu;
+            if (!m) continue;
+            const i64 b = 4 * w + q;
+            const int bx = (int)(b % nbx), by = (int)((b / nbx) % nby), bz = (int)(b / ((i64)nbx * nby));
+            const uint32_t code = (uint32_t)bx | ((uint32_t)by << 11) | ((uint32_t)bz << 22);
+            for (int r = 0; r < kRadii; r++)
+                if (m & (1u << r)) lists[r * stride + (i64)atomicAdd(&n[r], 1ull)] = code;
+        }
     }
 }
 
@@ -615,8 +639,9 @@ struct dmtz_ctx {
     i64 *as_tet = nullptr, *as_cur = nullptr, *ds_edge = nullptr, *ds_vert = nullptr;
     i64 capAS = 0, capDS = 0, capSad2 = 0;
     uint8_t *succ = nullptr;  // original ascending-path successor of each tetrahedron
-    uint8_t *brick_flags = nullptr;   // bricks to re-pair in the next sweep
-    uint32_t *brick_list = nullptr;   // their compacted list (counters[11])
+    uint32_t *brick_flags = nullptr;  // per brick (a byte each, four to a word): radius bits of the next sweep
+    uint32_t *brick_list = nullptr;   // compacted lists per radius, capB entries each
+    unsigned long long *brick_n = nullptr;  // their lengths
     i64 *sad2 = nullptr;      // original 2-saddle triangles
     unsigned long long *counters = nullptr;  // [0..3] cp lists, [4] requests, [5,6] paths, [8,9] min/max
                                              // keys, [10] original 2-saddles, [11] dirty bricks,
@@ -629,6 +654,8 @@ struct dmtz_ctx {
     std::vector<dmtz_ctx *> pool;  // worker contexts of dmtz_correct_batch
     uint8_t *mm = nullptr;         // mismatch bytes of the learned proposal's features
     i64 capMM = 0;
+    void *loopctl = nullptr;       // device copy of the graph loop's control block (kept: a
+                                   // cudaFree per call would synchronise the whole device)
 };
 
 namespace {
@@ -662,6 +689,8 @@ void free_all(dmtz_ctx *c) {
     cudaFree(c->as_tet); cudaFree(c->as_cur); cudaFree(c->ds_edge); cudaFree(c->ds_vert);
     cudaFree(c->counters); cudaFree(c->errword); cudaFree(c->changed);
     cudaFree(c->succ); cudaFree(c->sad2); cudaFree(c->brick_flags); cudaFree(c->brick_list);
+    cudaFree(c->brick_n);
+    c->brick_n = nullptr;
     c->succ = nullptr; c->sad2 = nullptr; c->brick_flags = nullptr; c->brick_list = nullptr;
     c->f = c->g = nullptr; c->cnt = nullptr; c->reqbits = nullptr; c->reqlist = nullptr;
     c->as_tet = c->as_cur = c->ds_edge = c->ds_vert = nullptr; c->counters = nullptr;
@@ -712,8 +741,9 @@ dmtz_status ensure(dmtz_ctx *ctx, const Grid &g) {
     CK(cudaMemset(ctx->reqbits, 0, sizeof(uint32_t) * (size_t)((V + 31) / 32 + 1)));
     CK(dalloc(&ctx->reqlist, V));
     CK(dalloc(&ctx->succ, 6 * V));
-    CK(dalloc(&ctx->brick_flags, nbr)); CK(dalloc(&ctx->brick_list, nbr));
-    CK(cudaMemset(ctx->brick_flags, 0, (size_t)nbr));
+    CK(dalloc(&ctx->brick_flags, (nbr + 3) / 4)); CK(dalloc(&ctx->brick_list, kRadii * nbr));
+    CK(dalloc(&ctx->brick_n, 8));
+    CK(cudaMemset(ctx->brick_flags, 0, sizeof(uint32_t) * (size_t)((nbr + 3) / 4)));
     ctx->capB = nbr;
     CK(dalloc(&ctx->counters, 16)); CK(dalloc(&ctx->errword, 1)); CK(dalloc(&ctx->changed, V));
     ctx->capV = g.V; ctx->capE = g.E; ctx->capF = g.F; ctx->capT = g.T;
@@ -761,17 +791,23 @@ unsigned sweep_grid(const dmtz_ctx *ctx, i64 nb) {
     return (unsigned)std::max<i64>(1, std::min<i64>(nb, cap));
 }
 
-// the five pairing passes and the criticality pass over a set of bricks
-void sweep(dmtz_ctx *ctx, const Grid &g, const FieldState &s, const BrickList &bl, i64 nb_max) {
+// the five pairing passes and the criticality pass, each over its brick set
+void sweep_passes(dmtz_ctx *ctx, const Grid &g, const FieldState &s, const BrickList bl[6], i64 nb_max) {
     const unsigned gr = sweep_grid(ctx, nb_max);
     cudaStream_t st = ctx->stream;
-    launch_pass<PASS_VERTEX>(g, s, bl, gr, st);
-    launch_pass<PASS_E2>(g, s, bl, gr, st);
-    launch_pass<PASS_F3>(g, s, bl, gr, st);
-    launch_pass<PASS_E4>(g, s, bl, gr, st);
-    launch_pass<PASS_F5>(g, s, bl, gr, st);
-    launch_pass<PASS_CRIT>(g, s, bl, gr, st);
+    launch_pass<PASS_VERTEX>(g, s, bl[0], gr, st);
+    launch_pass<PASS_E2>(g, s, bl[1], gr, st);
+    launch_pass<PASS_F3>(g, s, bl[2], gr, st);
+    launch_pass<PASS_E4>(g, s, bl[3], gr, st);
+    launch_pass<PASS_F5>(g, s, bl[4], gr, st);
+    launch_pass<PASS_CRIT>(g, s, bl[5], gr, st);
     ctx->launches += 6;
+}
+
+// the five pairing passes and the criticality pass over a set of bricks
+void sweep(dmtz_ctx *ctx, const Grid &g, const FieldState &s, const BrickList &bl, i64 nb_max) {
+    const BrickList per_pass[6] = {bl, bl, bl, bl, bl, bl};
+    sweep_passes(ctx, g, s, per_pass, nb_max);
 }
 
 BrickList all_bricks(const Grid &g, int shape, i64 &nb) {
@@ -811,19 +847,22 @@ void repair_dirty(dmtz_ctx *ctx, const Grid &g, const FieldState &s, const uint3
     const int shape = ctx->tune_shape;
     const i64 nb = bricks_of(g, shape, nbx, nby, nbz);
     cudaStream_t st = ctx->stream;
-    cudaMemsetAsync(ctx->counters + 11, 0, sizeof(unsigned long long), st);
+    cudaMemsetAsync(ctx->brick_n, 0, kRadii * sizeof(unsigned long long), st);
     k_mark_dirty<<<persistent_grid(), kBlock, 0, st>>>(g, nbx, nby, nbz, DMTZ_SHAPES[shape][0], DMTZ_SHAPES[shape][1],
                                                         DMTZ_SHAPES[shape][2], ctx->reqlist, ctx->counters + 4,
                                                         ctx->brick_flags);
     k_compact_bricks<<<persistent_grid(), kBlock, 0, st>>>(nbx, nby, nbz, ctx->brick_flags, ctx->brick_list,
-                                                            ctx->counters + 11);
+                                                            ctx->capB, ctx->brick_n);
     ctx->launches += 2;
-    BrickList bl;
-    bl.list = ctx->brick_list;
-    bl.n = ctx->counters + 11;
-    bl.nbx = nbx; bl.nby = nby; bl.nbz = nbz;
-    bl.shape = shape;
-    sweep(ctx, g, s, bl, nb);
+    static const int radius[6] = {1, 2, 3, 3, 4, 5};  // per pass
+    BrickList bl[6];
+    for (int p = 0; p < 6; p++) {
+        bl[p].list = ctx->brick_list + (i64)(radius[p] - 1) * ctx->capB;
+        bl[p].n = ctx->brick_n + (radius[p] - 1);
+        bl[p].nbx = nbx; bl[p].nby = nby; bl[p].nbz = nbz;
+        bl[p].shape = shape;
+    }
+    sweep_passes(ctx, g, s, bl, nb);
     scan_mismatch(ctx, g, s.crit, crit_o, want_saddles);
 }
 
@@ -1012,6 +1051,7 @@ void dmtz_ctx_destroy(dmtz_ctx *ctx) {
     cudaSetDevice(ctx->device);
     free_all(ctx);
     cudaFree(ctx->mm);
+    cudaFree(ctx->loopctl);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -1284,8 +1324,8 @@ static dmtz_status run_graph_loop(dmtz_ctx *ctx, const Grid &g, const RuleCtx &r
                                   LoopCtl init, LoopCtl *out) {
     cudaStream_t st = ctx->stream;
     const unsigned pgrid = persistent_grid();
-    LoopCtl *dctl = nullptr;
-    CK(dalloc(&dctl, 1));
+    if (!ctx->loopctl) CK(cudaMalloc(&ctx->loopctl, sizeof(LoopCtl)));
+    LoopCtl *dctl = static_cast<LoopCtl *>(ctx->loopctl);
     CK(cudaMemcpyAsync(dctl, &init, sizeof(LoopCtl), cudaMemcpyHostToDevice, st));
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -1367,7 +1407,6 @@ static dmtz_status run_graph_loop(dmtz_ctx *ctx, const Grid &g, const RuleCtx &r
     } while (0);
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
-    cudaFree(dctl);
     if (res != DMTZ_OK) {
         cudaGetLastError();
         return fail(ctx, res, "building or running the loop graph failed");
@@ -1810,6 +1849,26 @@ dmtz_status dmtz_correct_batch(dmtz_ctx *ctx, int n, const dmtz_instance *inst, 
         const dmtz_status cs = dmtz_ctx_create(&w, ctx->device);
         if (cs != DMTZ_OK) return fail(ctx, cs, "cannot create a worker context");
         ctx->pool.push_back(w);
+    }
+    // every worker's buffers are sized once for the largest extents of the
+    // batch: a reallocation in the middle would free device memory, and
+    // cudaFree waits for the whole device, i.e. for the other workers
+    int mW = 2, mH = 2, mD = 2;
+    for (int i = 0; i < n; i++) {
+        mW = std::max(mW, inst[i].W);
+        mH = std::max(mH, inst[i].H);
+        mD = std::max(mD, inst[i].D);
+    }
+    Grid gmax;
+    if (n > 0 && check_dims(ctx, mW, mH, mD, gmax) == DMTZ_OK) {
+        for (int k = 0; k < workers; k++) {
+            dmtz_ctx *w = ctx->pool[k];
+            w->list_frac = ctx->list_frac;
+            w->list_min = ctx->list_min;
+            cudaSetDevice(w->device);
+            const dmtz_status es = ensure(w, gmax);
+            if (es != DMTZ_OK) return fail(ctx, es, "cannot size worker buffers: " + w->err);
+        }
     }
     std::atomic<int> next(0);
     std::vector<dmtz_status> st((size_t)n, DMTZ_OK);
