@@ -85,6 +85,9 @@ def load_library(build_if_missing: bool = True):
     L.dmtz_mismatch.argtypes = [_vp, _int, _int, _int, _f64p, _f64p, _i64p, _i32p, _i32p, _i32p, _i32p]
     L.dmtz_fix_round.argtypes = [_vp, _int, _int, _int, _f64p, _f64p, _i32p, ctypes.c_double, _int, _int, _f64p]
     L.dmtz_path_detect.argtypes = [_vp, _int, _int, _int, _f64p, _f64p, _i64p, _i32p, _i32p, _i32p, _i32p]
+    L.dmtz_path_detect_connectivity.argtypes = [_vp, _int, _int, _int, _f64p, _f64p, _i64p, _i32p, _i32p, _i32p,
+                                                _i32p]
+    L.dmtz_path_detect_connectivity.restype = _int
     L.dmtz_correct.argtypes = [_vp, _int, _int, _int, _vp, _vp, _int, ctypes.c_double, ctypes.POINTER(Opts),
                                ctypes.POINTER(Report), _vp]
     L.dmtz_profile_sweep.argtypes = [_vp, _int, _int, _int, _vp, _vp, _int, _int, _f64p]
@@ -223,14 +226,16 @@ class Context:
                                            float(rel_eps), int(preserve_saddles), int(edit_type), out))
         return out
 
-    def path_detect(self, f, g, dims=None):
-        """Geometry-mode separatrix records (as_tet, as_cur, ds_edge, ds_vert), sorted."""
+    def path_detect(self, f, g, dims=None, connectivity=False):
+        """Separatrix records (as_tet, as_cur, ds_edge, ds_vert), sorted: geometry
+        mode, or connectivity mode (ds_vert = trouble maker)."""
         dims = _dims_of(np.asarray(f), dims)
         V, E, F, T = cell_counts(dims)
         c = np.zeros(2, np.int64)
         at, ac = np.empty(F, np.int32), np.empty(F, np.int32)
         de, dv = np.empty(E, np.int32), np.empty(E, np.int32)
-        self._check(self._L.dmtz_path_detect(self._h, *dims, _flat(f), _flat(g), c, at, ac, de, dv))
+        fn = self._L.dmtz_path_detect_connectivity if connectivity else self._L.dmtz_path_detect
+        self._check(fn(self._h, *dims, _flat(f), _flat(g), c, at, ac, de, dv))
         na, nd = int(c[0]), int(c[1])
         return at[:na].copy(), ac[:na].copy(), de[:nd].copy(), dv[:nd].copy()
 

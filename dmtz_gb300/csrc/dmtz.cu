@@ -213,11 +213,25 @@ struct PathRec {
 
 // Original ascending paths (is_false, main_3d.cu:4437-4497) step from a
 // tetrahedron through the facet it is paired with to that facet's other
-// coface.  The original gradient is fixed during a correction, so each
-// tetrahedron's successor is computed once and stored in one byte: the
-// successor's anchor offset ((dx+1) + 3(dy+1) + 9(dz+1), each in -1..1) times
-// 6 plus its slot; 255 = the path ends (boundary facet).  The reference's
-// back-pointer test on the way is always true for a consistent gradient.
+// coface (get_cell_tetra's other one; none = the path leaves the grid).  The
+// original gradient is fixed during a correction, so each tetrahedron's
+// successor is computed once and stored in one byte: the successor's anchor
+// offset ((dx+1) + 3(dy+1) + 9(dz+1), each in -1..1) times 6 plus its slot;
+// 255 = the path ends (a maximum, or a boundary facet).  The six bytes of an
+// anchor's tetrahedra share one 8-byte word (one coalesced store).  The
+// reference's back-pointer test on the way is always true for a consistent
+// gradient.
+__device__ __forceinline__ uint8_t asc_step(const Grid &g, int x, int y, int z, int ts, uint32_t tc) {
+    const int j = (tc >> (3 * ts)) & 7;
+    if (j == 7) return 255;
+    const signed char *tf = TOPO_TET_FACE[ts][j];
+    const int fs = tf[3], other = 1 - tf[4];
+    if (other >= TOPO_FACE_NCOF[fs]) return 255;
+    const signed char *oc = TOPO_FACE_COF[fs][other];
+    const int dx = tf[0] + oc[0], dy = tf[1] + oc[1], dz = tf[2] + oc[2];
+    if (!cell_ok(g, x + dx, y + dy, z + dz, 1, 1, 1)) return 255;
+    return (uint8_t)(((dx + 1) + 3 * (dy + 1) + 9 * (dz + 1)) * 6 + oc[3]);
+}
 __global__ void k_path_succ(Grid g, const uint32_t *tcodeP, uint8_t *succ) {
     i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= g.V) return;
@@ -225,33 +239,38 @@ __global__ void k_path_succ(Grid g, const uint32_t *tcodeP, uint8_t *succ) {
     decode_v(g, v, x, y, z);
     const bool cube = cell_ok(g, x, y, z, 1, 1, 1);
     const uint32_t tc = tcodeP[v];
+    uint64_t packed = 0xFFFF000000000000ull;
     for (int ts = 0; ts < 6; ts++) {
-        uint8_t out = 255;
-        const int j = (tc >> (3 * ts)) & 7;
-        if (cube && j != 7) {
-            const signed char *tf = TOPO_TET_FACE[ts][j];
-            const int fs = tf[3], other = 1 - tf[4];
-            if (other < TOPO_FACE_NCOF[fs]) {
-                const signed char *oc = TOPO_FACE_COF[fs][other];
-                const int dx = tf[0] + oc[0], dy = tf[1] + oc[1], dz = tf[2] + oc[2];
-                if (cell_ok(g, x + dx, y + dy, z + dz, 1, 1, 1))
-                    out = (uint8_t)(((dx + 1) + 3 * (dy + 1) + 9 * (dz + 1)) * 6 + oc[3]);
-            }
-        }
-        succ[v * 6 + ts] = out;
+        const uint8_t out = cube ? asc_step(g, x, y, z, ts, tc) : (uint8_t)255;
+        packed |= (uint64_t)out << (8 * ts);
     }
+    reinterpret_cast<uint64_t *>(succ)[v] = packed;
 }
 
 // compact list of the original 2-saddle triangles (anchor * 12 + slot)
 __global__ void k_sad2_list(Grid g, const uint32_t *critP, i64 *list, i64 cap, unsigned long long *n) {
-    i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= g.V) return;
-    uint32_t m = (critP[v] >> 8) & 0xFFFu;
+    // every lane of every warp takes part (block size is a multiple of 32);
+    // lanes past the end contribute nothing.  One atomic per warp: a single
+    // counter takes every append.
+    const i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t m = v < g.V ? (critP[v] >> 8) & 0xFFFu : 0u;
+    const unsigned lane = threadIdx.x & 31, full = 0xffffffffu;
+    const unsigned mine = __popc(m);
+    unsigned incl = mine;
+    for (int off = 1; off < 32; off <<= 1) {
+        const unsigned y = __shfl_up_sync(full, incl, off);
+        if (lane >= (unsigned)off) incl += y;
+    }
+    const unsigned total = __shfl_sync(full, incl, 31);
+    unsigned long long base = 0;
+    if (lane == 31 && total) base = atomicAdd(n, (unsigned long long)total);
+    base = __shfl_sync(full, base, 31);
+    unsigned long long at = base + incl - mine;
     while (m) {
         const int sl = __ffs(m) - 1;
         m &= m - 1;
-        const unsigned long long at = atomicAdd(n, 1ull);
         if ((i64)at < cap) list[at] = v * 12 + sl;
+        at++;
     }
 }
 
@@ -306,7 +325,7 @@ __global__ void k_path_as(Grid g, const i64 *sad2, const unsigned long long *nsa
                     found = true;
                     break;
                 }
-                const int s8 = succ[ci * 6 + cs];
+                const int s8 = succ[ci * 8 + cs];
                 if (s8 == 255) break;
                 const int d = s8 / 6;
                 cs = s8 - 6 * d;
@@ -346,6 +365,146 @@ __global__ void k_path_ds(RuleCtx c, PathRec R) {
                     if ((i64)at < R.cap_ds) {
                         R.ds_edge[at] = edge_ref(g, x, y, z, k);
                         R.ds_vert[at] = e;
+                    }
+                    break;
+                }
+            }
+        }
+    }
+}
+
+// ------------------------------------------------- connectivity-mode separatrices
+// (preserve_vpath=1, preserve_geometry=0): a separatrix counts as false when
+// its end differs, not its geometry.
+//
+// End of the descending path from vertex v under vertex directions pv: the
+// minimum reached (the walks of get_orginal_saddle_min_pairs and
+// get_false_ds_vpath_connectivity, main_3d.cu:4613-4687, 4961-5062).  With pvo
+// given, trouble (if still -1) becomes the first vertex on the way whose
+// direction under pvo differs (the reference's trouble_maker; it compares
+// before stepping, never at the end vertex).
+__device__ i64 desc_end(const Grid &g, const uint8_t *pv, const uint8_t *pvo, i64 v, i64 &trouble, i64 cap,
+                        int *err) {
+    for (i64 steps = 0;; steps++) {
+        const int d = pv[v];
+        if (d == 15) return v;
+        if (pvo && trouble < 0 && pvo[v] != d) trouble = v;
+        v += g.doff[d];
+        if (steps > cap) {
+            atomicOr(err, ERR_WALK);
+            return v;
+        }
+    }
+}
+// End of the ascending path from tetrahedron (x, y, z, s) under tet codes tc:
+// the maximum reached (reference id) or -1 when the path leaves the grid
+// (get_paired_id, main_3d.cu:4499-4537)
+__device__ i64 asc_end(const Grid &g, const uint32_t *tc, int x, int y, int z, int s, i64 cap, int *err) {
+    for (i64 steps = 0;; steps++) {
+        const uint32_t code = tc[x + (i64)y * g.W + (i64)z * g.WH];
+        if (((code >> (3 * s)) & 7) == 7) return tet_ref(g, x, y, z, s);
+        const int s8 = asc_step(g, x, y, z, s, code);
+        if (s8 == 255) return -1;
+        const int d = s8 / 6;
+        s = s8 - 6 * d;
+        x += d % 3 - 1;
+        y += (d / 3) % 3 - 1;
+        z += d / 9 - 1;
+        if (steps > cap) {
+            atomicOr(err, ERR_WALK);
+            return -1;
+        }
+    }
+}
+// is_false (main_3d.cu:4437-4497): along the original ascending path from the
+// tetrahedron, the first one whose decompressed pairing differs (into cur)
+__device__ bool first_diff(const Grid &g, const uint32_t *tcP, const uint32_t *tcQ, const uint8_t *succ, int x, int y,
+                           int z, int s, i64 cap, int *err, i64 &cur) {
+    for (i64 steps = 0;; steps++) {
+        const i64 ci = x + (i64)y * g.W + (i64)z * g.WH;
+        const int p = (tcP[ci] >> (3 * s)) & 7;
+        if (p == 7) return false;
+        if (p != (int)((tcQ[ci] >> (3 * s)) & 7)) {
+            cur = tet_ref(g, x, y, z, s);
+            return true;
+        }
+        const int s8 = succ[ci * 8 + s];
+        if (s8 == 255) return false;
+        const int d = s8 / 6;
+        s = s8 - 6 * d;
+        x += d % 3 - 1;
+        y += (d / 3) % 3 - 1;
+        z += d / 9 - 1;
+        if (steps > cap) {
+            atomicOr(err, ERR_WALK);
+            return false;
+        }
+    }
+}
+// get_false_ds_vpath_connectivity (main_3d.cu:4961-5062): for each original
+// 1-saddle edge, the decompressed descending paths from its endpoints (v1,
+// the higher id, first) against the original ones; the first endpoint whose
+// minimum differs records (edge, trouble maker), the trouble maker carried
+// over from v1's walk into v2's as in the reference.
+__global__ void k_conn_ds(RuleCtx c, PathRec R, i64 cap) {
+    const Grid &g = c.g;
+    for (i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x; v < g.V; v += (i64)gridDim.x * blockDim.x) {
+        uint32_t m = (c.P.crit[v] >> 1) & 0x7Fu;
+        if (!m) continue;
+        int x, y, z;
+        decode_v(g, v, x, y, z);
+        while (m) {
+            const int k = __ffs(m) - 1;
+            m &= m - 1;
+            const i64 ends[2] = {v + g.coff[TOPO_EDGE_V[k][0]], v + g.coff[TOPO_EDGE_V[k][1]]};
+            i64 trouble = -1, unused = -1;
+            for (int j = 0; j < 2; j++) {
+                const i64 eq = desc_end(g, c.Q.pv, c.P.pv, ends[j], trouble, cap, c.err);
+                const i64 ep = desc_end(g, c.P.pv, nullptr, ends[j], unused, cap, c.err);
+                if (eq != ep) {
+                    const unsigned long long at = atomicAdd(&R.n[1], 1ull);
+                    if ((i64)at < R.cap_ds) {
+                        R.ds_edge[at] = edge_ref(g, x, y, z, k);
+                        R.ds_vert[at] = trouble;
+                    }
+                    break;
+                }
+            }
+        }
+    }
+}
+// get_false_as_vpath_connectivity (main_3d.cu:4761-4835) as intended: for each
+// decompressed 2-saddle triangle, its cofaces in search order; a coface whose
+// decompressed ascending path ends at another maximum than the original one
+// (the original end is -1 for triangles that are not original 2-saddles, the
+// reference's initial value) is checked with is_false, and the first record
+// ends the triangle.  The reference indexes its table of original ends by the
+// direction loop's counter instead of the triangle (all triangles share 28
+// slots, written concurrently), so its own result depends on scheduling.
+__global__ void k_conn_as(Grid g, const uint32_t *critP, const uint32_t *critQ, const uint32_t *tcP,
+                          const uint32_t *tcQ, const uint8_t *succ, PathRec R, i64 cap, int *err) {
+    for (i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x; v < g.V; v += (i64)gridDim.x * blockDim.x) {
+        uint32_t m = (critQ[v] >> 8) & 0xFFFu;
+        if (!m) continue;
+        const uint32_t mp = (critP[v] >> 8) & 0xFFFu;
+        int x, y, z;
+        decode_v(g, v, x, y, z);
+        while (m) {
+            const int sl = __ffs(m) - 1;
+            m &= m - 1;
+            for (int j = 0; j < TOPO_FACE_NCOF[sl]; j++) {
+                const signed char *tc = TOPO_FACE_COF[sl][j];
+                const int cx = x + tc[0], cy = y + tc[1], cz = z + tc[2], cs = tc[3];
+                if (!cell_ok(g, cx, cy, cz, 1, 1, 1)) continue;
+                const i64 eq = asc_end(g, tcQ, cx, cy, cz, cs, cap, err);
+                const i64 ep = ((mp >> sl) & 1u) ? asc_end(g, tcP, cx, cy, cz, cs, cap, err) : -1;
+                if (eq == ep) continue;
+                i64 cur;
+                if (first_diff(g, tcP, tcQ, succ, cx, cy, cz, cs, cap, err, cur)) {
+                    const unsigned long long at = atomicAdd(&R.n[0], 1ull);
+                    if ((i64)at < R.cap_as) {
+                        R.as_tet[at] = tet_ref(g, cx, cy, cz, cs);
+                        R.as_cur[at] = cur;
                     }
                     break;
                 }
@@ -449,7 +608,7 @@ __global__ void k_asc_init(Grid g, const uint32_t *tcode, const uint8_t *succ, i
             lab[t] = t;  // a maximum
             continue;
         }
-        const int s8 = succ[t];
+        const int s8 = succ[v * 8 + ts];
         if (s8 == 255) {
             lab[t] = -1;  // leaves through the boundary
             continue;
@@ -740,7 +899,7 @@ dmtz_status ensure(dmtz_ctx *ctx, const Grid &g) {
     CK(dalloc(&ctx->reqbits, (V + 31) / 32 + 1));
     CK(cudaMemset(ctx->reqbits, 0, sizeof(uint32_t) * (size_t)((V + 31) / 32 + 1)));
     CK(dalloc(&ctx->reqlist, V));
-    CK(dalloc(&ctx->succ, 6 * V));
+    CK(dalloc(&ctx->succ, 8 * V));
     CK(dalloc(&ctx->brick_flags, (nbr + 3) / 4)); CK(dalloc(&ctx->brick_list, kRadii * nbr));
     CK(dalloc(&ctx->brick_n, 8));
     CK(cudaMemset(ctx->brick_flags, 0, sizeof(uint32_t) * (size_t)((nbr + 3) / 4)));
@@ -985,11 +1144,23 @@ dmtz_status prep_paths(dmtz_ctx *ctx, const Grid &g) {
 }
 
 // separatrix detection (ascending and descending) into the path records
-void detect_paths(dmtz_ctx *ctx, const Grid &g, const RuleCtx &rc, const PathRec &R, unsigned grid) {
-    cudaMemsetAsync(ctx->counters + 5, 0, 2 * sizeof(unsigned long long), ctx->stream);
-    k_path_as<<<grid, kBlock, 0, ctx->stream>>>(g, ctx->sad2, ctx->counters + 10, ctx->P.tcode, ctx->Q.tcode,
-                                                  ctx->succ, R, g.T + 16, ctx->errword);
-    k_path_ds<<<grid, kBlock, 0, ctx->stream>>>(rc, R);
+// geometry mode (conn = 0) or connectivity mode (conn = 1); no launch counting
+// (also used while capturing the graph loop)
+void launch_detect(dmtz_ctx *ctx, const Grid &g, const RuleCtx &rc, const PathRec &R, unsigned grid, int conn) {
+    cudaStream_t st = ctx->stream;
+    cudaMemsetAsync(ctx->counters + 5, 0, 2 * sizeof(unsigned long long), st);
+    if (conn) {
+        k_conn_as<<<grid, kBlock, 0, st>>>(g, ctx->P.crit, ctx->Q.crit, ctx->P.tcode, ctx->Q.tcode, ctx->succ, R,
+                                           g.T + 16, ctx->errword);
+        k_conn_ds<<<grid, kBlock, 0, st>>>(rc, R, g.V + 16);
+    } else {
+        k_path_as<<<grid, kBlock, 0, st>>>(g, ctx->sad2, ctx->counters + 10, ctx->P.tcode, ctx->Q.tcode, ctx->succ,
+                                           R, g.T + 16, ctx->errword);
+        k_path_ds<<<grid, kBlock, 0, st>>>(rc, R);
+    }
+}
+void detect_paths(dmtz_ctx *ctx, const Grid &g, const RuleCtx &rc, const PathRec &R, unsigned grid, int conn = 0) {
+    launch_detect(ctx, g, rc, R, grid, conn);
     ctx->launches += 2;
 }
 
@@ -1167,9 +1338,9 @@ dmtz_status dmtz_fix_round(dmtz_ctx *ctx, int W, int H, int D, const double *ori
     return DMTZ_OK;
 }
 
-dmtz_status dmtz_path_detect(dmtz_ctx *ctx, int W, int H, int D, const double *orig, const double *decp,
-                             int64_t counts[2], int32_t *as_tet, int32_t *as_cur, int32_t *ds_edge,
-                             int32_t *ds_vert) {
+static dmtz_status path_detect_impl(dmtz_ctx *ctx, int W, int H, int D, const double *orig, const double *decp,
+                                    int conn, int64_t counts[2], int32_t *as_tet, int32_t *as_cur, int32_t *ds_edge,
+                                    int32_t *ds_vert) {
     Grid g;
     dmtz_status s = check_dims(ctx, W, H, D, g);
     if (s != DMTZ_OK) return s;
@@ -1178,12 +1349,35 @@ dmtz_status dmtz_path_detect(dmtz_ctx *ctx, int W, int H, int D, const double *o
     CK(cudaMemsetAsync(ctx->errword, 0, sizeof(int), ctx->stream));
     RuleCtx rc = rule_ctx(ctx, g, 0.0, 0);
     if ((s = prep_paths(ctx, g)) != DMTZ_OK) return s;
-    detect_paths(ctx, g, rc, path_rec(ctx), persistent_grid());
     unsigned long long hc[2];
-    CK(cudaMemcpyAsync(hc, ctx->counters + 5, sizeof(hc), cudaMemcpyDeviceToHost, ctx->stream));
     int err = 0;
-    CK(cudaMemcpyAsync(&err, ctx->errword, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
+    for (int attempt = 0; attempt < 2; attempt++) {
+        detect_paths(ctx, g, rc, path_rec(ctx), persistent_grid(), conn);
+        CK(cudaMemcpyAsync(hc, ctx->counters + 5, sizeof(hc), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(&err, ctx->errword, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        // connectivity mode walks from the decompressed 2-saddles, which may
+        // outnumber the original ones the records were sized for: grow, redo
+        if ((i64)hc[0] <= ctx->capAS && (i64)hc[1] <= ctx->capDS) break;
+        if ((i64)hc[0] > ctx->capAS) {
+            cudaFree(ctx->as_tet);
+            cudaFree(ctx->as_cur);
+            ctx->as_tet = ctx->as_cur = nullptr;
+            ctx->capAS = 0;
+            CK(dalloc(&ctx->as_tet, (i64)hc[0]));
+            CK(dalloc(&ctx->as_cur, (i64)hc[0]));
+            ctx->capAS = (i64)hc[0];
+        }
+        if ((i64)hc[1] > ctx->capDS) {
+            cudaFree(ctx->ds_edge);
+            cudaFree(ctx->ds_vert);
+            ctx->ds_edge = ctx->ds_vert = nullptr;
+            ctx->capDS = 0;
+            CK(dalloc(&ctx->ds_edge, (i64)hc[1]));
+            CK(dalloc(&ctx->ds_vert, (i64)hc[1]));
+            ctx->capDS = (i64)hc[1];
+        }
+    }
     counts[0] = (int64_t)hc[0];
     counts[1] = (int64_t)hc[1];
     auto fetch = [&](i64 *da, i64 *db, unsigned long long n, int32_t *oa, int32_t *ob) -> dmtz_status {
@@ -1202,9 +1396,21 @@ dmtz_status dmtz_path_detect(dmtz_ctx *ctx, int W, int H, int D, const double *o
     };
     if ((s = fetch(ctx->as_tet, ctx->as_cur, hc[0], as_tet, as_cur)) != DMTZ_OK) return s;
     if ((s = fetch(ctx->ds_edge, ctx->ds_vert, hc[1], ds_edge, ds_vert)) != DMTZ_OK) return s;
-    if (err & ERR_WALK) return fail(ctx, DMTZ_ERR_CYCLE, "ascending path walk exceeded its step cap");
+    if (err & ERR_WALK) return fail(ctx, DMTZ_ERR_CYCLE, "a path walk exceeded its step cap");
     if (err & ERR_OOB) return fail(ctx, DMTZ_ERR_OOB, "a path rule indexed out of range");
     return DMTZ_OK;
+}
+
+dmtz_status dmtz_path_detect(dmtz_ctx *ctx, int W, int H, int D, const double *orig, const double *decp,
+                             int64_t counts[2], int32_t *as_tet, int32_t *as_cur, int32_t *ds_edge,
+                             int32_t *ds_vert) {
+    return path_detect_impl(ctx, W, H, D, orig, decp, 0, counts, as_tet, as_cur, ds_edge, ds_vert);
+}
+
+dmtz_status dmtz_path_detect_connectivity(dmtz_ctx *ctx, int W, int H, int D, const double *orig,
+                                          const double *decp, int64_t counts[2], int32_t *as_tet, int32_t *as_cur,
+                                          int32_t *ds_edge, int32_t *ds_vert) {
+    return path_detect_impl(ctx, W, H, D, orig, decp, 1, counts, as_tet, as_cur, ds_edge, ds_vert);
 }
 
 // ----------------------------------------------------------------------------- graph-driven loop
@@ -1320,7 +1526,7 @@ struct PhaseTimer {
 
 // Build and run the graph-driven loop.  Returns the final LoopCtl in *out.
 static dmtz_status run_graph_loop(dmtz_ctx *ctx, const Grid &g, const RuleCtx &rc, const CpLists &L,
-                                  const PathRec &PR, const FieldState &Qs, double range, int ps, int pt,
+                                  const PathRec &PR, const FieldState &Qs, double range, int ps, int pt, int conn,
                                   LoopCtl init, LoopCtl *out) {
     cudaStream_t st = ctx->stream;
     const unsigned pgrid = persistent_grid();
@@ -1372,12 +1578,7 @@ static dmtz_status run_graph_loop(dmtz_ctx *ctx, const Grid &g, const RuleCtx &r
                 res = DMTZ_ERR_CUDA;
                 break;
             }
-            if (state == LS_PDF || state == LS_PCHECK) {
-                cudaMemsetAsync(ctx->counters + 5, 0, 2 * sizeof(unsigned long long), st);
-                k_path_as<<<pgrid, kBlock, 0, st>>>(g, ctx->sad2, ctx->counters + 10, ctx->P.tcode, ctx->Q.tcode,
-                                                     ctx->succ, PR, g.T + 16, ctx->errword);
-                k_path_ds<<<pgrid, kBlock, 0, st>>>(rc, PR);
-            }
+            if (state == LS_PDF || state == LS_PCHECK) launch_detect(ctx, g, rc, PR, pgrid, conn);
             if (state != LS_PCHECK) {
                 cudaMemsetAsync(ctx->counters + 4, 0, sizeof(unsigned long long), st);
                 if (state == LS_CP) k_fix_cp<<<pgrid, kBlock, 0, st>>>(rc, L, ps);
@@ -1467,7 +1668,7 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
               filt = opts->filtration, pc = opts->preserve_connectors, pt = opts->preserve_type,
               et = opts->edit_type;
     if (pc == 1) return fail(ctx, DMTZ_ERR_UNSUPPORTED, "preserve_connectors=1 is not supported");
-    if (pvp == 1 && pg == 0) return fail(ctx, DMTZ_ERR_UNSUPPORTED, "connectivity-mode separatrices are not supported");
+    const int conn = (pvp == 1 && pg == 0) ? 1 : 0;  // connectivity-mode separatrices
     if (!(rel_eps >= 0.0) || !std::isfinite(rel_eps)) return fail(ctx, DMTZ_ERR_ARG, "rel_eps must be finite and >= 0");
     const i64 max_rounds = opts->max_rounds > 0 ? opts->max_rounds : 100000;
     CK(cudaSetDevice(ctx->device));
@@ -1546,7 +1747,7 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
             LoopCtl cur = c;
             while (true) {
                 for (int k = 0; k < 4; k++) cur.cap[k] = ctx->capL[k];
-                if ((s = run_graph_loop(ctx, g, rc, cp_lists(ctx), PR, Qs, range, ps, pt, cur, &fin)) != DMTZ_OK)
+                if ((s = run_graph_loop(ctx, g, rc, cp_lists(ctx), PR, Qs, range, ps, pt, conn, cur, &fin)) != DMTZ_OK)
                     return s;
                 if (!fin.overflow) break;
                 // a scan outgrew a list: grow it, rebuild the lists and resume
@@ -1607,7 +1808,7 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
         R.path_rounds++;
         if (!paths_fresh) {  // else the last re-check ran on this same state
             pt_.begin(PH_PATH);
-            detect_paths(ctx, g, rc, PR, pgrid);
+            detect_paths(ctx, g, rc, PR, pgrid, conn);
             pt_.end();
         }
         paths_fresh = false;
@@ -1627,7 +1828,7 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
         n_as = n_ds = n_wall = 0;
         if (!cp_any()) {
             pt_.begin(PH_PATH);
-            detect_paths(ctx, g, rc, PR, pgrid);
+            detect_paths(ctx, g, rc, PR, pgrid, conn);
             pt_.end();
             if ((s = read_counts()) != DMTZ_OK) return s;
             n_as = (i64)hc[5];

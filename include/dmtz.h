@@ -124,6 +124,18 @@ dmtz_status dmtz_path_detect(dmtz_ctx *ctx, int W, int H, int D, const double *o
                              int64_t counts[2], int32_t *as_tet, int32_t *as_cur, int32_t *ds_edge,
                              int32_t *ds_vert);
 
+/* Connectivity-mode separatrix check (preserve_vpath=1, preserve_geometry=0):
+ * a separatrix is false when its end differs, not its geometry.  Descending
+ * half as get_false_ds_vpath_connectivity (main_3d.cu:4961-5062; ds_vert is
+ * the reference's trouble maker, -1 when none was met).  Ascending half as
+ * get_false_as_vpath_connectivity (main_3d.cu:4761-4835) meant it: the
+ * original ends are kept per triangle, where the reference indexes them by a
+ * loop counter shared by all triangles (a race, so its own output depends on
+ * scheduling).  Same arguments and record layout as dmtz_path_detect. */
+dmtz_status dmtz_path_detect_connectivity(dmtz_ctx *ctx, int W, int H, int D, const double *orig,
+                                          const double *decp, int64_t counts[2], int32_t *as_tet, int32_t *as_cur,
+                                          int32_t *ds_edge, int32_t *ds_vert);
+
 /* The whole correction (main_3d.cu:6255-7149): extracts both complexes and
  * edits `decp` in place until they agree.  bound = (max(orig) - min(orig)) *
  * rel_eps, as in the reference.  edit_counter_out (optional, V ints) receives

@@ -1314,6 +1314,184 @@ int orc_path_detect(int W, int H, int D, const int *PV, const int *PE, const int
     return c->oob;
 }
 
+/* ---------------------------------------------------------------------------
+ * A18: connectivity-mode separatrices (preserve_vpath=1, preserve_geometry=0)
+ * ------------------------------------------------------------------------- */
+
+/* get_paired_id, main_3d.cu:4499-4537: end of the ascending path from tet id
+ * under the original (dec = 0) or decompressed (dec = 1) pairing */
+static int paired_id(ctx_t *c, int id, int dec) {
+    int cur = id, old, t;
+    long long steps = 0;
+    do {
+        old = cur;
+        t = dec ? QTa(cur) : PTa(cur);
+        if (t == -1) break;
+        const int pf = dec ? QFa(t) : PFa(t);
+        if (pf == -1 || (pf != -1 && (dec ? QTa(pf) : PTa(pf)) != t)) break;
+        int t1 = -1, t2 = -1;
+        cell_tetra(c, t, &t1, &t2);
+        cur = t1 == cur ? t2 : t1;
+        if (++steps > WALK_CAP) {
+            c->oob++;
+            break;
+        }
+    } while (cur != old && cur != -1);
+    return cur;
+}
+
+/* the descending walk of get_orginal_saddle_min_pairs (main_3d.cu:4613-4687)
+ * from vertex v0 under the original pairing: the minimum reached */
+static int min_of(ctx_t *c, int v0) {
+    int v = v0, cur = v0;
+    long long steps = 0;
+    do {
+        v = cur;
+        if (PVa(v) == -1) break;
+        const int e = PVa(v);
+        if (PEa(e) == -1) break;
+        int a, b;
+        edge_verts(&c->G, e, &a, &b);
+        cur = a == cur ? b : a;
+        if (++steps > WALK_CAP) {
+            c->oob++;
+            break;
+        }
+    } while (PVa(v) != -1);
+    return v;
+}
+
+/* the decompressed descending walk of get_false_ds_vpath_connectivity
+ * (main_3d.cu:4961-5062): end vertex; *trouble (if -1) becomes the first
+ * vertex whose original and decompressed pairings differ */
+static int dec_min_of(ctx_t *c, int v0, int *trouble) {
+    int v = v0, cur = v0;
+    long long steps = 0;
+    do {
+        v = cur;
+        if (QVa(v) == -1) break;
+        const int e = PVa(v), de = QVa(v);
+        if (e != de && *trouble == -1) *trouble = v;
+        if (QEa(de) == -1) break;
+        int a, b;
+        edge_verts(&c->G, de, &a, &b);
+        cur = a == cur ? b : a;
+        if (++steps > WALK_CAP) {
+            c->oob++;
+            break;
+        }
+    } while (QVa(v) != -1);
+    return v;
+}
+
+/* get_orginal_saddle_min_pairs / get_orginal_saddle_max_pairs
+ * (main_3d.cu:4613-4759): the original ends of every original saddle's
+ * separatrices; conn_min (2E) by edge, conn_max (2F) by triangle and coface
+ * number, -1 where unset.  The reference's max table is indexed by its
+ * direction-loop counter instead of the triangle (a race between all
+ * triangles); this restates the intended indexing. */
+static void conn_prep(ctx_t *c, int *conn_min, int *conn_max) {
+    const grid_t *G = &c->G;
+    for (int i = 0; i < 2 * G->E; i++) conn_min[i] = -1;
+    for (int i = 0; i < 2 * G->F; i++) conn_max[i] = -1;
+    for (int i = 0; i < G->E; i++) {
+        if (c->PE[i] != -1) continue;
+        int v1, v2;
+        edge_verts(G, i, &v1, &v2);
+        conn_min[2 * i] = min_of(c, v1);
+        conn_min[2 * i + 1] = min_of(c, v2);
+    }
+    for (int i = 0; i < G->F; i++) {
+        if (c->PF[i] != -1) continue;
+        int v1, v2, v3;
+        tri_verts(G, i, &v1, &v2, &v3);
+        int x1, y1, z1, x2, y2, z2, x3, y3, z3;
+        coords(G, v1, &x1, &y1, &z1);
+        coords(G, v2, &x2, &y2, &z2);
+        coords(G, v3, &x3, &y3, &z3);
+        int num = 0;
+        for (int k = 0; k < 14; k++) {
+            int nx = x1 + DIRS[k][0], ny = y1 + DIRS[k][1], nz = z1 + DIRS[k][2];
+            int n = nx + ny * G->W + nz * G->W * G->H;
+            if (nx >= G->W || ny >= G->H || nz >= G->D || nx < 0 || ny < 0 || nz < 0 || n >= G->V || n < 0) continue;
+            if (!is_dir(nx - x2, ny - y2, nz - z2) || !is_dir(nx - x3, ny - y3, nz - z3)) continue;
+            if (n == v1 || n == v2 || n == v3) continue;
+            conn_max[2 * i + num] = paired_id(c, tet_id(G, v1, v2, v3, n), 0);
+            num++;
+        }
+    }
+}
+
+/* get_false_as_vpath_connectivity (intended indexing) and
+ * get_false_ds_vpath_connectivity, main_3d.cu:4761-4835, 4961-5062 */
+static void conn_detect(ctx_t *c, const int *conn_min, const int *conn_max, int counts[2], int *as_tet, int *as_cur,
+                        int *ds_edge, int *ds_vert) {
+    const grid_t *G = &c->G;
+    int nas = 0;
+    for (int i = 0; i < G->F; i++) {
+        if (c->QF[i] != -1) continue; /* the decompressed 2-saddles */
+        int v1, v2, v3;
+        tri_verts(G, i, &v1, &v2, &v3);
+        int x1, y1, z1, x2, y2, z2, x3, y3, z3;
+        coords(G, v1, &x1, &y1, &z1);
+        coords(G, v2, &x2, &y2, &z2);
+        coords(G, v3, &x3, &y3, &z3);
+        int num = 0;
+        for (int k = 0; k < 14; k++) {
+            int nx = x1 + DIRS[k][0], ny = y1 + DIRS[k][1], nz = z1 + DIRS[k][2];
+            int n = nx + ny * G->W + nz * G->W * G->H;
+            if (nx >= G->W || ny >= G->H || nz >= G->D || nx < 0 || ny < 0 || nz < 0 || n >= G->V || n < 0) continue;
+            if (!is_dir(nx - x2, ny - y2, nz - z2) || !is_dir(nx - x3, ny - y3, nz - z3)) continue;
+            if (n == v1 || n == v2 || n == v3) continue;
+            const int tid = tet_id(G, v1, v2, v3, n);
+            const int dec_id = paired_id(c, tid, 1);
+            int cur;
+            if (dec_id != conn_max[2 * i + num] && is_false(c, tid, &cur)) {
+                if (as_tet) as_tet[nas] = tid;
+                if (as_cur) as_cur[nas] = cur;
+                nas++;
+                break;
+            }
+            num++;
+        }
+    }
+    int nds = 0;
+    for (int i = 0; i < G->E; i++) {
+        if (c->PE[i] != -1) continue;
+        int v1, v2;
+        edge_verts(G, i, &v1, &v2);
+        int trouble = -1;
+        const int e1 = dec_min_of(c, v1, &trouble);
+        int hit = e1 != conn_min[2 * i];
+        if (!hit) hit = dec_min_of(c, v2, &trouble) != conn_min[2 * i + 1];
+        if (hit) {
+            if (ds_edge) ds_edge[nds] = i;
+            if (ds_vert) ds_vert[nds] = trouble;
+            nds++;
+        }
+    }
+    counts[0] = nas;
+    counts[1] = nds;
+}
+
+int orc_path_detect_conn(int W, int H, int D, const int *PV, const int *PE, const int *PF, const int *PT,
+                         const int *QV, const int *QE, const int *QF, const int *QT, int counts[2], int *as_tet,
+                         int *as_cur, int *ds_edge, int *ds_vert) {
+    ctx_t cc;
+    ctx_t *c = &cc;
+    memset(c, 0, sizeof(*c));
+    grid_init(&c->G, W, H, D);
+    c->PV = PV; c->PE = PE; c->PF = PF; c->PT = PT;
+    c->QV = QV; c->QE = QE; c->QF = QF; c->QT = QT;
+    int *cmin = (int *)malloc(sizeof(int) * 2 * (size_t)c->G.E);
+    int *cmax = (int *)malloc(sizeof(int) * 2 * (size_t)c->G.F);
+    conn_prep(c, cmin, cmax);
+    conn_detect(c, cmin, cmax, counts, as_tet, as_cur, ds_edge, ds_vert);
+    free(cmin);
+    free(cmax);
+    return c->oob;
+}
+
 /* fix_as_vpath (type-2 branch; type 1 is never recorded), main_3d.cu:5135-5244 */
 static void fix_as_vpath(ctx_t *c, int t_idx) {
     const grid_t *G = &c->G;
@@ -1381,7 +1559,7 @@ int orc_correct(int W, int H, int D, const double *f, double *g, double rel_eps,
               et = flags[6];
     for (int i = 0; i < 8; i++) stats[i] = 0;
     if (pc == 1) return -1;
-    if (pv == 1 && pg == 0) return -1; /* connectivity mode is not part of the oracle */
+    const int conn = pv == 1 && pg == 0; /* connectivity-mode separatrices */
     if (max_outer <= 0) max_outer = 100000;
     grid_t G;
     grid_init(&G, W, H, D);
@@ -1447,6 +1625,7 @@ int orc_correct(int W, int H, int D, const double *f, double *g, double rel_eps,
     stats[4] = cc4[0]; stats[5] = cc4[1]; stats[6] = cc4[2]; stats[7] = cc4[3];
     for (size_t i = 0; i < V; i++) cnt[i] = 1; /* init_counter runs after the filters */
 
+    int *cmin = NULL, *cmax = NULL;
     int n_as = 1, n_ds = 1, n_wall = 1;
     long long total_ite = 0, cp_ite = 0, rounds = 0;
     const long long round_cap = (long long)max_outer * 64;
@@ -1458,6 +1637,12 @@ int orc_correct(int W, int H, int D, const double *f, double *g, double rel_eps,
     c.PV = PV; c.PE = PE; c.PF = PF; c.PT = PT;
     c.QV = QV; c.QE = QE; c.QF = QF; c.QT = QT;
     c.bound = bound; c.range = range; c.sentinel = sentinel; c.edit_type = et; c.buf = buf;
+    if (conn) { /* main_3d.cu:6566-6582, after the original pairing */
+        cmin = (int *)malloc(sizeof(int) * 2 * (size_t)G.E);
+        cmax = (int *)malloc(sizeof(int) * 2 * (size_t)G.F);
+        conn_prep(&c, cmin, cmax);
+        oob += c.oob;
+    }
 
     while (n_as > 0 || n_ds > 0 || n_wall > 0 || cc4[2] > 0 || cc4[3] > 0 || cc4[0] > 0 || cc4[1] > 0) {
         if (total_ite >= max_outer || rounds >= round_cap) {
@@ -1490,7 +1675,13 @@ int orc_correct(int W, int H, int D, const double *f, double *g, double rel_eps,
         if (pv == 0) break;
         /* separatrix phase, main_3d.cu:6943-7148 */
         int pc2[2] = {0, 0};
-        oob += orc_path_detect(W, H, D, PV, PE, PF, PT, QV, QE, QF, QT, pc2, as_tet, as_cur, ds_e, ds_v);
+        if (conn) {
+            c.oob = 0;
+            conn_detect(&c, cmin, cmax, pc2, as_tet, as_cur, ds_e, ds_v);
+            oob += c.oob;
+        } else {
+            oob += orc_path_detect(W, H, D, PV, PE, PF, PT, QV, QE, QF, QT, pc2, as_tet, as_cur, ds_e, ds_v);
+        }
         n_as = pc2[0];
         n_ds = pc2[1];
         n_wall = 0;
@@ -1505,7 +1696,13 @@ int orc_correct(int W, int H, int D, const double *f, double *g, double rel_eps,
         orc_cp_mismatch(W, H, D, PV, PE, PF, PT, QV, QE, QF, QT, cc4, lmin, lsad, l2s, lmax);
         n_as = n_ds = 0;
         if (cc4[0] == 0 && cc4[1] == 0 && cc4[2] == 0 && cc4[3] == 0) {
-            oob += orc_path_detect(W, H, D, PV, PE, PF, PT, QV, QE, QF, QT, pc2, as_tet, as_cur, ds_e, ds_v);
+            if (conn) {
+                c.oob = 0;
+                conn_detect(&c, cmin, cmax, pc2, as_tet, as_cur, ds_e, ds_v);
+                oob += c.oob;
+            } else {
+                oob += orc_path_detect(W, H, D, PV, PE, PF, PT, QV, QE, QF, QT, pc2, as_tet, as_cur, ds_e, ds_v);
+            }
             n_as = pc2[0];
             n_ds = pc2[1];
         }
@@ -1517,6 +1714,7 @@ int orc_correct(int W, int H, int D, const double *f, double *g, double rel_eps,
     if (cnt_out) memcpy(cnt_out, cnt, sizeof(int) * V);
     free(P); free(Q); free(lmin); free(lsad); free(l2s); free(lmax);
     free(as_tet); free(as_cur); free(ds_e); free(ds_v); free(cnt); free(buf);
+    free(cmin); free(cmax);
     return 0;
 }
 

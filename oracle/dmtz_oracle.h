@@ -92,6 +92,16 @@ int orc_labels(int W, int H, int D, const double *data, int *desc, int *asc, int
 void orc_face_cofaces(int W, int H, int D, int n, const int *faces, int *out2);
 void orc_edge_verts(int W, int H, int D, int n, const int *edges, int *out2);
 
+/* Connectivity-mode separatrix check (preserve_vpath=1, preserve_geometry=0;
+ * get_false_as_vpath_connectivity with the intended per-triangle index and
+ * get_false_ds_vpath_connectivity, main_3d.cu:4613-4835, 4961-5062): records
+ * as orc_path_detect's, ds_vert = the trouble maker (may be -1).  Returns the
+ * number of out-of-bounds events. */
+int orc_path_detect_conn(int W, int H, int D,
+                         const int *PV, const int *PE, const int *PF, const int *PT,
+                         const int *QV, const int *QE, const int *QF, const int *QT,
+                         int counts[2], int *as_tet, int *as_cur, int *ds_edge, int *ds_vert);
+
 /* mask[v] (V bytes) = 1 when a cell anchored at v (componentwise-minimum
  * vertex) is critical in exactly one of the two pairings */
 void orc_mismatch_anchors(int W, int H, int D,

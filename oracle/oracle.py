@@ -46,6 +46,8 @@ def lib():
         L.orc_fix_cp.restype = ctypes.c_int
         L.orc_path_detect.argtypes = [ctypes.c_int] * 3 + [_i32p] * 8 + [_i32p] + [_i32p] * 4
         L.orc_path_detect.restype = ctypes.c_int
+        L.orc_path_detect_conn.argtypes = [ctypes.c_int] * 3 + [_i32p] * 8 + [_i32p] + [_i32p] * 4
+        L.orc_path_detect_conn.restype = ctypes.c_int
         L.orc_correct.argtypes = [ctypes.c_int] * 3 + [_f64p, _f64p, ctypes.c_double, _i32p, ctypes.c_int,
                                                         ctypes.c_int, _i64p, _i32p]
         L.orc_correct.restype = ctypes.c_int
@@ -106,8 +108,9 @@ def fix_cp(f, g, cnt, bound, rng, edit_type, preserve_saddles, P, Q, lists, dims
     return buf, oob
 
 
-def path_detect(P, Q, dims):
-    """Geometry-mode separatrix records: (as_tet, as_cur, ds_edge, ds_vert)."""
+def path_detect(P, Q, dims, connectivity=False):
+    """Separatrix records (as_tet, as_cur, ds_edge, ds_vert, oob) of geometry
+    mode, or of connectivity mode (ds_vert = trouble maker)."""
     W, H, D = dims
     V, E, F, T = counts(dims)
     c = np.zeros(2, np.int32)
@@ -115,7 +118,8 @@ def path_detect(P, Q, dims):
     a_c = np.empty(F, np.int32)
     d_e = np.empty(E, np.int32)
     d_v = np.empty(E, np.int32)
-    oob = lib().orc_path_detect(W, H, D, *P, *Q, c, a_t, a_c, d_e, d_v)
+    fn = lib().orc_path_detect_conn if connectivity else lib().orc_path_detect
+    oob = fn(W, H, D, *P, *Q, c, a_t, a_c, d_e, d_v)
     na, nd = int(c[0]), int(c[1])
     return a_t[:na].copy(), a_c[:na].copy(), d_e[:nd].copy(), d_v[:nd].copy(), oob
 
@@ -132,7 +136,7 @@ def correct(f, g, dims, rel_eps, flags, max_outer=0, threads=1):
     cnt = np.empty(V, np.int32)
     rc = lib().orc_correct(W, H, D, ff, gg, float(rel_eps), fl, int(max_outer), int(threads), st, cnt)
     if rc != 0:
-        raise ValueError("flag combination not supported by the oracle")
+        raise ValueError("flag combination not supported by the oracle (preserve_connectors=1)")
     stats = dict(outer_iterations=int(st[0]), cp_iterations=int(st[1]), oob=int(st[2]), converged=bool(st[3]),
                  initial_mismatch=[int(x) for x in st[4:8]])
     return gg, stats, cnt
