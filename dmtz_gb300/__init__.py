@@ -98,6 +98,9 @@ def load_library(build_if_missing: bool = True):
     L.dmtz_get_tuning.argtypes = [_vp, ctypes.POINTER(_int), ctypes.POINTER(_int)]
     L.dmtz_autotune.argtypes = [_vp, _int, _int, _int, _vp, _vp, _int, ctypes.POINTER(_int), ctypes.POINTER(ctypes.c_double)]
     L.dmtz_device_name.argtypes = [_vp, ctypes.c_char_p, _int]
+    L.dmtz_quantize.argtypes = [_vp, _int, _int, _int, _vp, _vp, _int, ctypes.c_double, ctypes.c_double,
+                                ctypes.c_uint64]
+    L.dmtz_quantize.restype = _int
     L.dmtz_set_list_reserve.argtypes = [_vp, ctypes.c_double, ctypes.c_int64]
     L.dmtz_set_list_reserve.restype = _int
     # learned proposal
@@ -291,6 +294,22 @@ class Context:
 
     def set_tuning(self, shape, blocks_per_sm):
         self._check(self._L.dmtz_set_tuning(self._h, int(shape), int(blocks_per_sm)))
+
+    def quantize(self, f, rel_eps, noise_frac=0.05, seed=0, dims=None):
+        """Decompression model on the GPU (host arrays): SZ-style quantisation of
+        f with bin 2 eps plus seeded noise on a fraction of the vertices,
+        clamped to f +- eps.  Returns g (float64, flat)."""
+        dims = _dims_of(np.asarray(f), dims)
+        ff = _flat(f)
+        gg = np.empty_like(ff)
+        self._check(self._L.dmtz_quantize(self._h, *dims, ff.ctypes.data, gg.ctypes.data, 0, float(rel_eps),
+                                          float(noise_frac), ctypes.c_uint64(int(seed) & (2**64 - 1))))
+        return gg
+
+    def quantize_ptr(self, f_ptr: int, g_ptr: int, dims, rel_eps, noise_frac=0.05, seed=0):
+        """quantize on device buffers (float64)."""
+        self._check(self._L.dmtz_quantize(self._h, *dims, _vp(f_ptr), _vp(g_ptr), 1, float(rel_eps),
+                                          float(noise_frac), ctypes.c_uint64(int(seed) & (2**64 - 1))))
 
     def set_list_reserve(self, fraction=1.0 / 16, min_entries=1 << 20):
         """Initial room of the mismatch lists (fraction of cells, at least

@@ -694,6 +694,34 @@ __global__ void k_check_finite(const double *a, i64 n, int *bad) {
 // =============================================================================
 // host side
 // =============================================================================
+// ----------------------------------------------------- decompression model
+// SZ-style error-bounded quantisation of the original field, done on the GPU
+// (the reference runs an external compressor and reads its output back,
+// main_3d.cu:6331-6356): g = fmin + 2 eps * rint((f - fmin) / (2 eps)); then a
+// fraction `frac` of the vertices gets extra uniform noise in [-eps, eps); then
+// g is clamped into [f - eps, f + eps].  Random numbers are a counter-based
+// hash of (seed, vertex, stream): the splitmix64 finaliser, 53 bits to [0, 1).
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+__device__ __forceinline__ double unit_rand(uint64_t seed, i64 v, int k) {
+    const uint64_t h = mix64(seed + 0x9E3779B97F4A7C15ull * (uint64_t)(2 * v + k + 1));
+    return (double)(h >> 11) * 0x1.0p-53;
+}
+__global__ void k_quantize(i64 V, const double *f, double *g, double fmn, double eps, double frac, uint64_t seed) {
+    const double w = __dmul_rn(2.0, eps);
+    for (i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (i64)gridDim.x * blockDim.x) {
+        const double fv = f[v];
+        double q = w > 0.0 ? __dadd_rn(fmn, __dmul_rn(w, rint(__ddiv_rn(__dsub_rn(fv, fmn), w)))) : fv;
+        if (unit_rand(seed, v, 0) < frac)
+            q = __dadd_rn(q, __dmul_rn(eps, __dsub_rn(__dmul_rn(2.0, unit_rand(seed, v, 1)), 1.0)));
+        const double lo = __dsub_rn(fv, eps), hi = __dadd_rn(fv, eps);
+        g[v] = q < lo ? lo : (q > hi ? hi : q);
+    }
+}
+
 // ----------------------------------------------------- learned-proposal glue
 // Network input per vertex (layout in cnn.cuh) and the mismatch byte mm[v]
 // (criticality of v's own cells differs between the two gradients).
@@ -1879,6 +1907,50 @@ dmtz_status dmtz_correct_learned(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int
                                  dmtz_report *rep, int32_t *edit_counter_out) {
     if (!net) return fail(ctx, DMTZ_ERR_ARG, "null network");
     return correct_impl(ctx, net, W, H, D, orig, decp, on_device, rel_eps, opts, rep, edit_counter_out);
+}
+
+dmtz_status dmtz_quantize(dmtz_ctx *ctx, int W, int H, int D, const double *orig, double *decp, int on_device,
+                          double rel_eps, double noise_frac, uint64_t seed) {
+    Grid g;
+    dmtz_status s = check_dims(ctx, W, H, D, g);
+    if (s != DMTZ_OK) return s;
+    if (!orig || !decp) return fail(ctx, DMTZ_ERR_ARG, "null field");
+    if (!(rel_eps >= 0.0) || !std::isfinite(rel_eps) || !(noise_frac >= 0.0 && noise_frac <= 1.0))
+        return fail(ctx, DMTZ_ERR_ARG, "rel_eps must be finite and >= 0, noise_frac in [0, 1]");
+    CK(cudaSetDevice(ctx->device));
+    if (!ctx->counters) {
+        CK(dalloc(&ctx->counters, 16));
+        CK(dalloc(&ctx->errword, 1));
+    }
+    cudaStream_t st = ctx->stream;
+    const double *fd = orig;
+    double *gd = decp;
+    double *tmp = nullptr;
+    if (!on_device) {  // staging buffers for host fields
+        CK(dalloc(&tmp, 2 * g.V));
+        CK(cudaMemcpyAsync(tmp, orig, sizeof(double) * (size_t)g.V, cudaMemcpyHostToDevice, st));
+        fd = tmp;
+        gd = tmp + g.V;
+    }
+    CK(cudaMemsetAsync(ctx->errword, 0, sizeof(int), st));
+    k_check_finite<<<persistent_grid(), kBlock, 0, st>>>(fd, g.V, ctx->errword);
+    int bad = 0;
+    CK(cudaMemcpyAsync(&bad, ctx->errword, sizeof(int), cudaMemcpyDeviceToHost, st));
+    double mn, mx;
+    if ((s = device_minmax(ctx, fd, g.V, mn, mx)) != DMTZ_OK) {
+        cudaFree(tmp);
+        return s;
+    }
+    if (bad) {
+        cudaFree(tmp);
+        return fail(ctx, DMTZ_ERR_ARG, "input contains NaN or Inf");
+    }
+    k_quantize<<<persistent_grid(), kBlock, 0, st>>>(g.V, fd, gd, mn, (mx - mn) * rel_eps, noise_frac, seed);
+    if (!on_device) CK(cudaMemcpyAsync(decp, gd, sizeof(double) * (size_t)g.V, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    cudaFree(tmp);
+    CK(cudaGetLastError());
+    return DMTZ_OK;
 }
 
 dmtz_status dmtz_features(dmtz_ctx *ctx, int W, int H, int D, const double *orig, const double *decp, int on_device,

@@ -123,13 +123,14 @@ def batch_workload(n: int = 64, seed: int = 2024, lo: int = 32, hi: int = 192):
     return out
 
 
-def power_law_device(dims, seed: int, rel_eps: float, slope: float = -3.0, frac: float = 0.05):
-    """Large synthetic case generated on the GPU (torch is used only as a
+def power_law_device(dims, seed: int, slope: float = -3.0):
+    """Large power-law field generated on the GPU (torch is used only as a
     seeded random-number and FFT toolbox here, for fields too big to build in
-    host memory quickly): the same recipe as power_law + decompress_sz, with
-    torch's CUDA generator instead of numpy's, so the values differ from the
-    host recipe's for the same seed.  Returns (f, g) as float64 device
-    tensors of shape (D*H*W,) and the bound eps = rel_eps x range."""
+    host memory quickly): the recipe of power_law with torch's CUDA generator
+    instead of numpy's, so the values differ from the host recipe's for the
+    same seed.  Returns f as a float64 device tensor of shape (D*H*W,) holding
+    float32 values.  The decompressed field comes from the library's own
+    quantiser (Context.quantize_ptr)."""
     import torch
 
     W, H, D = dims
@@ -147,15 +148,6 @@ def power_law_device(dims, seed: int, rel_eps: float, slope: float = -3.0, frac:
     del amp, k2
     f = torch.fft.irfftn(spec, s=(D, H, W))
     del spec
-    f = ((f - f.min()) / (f.max() - f.min())).reshape(-1)  # float32 values, as the host recipe
-    f = f.double()
-    eps = rel_eps * float(f.max() - f.min())
-    fmin = float(f.min())
-    g = fmin + 2.0 * eps * torch.round((f - fmin) / (2.0 * eps))
-    sel = torch.rand(f.shape, generator=gen, device="cuda", dtype=torch.float32) < frac
-    noise = (torch.rand(f.shape, generator=gen, device="cuda", dtype=torch.float64) * 2.0 - 1.0) * eps
-    g += torch.where(sel, noise, torch.zeros_like(noise))
-    del sel, noise
-    g = torch.minimum(torch.maximum(g, f - eps), f + eps)
+    f = ((f - f.min()) / (f.max() - f.min())).reshape(-1).double()
     torch.cuda.synchronize()
-    return f, g, eps
+    return f

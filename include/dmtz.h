@@ -156,6 +156,16 @@ dmtz_status dmtz_correct(dmtz_ctx *ctx, int W, int H, int D, const double *orig,
 dmtz_status dmtz_labels(dmtz_ctx *ctx, int W, int H, int D, const double *data, int on_device, int32_t *desc,
                         int32_t *asc);
 
+/* Decompression model on the GPU, for benchmarks and training data (the
+ * reference runs an external compressor and reads the result back,
+ * main_3d.cu:6331-6356): decp = SZ-style error-bounded quantisation of orig,
+ * fmin + 2 eps * rint((orig - fmin) / (2 eps)) with eps = rel_eps x range,
+ * plus uniform noise in [-eps, eps) on a fraction noise_frac of the vertices
+ * (a counter-based hash of seed and vertex: the same output for the same
+ * inputs on any GPU), clamped into [orig - eps, orig + eps]. */
+dmtz_status dmtz_quantize(dmtz_ctx *ctx, int W, int H, int D, const double *orig, double *decp, int on_device,
+                          double rel_eps, double noise_frac, uint64_t seed);
+
 /* ---- batching and tuning (no counterpart in the reference, which corrects
  * one field per process run) ---- */
 
