@@ -841,6 +841,9 @@ struct dmtz_ctx {
     std::vector<dmtz_ctx *> pool;  // worker contexts of dmtz_correct_batch
     uint8_t *mm = nullptr;         // mismatch bytes of the learned proposal's features
     i64 capMM = 0;
+    i64 *bnd = nullptr;            // surface anchors of the grid bndW x bndH x bndD (full sweeps)
+    i64 bnd_n = 0, bnd_cap = 0;
+    int bndW = 0, bndH = 0, bndD = 0;
     void *loopctl = nullptr;       // device copy of the graph loop's control block (kept: a
                                    // cudaFree per call would synchronise the whole device)
 };
@@ -991,8 +994,56 @@ void sweep_passes(dmtz_ctx *ctx, const Grid &g, const FieldState &s, const Brick
     ctx->launches += 6;
 }
 
-// the five pairing passes and the criticality pass over a set of bricks
+// the list of the grid's surface anchors, built once per grid shape
+bool surface_list(dmtz_ctx *ctx, const Grid &g) {
+    if (ctx->bnd && ctx->bndW == g.W && ctx->bndH == g.H && ctx->bndD == g.D) return true;
+    const i64 need = std::min<i64>(g.V, 2 * ((i64)g.W * g.H + (i64)g.W * g.D + (i64)g.H * g.D));
+    if (need > ctx->bnd_cap) {
+        cudaFree(ctx->bnd);
+        ctx->bnd = nullptr;
+        ctx->bnd_cap = 0;
+        if (dalloc(&ctx->bnd, need) != cudaSuccess) {
+            cudaGetLastError();
+            ctx->bnd = nullptr;
+            return false;
+        }
+        ctx->bnd_cap = need;
+    }
+    cudaMemsetAsync(ctx->counters + 15, 0, sizeof(unsigned long long), ctx->stream);
+    k_bnd_list<<<grid_for(g.V), kBlock, 0, ctx->stream>>>(g, ctx->bnd, ctx->counters + 15);
+    unsigned long long n = 0;
+    cudaMemcpyAsync(&n, ctx->counters + 15, sizeof(n), cudaMemcpyDeviceToHost, ctx->stream);
+    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return false;
+    ctx->bnd_n = (i64)n;
+    ctx->bndW = g.W;
+    ctx->bndH = g.H;
+    ctx->bndD = g.D;
+    return true;
+}
+
+// the five pairing passes and the criticality pass over a set of bricks; a
+// full sweep runs the grid's surface anchors separately, in dense warps
 void sweep(dmtz_ctx *ctx, const Grid &g, const FieldState &s, const BrickList &bl, i64 nb_max) {
+    if (bl.list == nullptr && surface_list(ctx, g)) {
+        const unsigned gr = sweep_grid(ctx, nb_max);
+        cudaStream_t st = ctx->stream;
+        const i64 *b = ctx->bnd;
+        const i64 nbd = ctx->bnd_n;
+        launch_pass<PASS_VERTEX>(g, s, bl, gr, st, 1);
+        launch_bnd<PASS_VERTEX>(g, s, b, nbd, st);
+        launch_pass<PASS_E2>(g, s, bl, gr, st, 1);
+        launch_bnd<PASS_E2>(g, s, b, nbd, st);
+        launch_pass<PASS_F3>(g, s, bl, gr, st, 1);
+        launch_bnd<PASS_F3>(g, s, b, nbd, st);
+        launch_pass<PASS_E4>(g, s, bl, gr, st, 1);
+        launch_bnd<PASS_E4>(g, s, b, nbd, st);
+        launch_pass<PASS_F5>(g, s, bl, gr, st, 1);
+        launch_bnd<PASS_F5>(g, s, b, nbd, st);
+        launch_pass<PASS_CRIT>(g, s, bl, gr, st, 1);
+        launch_bnd<PASS_CRIT>(g, s, b, nbd, st);
+        ctx->launches += 12;
+        return;
+    }
     const BrickList per_pass[6] = {bl, bl, bl, bl, bl, bl};
     sweep_passes(ctx, g, s, per_pass, nb_max);
 }
@@ -1250,6 +1301,7 @@ void dmtz_ctx_destroy(dmtz_ctx *ctx) {
     cudaSetDevice(ctx->device);
     free_all(ctx);
     cudaFree(ctx->mm);
+    cudaFree(ctx->bnd);
     cudaFree(ctx->loopctl);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -2210,19 +2262,29 @@ dmtz_status dmtz_profile_sweep(dmtz_ctx *ctx, int W, int H, int D, const double 
     i64 nb;
     const BrickList bl = all_bricks(g, ctx->tune_shape, nb);
     const unsigned gr = sweep_grid(ctx, nb);
+    // as a full sweep runs them: each pass's brick kernel, then its surface anchors
+    const int sk = surface_list(ctx, g) ? 1 : 0;
+    const i64 *bd = ctx->bnd;
+    const i64 nbd = sk ? ctx->bnd_n : 0;
     for (int r = 0; r < reps; r++) {
         CK(cudaEventRecord(ev[0], st));
-        launch_pass<PASS_VERTEX>(g, Qs, bl, gr, st);
+        launch_pass<PASS_VERTEX>(g, Qs, bl, gr, st, sk);
+        launch_bnd<PASS_VERTEX>(g, Qs, bd, nbd, st);
         CK(cudaEventRecord(ev[1], st));
-        launch_pass<PASS_E2>(g, Qs, bl, gr, st);
+        launch_pass<PASS_E2>(g, Qs, bl, gr, st, sk);
+        launch_bnd<PASS_E2>(g, Qs, bd, nbd, st);
         CK(cudaEventRecord(ev[2], st));
-        launch_pass<PASS_F3>(g, Qs, bl, gr, st);
+        launch_pass<PASS_F3>(g, Qs, bl, gr, st, sk);
+        launch_bnd<PASS_F3>(g, Qs, bd, nbd, st);
         CK(cudaEventRecord(ev[3], st));
-        launch_pass<PASS_E4>(g, Qs, bl, gr, st);
+        launch_pass<PASS_E4>(g, Qs, bl, gr, st, sk);
+        launch_bnd<PASS_E4>(g, Qs, bd, nbd, st);
         CK(cudaEventRecord(ev[4], st));
-        launch_pass<PASS_F5>(g, Qs, bl, gr, st);
+        launch_pass<PASS_F5>(g, Qs, bl, gr, st, sk);
+        launch_bnd<PASS_F5>(g, Qs, bd, nbd, st);
         CK(cudaEventRecord(ev[5], st));
-        launch_pass<PASS_CRIT>(g, Qs, bl, gr, st);
+        launch_pass<PASS_CRIT>(g, Qs, bl, gr, st, sk);
+        launch_bnd<PASS_CRIT>(g, Qs, bd, nbd, st);
         CK(cudaEventRecord(ev[6], st));
         CK(cudaEventSynchronize(ev[6]));
         for (int k = 0; k < 6; k++) {

@@ -349,8 +349,29 @@ enum { PASS_VERTEX = 0, PASS_E2, PASS_F3, PASS_E4, PASS_F5, PASS_CRIT };
 #define DMTZ_SWEEP_MINB 16
 #endif
 
+// the generic (bounds-checked) version of one pass at one anchor
+template <int PASS>
+__device__ __forceinline__ void pass_at(const Grid &g, const FieldState &s, i64 v, int x, int y, int z) {
+    if (PASS == PASS_VERTEX) pass_vertex_at(g, s, v, x, y, z);
+    else if (PASS == PASS_E2) pass_edge_a2_at(g, s, v, x, y, z);
+    else if (PASS == PASS_F3) pass_face_a3_at(g, s, v, x, y, z);
+    else if (PASS == PASS_E4) pass_edge_a4_at(g, s, v, x, y, z);
+    else if (PASS == PASS_F5) pass_face_a5_at(g, s, v, x, y, z);
+    else {
+        uint32_t tc;
+        s.crit[v] = crit_mask(g, s, v, x, y, z, &tc);
+        if (s.tcode) s.tcode[v] = tc;
+    }
+}
+
+// One pass over the anchors of the listed bricks.  With skip_bnd, anchors on
+// the grid's surface are left to k_sweep_bnd: in a brick that touches the
+// surface, a warp holding both kinds would run the fast and the generic code
+// one after the other (the surface is 2 % of the anchors at 256^3 but its
+// mixed warps cost a quarter of a sweep).
 template <int PASS, int SX, int SY, int SZ>
-__global__ void __launch_bounds__(DMTZ_BRICK, DMTZ_SWEEP_MINB) k_sweep(Grid g, FieldState s, BrickList bl) {
+__global__ void __launch_bounds__(DMTZ_BRICK, DMTZ_SWEEP_MINB) k_sweep(Grid g, FieldState s, BrickList bl,
+                                                                     int skip_bnd) {
     static_assert(SX * SY * SZ == DMTZ_BRICK, "a brick is one block");
     const i64 nb = brick_count(bl);
     const int lx = threadIdx.x % SX, ly = (threadIdx.x / SX) % SY, lz = threadIdx.x / (SX * SY);
@@ -360,8 +381,9 @@ __global__ void __launch_bounds__(DMTZ_BRICK, DMTZ_SWEEP_MINB) k_sweep(Grid g, F
         const int x = bx * SX + lx, y = by * SY + ly, z = bz * SZ + lz;
         if (x >= g.W || y >= g.H || z >= g.D) continue;
         const i64 v = x + (i64)y * g.W + (i64)z * g.WH;
-        const bool interior =
-            g.small && x >= 1 && y >= 1 && z >= 1 && x <= g.W - 2 && y <= g.H - 2 && z <= g.D - 2;
+        const bool inner = x >= 1 && y >= 1 && z >= 1 && x <= g.W - 2 && y <= g.H - 2 && z <= g.D - 2;
+        if (skip_bnd && !inner) continue;
+        const bool interior = g.small && inner;
         const int v32 = (int)v;  // used only when g.small
         if (PASS == PASS_VERTEX) {
             if (interior) fast_vertex(g, s, v32);
@@ -390,16 +412,53 @@ __global__ void __launch_bounds__(DMTZ_BRICK, DMTZ_SWEEP_MINB) k_sweep(Grid g, F
     }
 }
 
+// one pass over a list of surface anchors (dense warps, generic code)
+template <int PASS>
+__global__ void __launch_bounds__(256) k_sweep_bnd(Grid g, FieldState s, const i64 *list, i64 n) {
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+        const i64 v = list[i];
+        int x, y, z;
+        decode_v(g, v, x, y, z);
+        pass_at<PASS>(g, s, v, x, y, z);
+    }
+}
+
+// the anchors on the grid's surface (any coordinate 0 or dim-1), one warp
+// atomic per warp
+__global__ void k_bnd_list(Grid g, i64 *list, unsigned long long *n) {
+    const i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+    bool on = false;
+    if (v < g.V) {
+        int x, y, z;
+        decode_v(g, v, x, y, z);
+        on = x == 0 || y == 0 || z == 0 || x == g.W - 1 || y == g.H - 1 || z == g.D - 1;
+    }
+    const unsigned mask = __ballot_sync(0xffffffffu, on);
+    if (!mask) return;
+    const unsigned lane = threadIdx.x & 31;
+    unsigned long long base = 0;
+    if (lane == (unsigned)(__ffs(mask) - 1)) base = atomicAdd(n, (unsigned long long)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, __ffs(mask) - 1);
+    if (on) list[base + __popc(mask & ((1u << lane) - 1u))] = v;
+}
+
 }  // namespace dmtz
 
 namespace dmtz {
+template <int PASS>
+inline void launch_bnd(const Grid &g, const FieldState &s, const i64 *list, i64 n, cudaStream_t st) {
+    if (n <= 0) return;
+    const unsigned gr = (unsigned)std::min<i64>((n + 255) / 256, 65535);
+    k_sweep_bnd<PASS><<<gr, 256, 0, st>>>(g, s, list, n);
+}
 // launch one pass over a brick list with the list's brick shape
 template <int PASS>
-inline void launch_pass(const Grid &g, const FieldState &s, const BrickList &bl, unsigned grid, cudaStream_t st) {
+inline void launch_pass(const Grid &g, const FieldState &s, const BrickList &bl, unsigned grid, cudaStream_t st,
+                        int skip_bnd = 0) {
     switch (bl.shape) {
-    case 1: k_sweep<PASS, 16, 4, 2><<<grid, DMTZ_BRICK, 0, st>>>(g, s, bl); break;
-    case 2: k_sweep<PASS, 32, 2, 2><<<grid, DMTZ_BRICK, 0, st>>>(g, s, bl); break;
-    default: k_sweep<PASS, 8, 4, 4><<<grid, DMTZ_BRICK, 0, st>>>(g, s, bl); break;
+    case 1: k_sweep<PASS, 16, 4, 2><<<grid, DMTZ_BRICK, 0, st>>>(g, s, bl, skip_bnd); break;
+    case 2: k_sweep<PASS, 32, 2, 2><<<grid, DMTZ_BRICK, 0, st>>>(g, s, bl, skip_bnd); break;
+    default: k_sweep<PASS, 8, 4, 4><<<grid, DMTZ_BRICK, 0, st>>>(g, s, bl, skip_bnd); break;
     }
 }
 }  // namespace dmtz
