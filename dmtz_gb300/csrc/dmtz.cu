@@ -513,6 +513,51 @@ __global__ void k_conn_as(Grid g, const uint32_t *critP, const uint32_t *critQ, 
     }
 }
 
+// k_path_as split in two for parallelism: one thread per (2-saddle, coface)
+// walks (res = the first differing tetrahedron, -1 none, -2 no coface), then
+// one thread per 2-saddle keeps the first coface in search order that has
+// one: the same records.
+__global__ void k_path_as_walk(Grid g, const i64 *sad2, const unsigned long long *nsad, const uint32_t *tcP,
+                               const uint32_t *tcQ, const uint8_t *succ, i64 *res, i64 cap, int *err) {
+    const i64 n = 2 * (i64)*nsad;
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+        const i64 code = sad2[i >> 1];
+        const int j = (int)(i & 1);
+        const i64 v = code / 12;
+        const int sl = (int)(code % 12);
+        i64 r = -2;
+        if (j < TOPO_FACE_NCOF[sl]) {
+            int x, y, z;
+            decode_v(g, v, x, y, z);
+            const signed char *tc = TOPO_FACE_COF[sl][j];
+            const int cx = x + tc[0], cy = y + tc[1], cz = z + tc[2], cs = tc[3];
+            if (cell_ok(g, cx, cy, cz, 1, 1, 1)) {
+                i64 cur;
+                r = first_diff(g, tcP, tcQ, succ, cx, cy, cz, cs, cap, err, cur) ? cur : -1;
+            }
+        }
+        res[i] = r;
+    }
+}
+__global__ void k_path_as_pick(Grid g, const i64 *sad2, const unsigned long long *nsad, const i64 *res, PathRec R) {
+    const i64 n = (i64)*nsad;
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+        const int j = res[2 * i] >= 0 ? 0 : (res[2 * i + 1] >= 0 ? 1 : -1);
+        if (j < 0) continue;
+        const i64 code = sad2[i];
+        const i64 v = code / 12;
+        const int sl = (int)(code % 12);
+        int x, y, z;
+        decode_v(g, v, x, y, z);
+        const signed char *tc = TOPO_FACE_COF[sl][j];
+        const unsigned long long at = atomicAdd(&R.n[0], 1ull);
+        if ((i64)at < R.cap_as) {
+            R.as_tet[at] = tet_ref(g, x + tc[0], y + tc[1], z + tc[2], tc[3]);
+            R.as_cur[at] = res[2 * i + j];
+        }
+    }
+}
+
 __global__ void k_fix_path(RuleCtx c, PathRec R) {
     const i64 na = min((i64)R.n[0], R.cap_as), nd = min((i64)R.n[1], R.cap_ds);
     for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < na + nd; i += (i64)gridDim.x * blockDim.x) {
@@ -830,6 +875,7 @@ struct dmtz_ctx {
     uint32_t *brick_list = nullptr;   // compacted lists per radius, capB entries each
     unsigned long long *brick_n = nullptr;  // their lengths
     i64 *sad2 = nullptr;      // original 2-saddle triangles
+    i64 *as_res = nullptr;    // per (2-saddle, coface) walk results, 2 x capSad2
     unsigned long long *counters = nullptr;  // [0..3] cp lists, [4] requests, [5,6] paths, [8,9] min/max
                                              // keys, [10] original 2-saddles, [11] dirty bricks,
                                              // [12] edited vertices
@@ -879,6 +925,8 @@ void free_all(dmtz_ctx *c) {
     cudaFree(c->as_tet); cudaFree(c->as_cur); cudaFree(c->ds_edge); cudaFree(c->ds_vert);
     cudaFree(c->counters); cudaFree(c->errword); cudaFree(c->changed);
     cudaFree(c->succ); cudaFree(c->sad2); cudaFree(c->brick_flags); cudaFree(c->brick_list);
+    cudaFree(c->as_res);
+    c->as_res = nullptr;
     cudaFree(c->brick_n);
     c->brick_n = nullptr;
     c->succ = nullptr; c->sad2 = nullptr; c->brick_flags = nullptr; c->brick_list = nullptr;
@@ -1197,11 +1245,13 @@ dmtz_status prep_paths(dmtz_ctx *ctx, const Grid &g) {
         cudaFree(ctx->as_tet);
         cudaFree(ctx->as_cur);
         cudaFree(ctx->sad2);
-        ctx->as_tet = ctx->as_cur = ctx->sad2 = nullptr;
+        cudaFree(ctx->as_res);
+        ctx->as_tet = ctx->as_cur = ctx->sad2 = ctx->as_res = nullptr;
         ctx->capAS = ctx->capSad2 = 0;
         CK(dalloc(&ctx->as_tet, (i64)n[1]));
         CK(dalloc(&ctx->as_cur, (i64)n[1]));
         CK(dalloc(&ctx->sad2, (i64)n[1]));
+        CK(dalloc(&ctx->as_res, 2 * (i64)n[1]));
         ctx->capAS = ctx->capSad2 = (i64)n[1];
     }
     // buffers exist even when a count is 0 (kernels take their addresses)
@@ -1213,6 +1263,7 @@ dmtz_status prep_paths(dmtz_ctx *ctx, const Grid &g) {
         CK(dalloc(&ctx->as_tet, 1));
         CK(dalloc(&ctx->as_cur, 1));
         CK(dalloc(&ctx->sad2, 1));
+        CK(dalloc(&ctx->as_res, 2));
     }
     CK(cudaMemsetAsync(ctx->counters + 10, 0, sizeof(unsigned long long), st));
     k_path_succ<<<grid_for(g.V), kBlock, 0, st>>>(g, ctx->P.tcode, ctx->succ);
@@ -1233,14 +1284,15 @@ void launch_detect(dmtz_ctx *ctx, const Grid &g, const RuleCtx &rc, const PathRe
                                            g.T + 16, ctx->errword);
         k_conn_ds<<<grid, kBlock, 0, st>>>(rc, R, g.V + 16);
     } else {
-        k_path_as<<<grid, kBlock, 0, st>>>(g, ctx->sad2, ctx->counters + 10, ctx->P.tcode, ctx->Q.tcode, ctx->succ,
-                                           R, g.T + 16, ctx->errword);
+        k_path_as_walk<<<2 * grid, kBlock, 0, st>>>(g, ctx->sad2, ctx->counters + 10, ctx->P.tcode, ctx->Q.tcode,
+                                                    ctx->succ, ctx->as_res, g.T + 16, ctx->errword);
+        k_path_as_pick<<<grid, kBlock, 0, st>>>(g, ctx->sad2, ctx->counters + 10, ctx->as_res, R);
         k_path_ds<<<grid, kBlock, 0, st>>>(rc, R);
     }
 }
 void detect_paths(dmtz_ctx *ctx, const Grid &g, const RuleCtx &rc, const PathRec &R, unsigned grid, int conn = 0) {
     launch_detect(ctx, g, rc, R, grid, conn);
-    ctx->launches += 2;
+    ctx->launches += conn ? 2 : 3;
 }
 
 unsigned persistent_grid() {
@@ -1839,8 +1891,9 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
             }
             pt_.end();
             // kernels per body run: switch + control, plus each state's own
+            const int64_t det = conn ? 2 : 3;  // separatrix detection kernels
             ctx->launches += 2 * (fin.runs[0] + fin.runs[1] + fin.runs[2] + fin.runs[3]) + 11 * fin.runs[LS_CP] +
-                             13 * fin.runs[LS_PDF] + 2 * fin.runs[LS_PCHECK] + 11 * fin.runs[LS_PFIX];
+                             (11 + det) * fin.runs[LS_PDF] + det * fin.runs[LS_PCHECK] + 11 * fin.runs[LS_PFIX];
         }
         R.outer_iterations = fin.outer;
         R.cp_rounds = fin.cp_rounds;
