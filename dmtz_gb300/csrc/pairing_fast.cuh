@@ -1,7 +1,7 @@
 // pairing_fast.cuh — interior fast path of the pairing passes.
 //
 // An anchor at 1 <= x,y,z <= dim-2 owns all 26 of its cells and every vertex
-// its passes look at (offsets -1..2) exists, so no bounds test is needed.
+// its passes look at (offsets -1..1) exists, so no bounds test is needed.
 // Vertex indices are 32-bit here (grids below 2^31 vertices, Grid::small):
 // half the integer work of 64-bit ids in the address and tie-break
 // arithmetic, which dominates these instruction-bound passes.
@@ -341,12 +341,12 @@ __device__ __forceinline__ void fast_crit(const Grid &g, const FieldState &s, in
 // ---------------------------------------------------------------- brick sweep
 enum { PASS_VERTEX = 0, PASS_E2, PASS_F3, PASS_E4, PASS_F5, PASS_CRIT };
 
-// minimum resident blocks per SM the sweep kernels are compiled for: 16
-// blocks of 128 threads fill an SM and cap the kernels at 32 registers.  The
-// passes are latency- and issue-bound; full occupancy beats the few spills
-// this causes (sweep 6.9 -> 5.9 ms at 256^3 on GB300).
+// minimum resident blocks per SM the sweep kernels are compiled for: 12
+// blocks of 128 threads cap them at 40 registers.  Measured on GB300 at 256^3
+// (staged kernels): 16 blocks / 32 registers spill and take 4.98 ms per sweep,
+// 12 / 40 take 4.56 ms, 10 / 48 4.68 ms, 8 / 64 4.89 ms.
 #ifndef DMTZ_SWEEP_MINB
-#define DMTZ_SWEEP_MINB 16
+#define DMTZ_SWEEP_MINB 12
 #endif
 
 // the generic (bounds-checked) version of one pass at one anchor
@@ -364,50 +364,131 @@ __device__ __forceinline__ void pass_at(const Grid &g, const FieldState &s, i64 
     }
 }
 
+// ------------------------------------------------------------- staged sweep
 // One pass over the anchors of the listed bricks.  With skip_bnd, anchors on
 // the grid's surface are left to k_sweep_bnd: in a brick that touches the
 // surface, a warp holding both kinds would run the fast and the generic code
 // one after the other (the surface is 2 % of the anchors at 256^3 but its
 // mixed warps cost a quarter of a sweep).
+//
+// The interior passes read only anchors at offsets -1..1 (the corner, third-
+// and fourth-vertex, edge- and face-anchor tables all stay in that range), so
+// a brick's inputs are its anchors plus a one-anchor halo.  k_sweep_sm copies
+// the pass's input arrays for that box into shared memory (box rows are
+// contiguous in HBM), runs the fast path on box indices -- a Grid whose row
+// and plane strides are the box's, so every neighbour offset is a
+// compile-time constant -- into box-sized shared output arrays, and writes
+// its anchors' outputs back.  Shared-memory latency replaces the L1/L2
+// latency of the neighbour loads that stalled the passes.
+template <int BX, int BY>
+__device__ __forceinline__ Grid box_grid() {
+    Grid b;
+    b.W = BX;
+    b.H = BY;
+    b.D = 1;
+    b.WH = BX * BY;
+    b.small = 1;
+    b.WHi = BX * BY;
+    DMTZ_FOR(14, I, {
+        constexpr int i = decltype(I)::value;
+        constexpr int d = cxt::TOPO_DIRS[i][0] + cxt::TOPO_DIRS[i][1] * BX + cxt::TOPO_DIRS[i][2] * BX * BY;
+        b.doff32[i] = d;
+    });
+#pragma unroll
+    for (int c8 = 0; c8 < 8; c8++) b.coff32[c8] = (c8 & 1) + ((c8 >> 1) & 1) * BX + ((c8 >> 2) & 1) * BX * BY;
+    return b;
+}
+
 template <int PASS, int SX, int SY, int SZ>
-__global__ void __launch_bounds__(DMTZ_BRICK, DMTZ_SWEEP_MINB) k_sweep(Grid g, FieldState s, BrickList bl,
-                                                                     int skip_bnd) {
+__global__ void __launch_bounds__(DMTZ_BRICK, DMTZ_SWEEP_MINB) k_sweep_sm(Grid g, FieldState s, BrickList bl,
+                                                                        int skip_bnd) {
     static_assert(SX * SY * SZ == DMTZ_BRICK, "a brick is one block");
-    const i64 nb = brick_count(bl);
+    constexpr int BX = SX + 2, BY = SY + 2, BZ = SZ + 2, NB = BX * BY * BZ;
+    // pass: inputs -> outputs (shared arrays)
+    //   0: val -> key low pv        1: low pv key -> ea2 (a)
+    //   2: low key ea2 (a) -> fa3 (b) fp3 (c)
+    //   3: ea2 (a) low pv key fp3 (c) -> eup (b)
+    //   4: eup (a) fa3 (b) fp3 (c) low key -> fup (d)
+    //   5: pv eup (a) fup (b) -> crit (d) tcode (e)
+    constexpr bool K = PASS <= 4, L = PASS <= 4, PV = PASS != 2 && PASS != 4, A = PASS >= 1, B = PASS >= 2,
+                   C = PASS >= 2 && PASS <= 4, DD = PASS >= 4, E = PASS == 5, VAL = PASS == 0;
+    __shared__ uint64_t sh_key[K ? NB : 1];
+    __shared__ double sh_val[VAL ? NB : 1];
+    __shared__ uint16_t sh_low[L ? NB : 1];
+    __shared__ uint8_t sh_pv[PV ? NB : 1];
+    __shared__ uint32_t sh_a[A ? NB : 1];
+    __shared__ uint32_t sh_b[B ? NB : 1];
+    __shared__ uint16_t sh_c[C ? NB : 1];
+    __shared__ uint32_t sh_d[DD ? NB : 1];
+    __shared__ uint32_t sh_e[E ? NB : 1];
+    const Grid gb = box_grid<BX, BY>();
+    FieldState t;  // box views of the pass's inputs and outputs
+    t.val = sh_val;
+    t.key = sh_key;
+    t.low = sh_low;
+    t.pv = sh_pv;
+    t.ea2 = sh_a;
+    t.fa3 = sh_b;
+    t.fp3 = sh_c;
+    t.eup = PASS == 3 ? sh_b : sh_a;
+    t.fup = PASS == 4 ? sh_d : sh_b;
+    t.crit = sh_d;
+    t.tcode = (PASS == 5 && s.tcode) ? sh_e : nullptr;
     const int lx = threadIdx.x % SX, ly = (threadIdx.x / SX) % SY, lz = threadIdx.x / (SX * SY);
-    for (i64 b = blockIdx.x; b < nb; b += gridDim.x) {
+    const int li = (lx + 1) + BX * ((ly + 1) + BY * (lz + 1));  // this thread's anchor in the box
+    const i64 nbr = brick_count(bl);
+    for (i64 b = blockIdx.x; b < nbr; b += gridDim.x) {
         int bx, by, bz;
         brick_coords(bl, b, bx, by, bz);
-        const int x = bx * SX + lx, y = by * SY + ly, z = bz * SZ + lz;
-        if (x >= g.W || y >= g.H || z >= g.D) continue;
-        const i64 v = x + (i64)y * g.W + (i64)z * g.WH;
-        const bool inner = x >= 1 && y >= 1 && z >= 1 && x <= g.W - 2 && y <= g.H - 2 && z <= g.D - 2;
-        if (skip_bnd && !inner) continue;
-        const bool interior = g.small && inner;
-        const int v32 = (int)v;  // used only when g.small
-        if (PASS == PASS_VERTEX) {
-            if (interior) fast_vertex(g, s, v32);
-            else pass_vertex_at(g, s, v, x, y, z);
-        } else if (PASS == PASS_E2) {
-            if (interior) fast_edge_a2(g, s, v32);
-            else pass_edge_a2_at(g, s, v, x, y, z);
-        } else if (PASS == PASS_F3) {
-            if (interior) fast_face_a3(g, s, v32);
-            else pass_face_a3_at(g, s, v, x, y, z);
-        } else if (PASS == PASS_E4) {
-            if (interior) fast_edge_a4(g, s, v32);
-            else pass_edge_a4_at(g, s, v, x, y, z);
-        } else if (PASS == PASS_F5) {
-            if (interior) fast_face_a5(g, s, v32);
-            else pass_face_a5_at(g, s, v, x, y, z);
-        } else {
-            if (interior) {
-                fast_crit(g, s, v32);
-            } else {
-                uint32_t tc;
-                s.crit[v] = crit_mask(g, s, v, x, y, z, &tc);
-                if (s.tcode) s.tcode[v] = tc;
+        const int x0 = bx * SX, y0 = by * SY, z0 = bz * SZ;
+        __syncthreads();  // the previous brick's readers are done
+        for (int e = threadIdx.x; e < NB; e += DMTZ_BRICK) {
+            const int ux = x0 - 1 + e % BX, uy = y0 - 1 + (e / BX) % BY, uz = z0 - 1 + e / (BX * BY);
+            const bool in = ux >= 0 && uy >= 0 && uz >= 0 && ux < g.W && uy < g.H && uz < g.D;
+            const i64 u = in ? ux + (i64)uy * g.W + (i64)uz * g.WH : 0;
+            if (VAL) sh_val[e] = in ? s.val[u] : 0.0;
+            if (PASS >= 1 && PASS <= 4) {
+                sh_low[e] = in ? s.low[u] : (uint16_t)0;
+                sh_key[e] = in ? s.key[u] : 0ull;
             }
+            if (PASS == 1 || PASS == 3 || PASS == 5) sh_pv[e] = in ? s.pv[u] : (uint8_t)15;
+            if (PASS == 2 || PASS == 3) sh_a[e] = in ? s.ea2[u] : 0u;
+            if (PASS == 4 || PASS == 5) sh_a[e] = in ? s.eup[u] : 0u;
+            if (PASS == 3 || PASS == 4) sh_c[e] = in ? s.fp3[u] : (uint16_t)0;
+            if (PASS == 4) sh_b[e] = in ? s.fa3[u] : 0u;
+            if (PASS == 5) sh_b[e] = in ? s.fup[u] : 0u;
+        }
+        __syncthreads();
+        const int x = x0 + lx, y = y0 + ly, z = z0 + lz;
+        const bool ingrid = x < g.W && y < g.H && z < g.D;
+        const bool inner = ingrid && x >= 1 && y >= 1 && z >= 1 && x <= g.W - 2 && y <= g.H - 2 && z <= g.D - 2;
+        const i64 v = x + (i64)y * g.W + (i64)z * g.WH;
+        if (inner) {
+            if (PASS == 0) {
+                fast_vertex(gb, t, li);
+                s.key[v] = sh_key[li];
+                s.low[v] = sh_low[li];
+                s.pv[v] = sh_pv[li];
+            } else if (PASS == 1) {
+                fast_edge_a2(gb, t, li);
+                s.ea2[v] = sh_a[li];
+            } else if (PASS == 2) {
+                fast_face_a3(gb, t, li);
+                s.fa3[v] = sh_b[li];
+                s.fp3[v] = sh_c[li];
+            } else if (PASS == 3) {
+                fast_edge_a4(gb, t, li);
+                s.eup[v] = sh_b[li];
+            } else if (PASS == 4) {
+                fast_face_a5(gb, t, li);
+                s.fup[v] = sh_d[li];
+            } else {
+                fast_crit(gb, t, li);
+                s.crit[v] = sh_d[li];
+                if (s.tcode) s.tcode[v] = sh_e[li];
+            }
+        } else if (ingrid && !skip_bnd) {
+            pass_at<PASS>(g, s, v, x, y, z);
         }
     }
 }
@@ -456,9 +537,9 @@ template <int PASS>
 inline void launch_pass(const Grid &g, const FieldState &s, const BrickList &bl, unsigned grid, cudaStream_t st,
                         int skip_bnd = 0) {
     switch (bl.shape) {
-    case 1: k_sweep<PASS, 16, 4, 2><<<grid, DMTZ_BRICK, 0, st>>>(g, s, bl, skip_bnd); break;
-    case 2: k_sweep<PASS, 32, 2, 2><<<grid, DMTZ_BRICK, 0, st>>>(g, s, bl, skip_bnd); break;
-    default: k_sweep<PASS, 8, 4, 4><<<grid, DMTZ_BRICK, 0, st>>>(g, s, bl, skip_bnd); break;
+    case 1: k_sweep_sm<PASS, 16, 4, 2><<<grid, DMTZ_BRICK, 0, st>>>(g, s, bl, skip_bnd); break;
+    case 2: k_sweep_sm<PASS, 32, 2, 2><<<grid, DMTZ_BRICK, 0, st>>>(g, s, bl, skip_bnd); break;
+    default: k_sweep_sm<PASS, 8, 4, 4><<<grid, DMTZ_BRICK, 0, st>>>(g, s, bl, skip_bnd); break;
     }
 }
 }  // namespace dmtz
