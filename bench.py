@@ -328,13 +328,15 @@ def run_batch(args):
         t1 = time.perf_counter()
         out = ctx.correct_batch(fields, workers=workers, max_rounds=args.max_rounds)
         dt = time.perf_counter() - t1
-        res[workers] = (dt, sum(1 for o in out if o[1]["converged"]))
+        res[workers] = (dt, sum(1 for o in out if o[1]["converged"]), sum(o[1]["stall_breaks"] for o in out),
+                        sum(1 for o in out if o[1]["stall_breaks"]))
     line = {"metric": "Mvox/s, 64-field uneven batch corrected in one call (full-MSC flags)",
             "value": vox / res[8][0] / 1e6, "unit": "Mvox/s", "n_gpus": 1, "steps": 1, "warmup": 1,
             "ms_per_step": res[8][0] * 1e3, "higher_is_better": True, "dtype": "f64", "data": "synthetic",
             "config": {"workload": "64 fields, dims U{32..192}^3, f32/f64 alternating, gauss/powerlaw, "
                                    "eps in {1e-2,1e-3,1e-4} x range", "voxels": int(vox), "workers": 8,
-                       "converged": res[8][1], "max_rounds": args.max_rounds, "tuning": [shape, bps],
+                       "converged": res[8][1], "stall_breaks": res[8][2], "fields_with_stall_breaks": res[8][3],
+                       "max_rounds": args.max_rounds, "tuning": [shape, bps],
                        "one_worker_s": res[1][0], "overlap_speedup": res[1][0] / res[8][0],
                        "generation_s": gen_s}}
     print(json.dumps(line), flush=True)
@@ -489,8 +491,8 @@ def run_big(args):
                        "wall_s": wall, "converged": rep["converged"], "within_bound": within,
                        "outer_iterations": rep["outer_iterations"], "cp_rounds": rep["cp_rounds"],
                        "path_rounds": rep["path_rounds"], "initial_mismatch": rep["initial_mismatch"],
-                       "final_mismatch": rep["final_mismatch"], "phase_ms": rep["phase_ms"],
-                       "context_device_gb": (free0 - free1) / 1e9, "device_total_gb": total / 1e9,
+                       "final_mismatch": rep["final_mismatch"], "stall_breaks": rep["stall_breaks"],
+                       "phase_ms": rep["phase_ms"], "context_device_gb": (free0 - free1) / 1e9, "device_total_gb": total / 1e9,
                        "bytes_per_vertex": (free0 - free1) / V}}
     print(json.dumps(line), flush=True)
     ctx.close()

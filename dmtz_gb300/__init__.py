@@ -37,7 +37,7 @@ class DmtzError(RuntimeError):
 class Opts(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int) for n in (
         "preserve_saddles", "preserve_vpath", "preserve_geometry", "filtration", "preserve_connectors",
-        "preserve_type", "edit_type", "max_rounds", "use_graph")]
+        "preserve_type", "edit_type", "max_rounds", "use_graph", "break_stalls")]
 
 
 class Report(ctypes.Structure):
@@ -45,7 +45,8 @@ class Report(ctypes.Structure):
                 ("initial_mismatch", ctypes.c_int64 * 4), ("final_mismatch", ctypes.c_int64 * 4),
                 ("final_paths", ctypes.c_int64 * 2), ("edited_vertices", ctypes.c_int64),
                 ("converged", ctypes.c_int32), ("error_flags", ctypes.c_int32), ("seconds", ctypes.c_double),
-                ("kernel_launches", ctypes.c_int64), ("phase_ms", ctypes.c_double * 6)]
+                ("kernel_launches", ctypes.c_int64), ("phase_ms", ctypes.c_double * 6),
+                ("stall_breaks", ctypes.c_int64)]
 
     PHASES = ("pairing", "fix_cp", "path_detect", "fix_path", "apply", "setup")
 
@@ -55,6 +56,7 @@ class Report(ctypes.Structure):
                     final_paths=list(self.final_paths), edited_vertices=self.edited_vertices,
                     converged=bool(self.converged),
                     error_flags=self.error_flags, seconds=self.seconds, kernel_launches=self.kernel_launches,
+                    stall_breaks=self.stall_breaks,
                     phase_ms=dict(zip(self.PHASES, [round(x, 4) for x in self.phase_ms])))
 
 
@@ -243,14 +245,14 @@ class Context:
         return at[:na].copy(), ac[:na].copy(), de[:nd].copy(), dv[:nd].copy()
 
     def correct(self, f, g, rel_eps, flags=(1, 1, 1, 0, 0, 0, 0), dims=None, max_rounds=0, use_graph=0,
-                return_counter=False):
+                return_counter=False, break_stalls=True):
         """Full correction of g against f.  Returns (corrected g, report dict[, edit counter])."""
         dims = _dims_of(np.asarray(f), dims)
         ff = _flat(f)
         gg = np.array(_flat(g), copy=True)
         V = ff.size
         cnt = np.empty(V, np.int32)
-        o = Opts(*[int(x) for x in flags], int(max_rounds), int(use_graph))
+        o = Opts(*[int(x) for x in flags], int(max_rounds), int(use_graph), int(bool(break_stalls)))
         r = Report()
         rc = self._L.dmtz_correct(self._h, *dims, ff.ctypes.data, gg.ctypes.data, 0, float(rel_eps),
                                   ctypes.byref(o), ctypes.byref(r), cnt.ctypes.data)
@@ -259,7 +261,8 @@ class Context:
         rep["edited_vertices"] = int((gg != _flat(g)).sum())
         return (gg, rep, cnt) if return_counter else (gg, rep)
 
-    def correct_batch(self, fields, flags=(1, 1, 1, 0, 0, 0, 0), workers=8, max_rounds=0, use_graph=1):
+    def correct_batch(self, fields, flags=(1, 1, 1, 0, 0, 0, 0), workers=8, max_rounds=0, use_graph=1,
+                      break_stalls=True):
         """Correct many fields of any sizes in one call.
 
         fields: iterable of (f, g, rel_eps) with f, g float32 or float64 arrays of
@@ -282,7 +285,7 @@ class Context:
         arr = (Instance * max(n, 1))(*insts)
         reps = (Report * max(n, 1))()
         sts = np.zeros(max(n, 1), np.int32)
-        o = Opts(*[int(x) for x in flags], int(max_rounds), int(use_graph))
+        o = Opts(*[int(x) for x in flags], int(max_rounds), int(use_graph), int(bool(break_stalls)))
         self._L.dmtz_correct_batch(self._h, n, ctypes.cast(arr, ctypes.c_void_p), ctypes.byref(o),
                                    ctypes.cast(reps, ctypes.c_void_p), sts.ctypes.data, int(workers))
         return [(outs[i], reps[i].as_dict(), int(sts[i])) for i in range(n)]
@@ -332,12 +335,12 @@ class Context:
         return best[0], best[1], ms.value
 
     def correct_ptr(self, f_ptr: int, g_ptr: int, dims, rel_eps, flags=(1, 1, 1, 0, 0, 0, 0), on_device=True,
-                    max_rounds=0, use_graph=0, allow_nonconverged=False):
+                    max_rounds=0, use_graph=0, allow_nonconverged=False, break_stalls=True):
         """Correction on raw float64 buffers (device pointers when on_device, else host
         pointers, e.g. pinned memory); g is edited in place.  With
         allow_nonconverged, hitting max_rounds returns the report (converged
         False) instead of raising."""
-        o = Opts(*[int(x) for x in flags], int(max_rounds), int(use_graph))
+        o = Opts(*[int(x) for x in flags], int(max_rounds), int(use_graph), int(bool(break_stalls)))
         r = Report()
         self._check(self._L.dmtz_correct(self._h, *dims, _vp(f_ptr), _vp(g_ptr), int(bool(on_device)),
                                          float(rel_eps), ctypes.byref(o), ctypes.byref(r), None),
@@ -359,22 +362,23 @@ class Context:
                                           float(rel_eps), _vp(feat_ptr), _vp(active_ptr)))
 
     def correct_learned(self, net, f, g, rel_eps, flags=(1, 1, 1, 0, 0, 0, 0), dims=None, max_rounds=0,
-                        use_graph=0):
+                        use_graph=0, break_stalls=True):
         """Correction started from the network's proposal (host arrays).
         Returns (corrected g, report dict)."""
         dims = _dims_of(np.asarray(f), dims)
         ff = _flat(f)
         gg = np.array(_flat(g), copy=True)
-        o = Opts(*[int(x) for x in flags], int(max_rounds), int(use_graph))
+        o = Opts(*[int(x) for x in flags], int(max_rounds), int(use_graph), int(bool(break_stalls)))
         r = Report()
         self._check(self._L.dmtz_correct_learned(self._h, net._h, *dims, ff.ctypes.data, gg.ctypes.data, 0,
                                                  float(rel_eps), ctypes.byref(o), ctypes.byref(r), None))
         return gg, r.as_dict()
 
     def correct_learned_ptr(self, net, f_ptr: int, g_ptr: int, dims, rel_eps, flags=(1, 1, 1, 0, 0, 0, 0),
-                            on_device=True, max_rounds=0, use_graph=0, allow_nonconverged=False):
+                            on_device=True, max_rounds=0, use_graph=0, allow_nonconverged=False,
+                            break_stalls=True):
         """correct_learned on raw float64 buffers (g edited in place)."""
-        o = Opts(*[int(x) for x in flags], int(max_rounds), int(use_graph))
+        o = Opts(*[int(x) for x in flags], int(max_rounds), int(use_graph), int(bool(break_stalls)))
         r = Report()
         self._check(self._L.dmtz_correct_learned(self._h, net._h, *dims, _vp(f_ptr), _vp(g_ptr),
                                                  int(bool(on_device)), float(rel_eps), ctypes.byref(o),

@@ -586,16 +586,113 @@ __global__ void k_apply(RuleCtx c, double range, int preserve_type, int update, 
         if (!req || !update) continue;
         const double f = c.f[v];
         const double gv = g[v];
+        const int cv = cnt[v];
         const double lowb = __dsub_rn(f, c.bound);
-        if (preserve_type == 0 && fabs(d) > tiny && cnt[v] < 5 && fabs(__dsub_rn(f, __dadd_rn(gv, d))) <= c.bound) {
+        if (preserve_type == 0 && fabs(d) > tiny && cv < 5 && fabs(__dsub_rn(f, __dadd_rn(gv, d))) <= c.bound) {
             g[v] = __dadd_rn(gv, d);
-            cnt[v] += 1;
+            cnt[v] = cv + 1;
+            if (c.progress) *c.progress = 1ull;
         } else {
             cnt[v] = 6;
             g[v] = lowb;
+            if (c.progress && (cv != 6 || gv != lowb)) *c.progress = 1ull;
         }
         if (changed) changed[v] = 1;
     }
+}
+
+// ------------------------------------------------------------- stall breaker
+// A round whose update changes no value and no edit counter leaves the state
+// as it was, so the reference's loop repeats it forever (main_3d.cu:6784 has
+// no exit for this; e.g. a false extremum no rule addresses, or requests on
+// vertices already at f - bound).  With break_stalls, such a round instead
+// sets every vertex within `radius` (per axis) of a vertex of a remaining
+// mismatched cell -- or of a separatrix record's tetrahedron or vertex -- back
+// to its original value, which is always within the bound, and requests it so
+// that the next re-pairing covers it; then the loop goes on.  Rounds that make
+// progress are never touched, so runs that converge under the reference's
+// rules give the reference's output.
+//
+// The region is built in spare bits of the per-vertex `changed` bytes (bit 0
+// is the edit mark): seeds get bit 1, three separable line dilations grow it
+// to the box of half-width `radius` around every seed, and k_snap_mask resets
+// the region and clears the bits.  Seed writers all store (bit 0 | 2) to the
+// byte, and bit 0 does not change meanwhile, so unordered writes agree.
+constexpr uint8_t kSnapSeed = 2, kSnapGrow = 4;
+__device__ __forceinline__ void seed_vertex(const Grid &g, uint8_t *m, i64 v) {
+    if (v >= 0 && v < g.V) m[v] = (uint8_t)(m[v] | kSnapSeed);
+}
+__global__ void k_seed_cells(Grid g, CpLists L, uint8_t *m) {
+    const i64 n0 = min((i64)L.n[0], L.cap[0]), n1 = min((i64)L.n[1], L.cap[1]), n2 = min((i64)L.n[2], L.cap[2]),
+              n3 = min((i64)L.n[3], L.cap[3]);
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n0 + n1 + n2 + n3; i += (i64)gridDim.x * blockDim.x) {
+        i64 vs[4] = {-1, -1, -1, -1};
+        if (i < n0) {
+            vs[0] = L.l[0][i];
+        } else if (i < n0 + n1) {
+            edge_verts(g, L.l[1][i - n0], vs[0], vs[1]);
+        } else if (i < n0 + n1 + n2) {
+            tri_verts(g, L.l[2][i - n0 - n1], vs[0], vs[1], vs[2]);
+        } else {
+            tet_verts(g, L.l[3][i - n0 - n1 - n2], vs[0], vs[1], vs[2], vs[3]);
+        }
+        for (int k = 0; k < 4; k++) seed_vertex(g, m, vs[k]);
+    }
+}
+__global__ void k_seed_paths(Grid g, PathRec R, uint8_t *m) {
+    const i64 na = min((i64)R.n[0], R.cap_as), nd = min((i64)R.n[1], R.cap_ds);
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < na + nd; i += (i64)gridDim.x * blockDim.x) {
+        i64 vs[4] = {-1, -1, -1, -1};
+        if (i < na) tet_verts(g, R.as_cur[i], vs[0], vs[1], vs[2], vs[3]);
+        else vs[0] = R.ds_vert[i - na];
+        for (int k = 0; k < 4; k++) seed_vertex(g, m, vs[k]);
+    }
+}
+// one thread per line along `axis` (0 = x, 1 = y, 2 = z): every position
+// within `radius` of a seed of the line becomes a seed
+__global__ void k_dilate_axis(Grid g, uint8_t *m, int axis, int radius) {
+    const int n = axis == 0 ? g.W : axis == 1 ? g.H : g.D;
+    const i64 step = axis == 0 ? 1 : axis == 1 ? (i64)g.W : g.WH;
+    const i64 lines = g.V / n;
+    for (i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x; t < lines; t += (i64)gridDim.x * blockDim.x) {
+        i64 base;
+        if (axis == 0) base = t * g.W;                                  // t = y + H z
+        else if (axis == 1) base = (t % g.W) + (t / g.W) * g.WH;        // t = x + W z
+        else base = t;                                                  // t = x + W y
+        int last = -radius - 1;
+        for (int i = 0; i < n; i++) {
+            const uint8_t b = m[base + i * step];
+            if (b & kSnapSeed) last = i;
+            if (i - last <= radius) m[base + i * step] = (uint8_t)(b | kSnapGrow);
+        }
+        int next = n + radius + 1;
+        for (int i = n - 1; i >= 0; i--) {
+            uint8_t b = m[base + i * step];
+            if (b & kSnapSeed) next = i;
+            if (next - i <= radius) b |= kSnapGrow;
+            m[base + i * step] = (uint8_t)((b & 1) | ((b & kSnapGrow) ? kSnapSeed : 0));
+        }
+    }
+}
+__global__ void k_snap_mask(RuleCtx c, uint8_t *m) {
+    double *gv = const_cast<double *>(c.gv);
+    for (i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x; v < c.g.V; v += (i64)gridDim.x * blockDim.x) {
+        const uint8_t b = m[v];
+        if (!(b & kSnapSeed)) continue;
+        m[v] = (uint8_t)(b & 1);
+        if (gv[v] != c.f[v]) {
+            gv[v] = c.f[v];
+            m[v] = 1;
+            lower(c, v);  // a request: the re-pairing looks here
+        }
+    }
+}
+// the request bits of the listed vertices back to 0 (k_apply does this for
+// the vertices it updates; snapped vertices are only re-paired)
+__global__ void k_clear_req(const i64 *reqlist, const unsigned long long *n, i64 cap, uint32_t *reqbits) {
+    const i64 m = min((i64)*n, cap);
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (i64)gridDim.x * blockDim.x)
+        reqbits[reqlist[i] >> 5] = 0;
 }
 
 // filter_vertices / _edges / _faces / _tetrahedras (main_3d.cu:2405-2490):
@@ -1187,6 +1284,7 @@ RuleCtx rule_ctx(dmtz_ctx *ctx, const Grid &g, double bound, int edit_type) {
     c.reqn = ctx->counters + 4;
     c.reqcap = g.V;
     c.err = ctx->errword;
+    c.progress = ctx->counters + 7;
     return c;
 }
 
@@ -1567,6 +1665,8 @@ struct LoopCtl {
     long long cap[4];   // mismatch list capacities
     int overflow;       // a scan overflowed a list: stop, grow, scan again, resume at `state`
     int last;           // state of the last body run
+    int break_stalls;   // stop when a round changed nothing (the host breaks the stall)
+    int stalled;
 };
 }  // namespace
 
@@ -1614,9 +1714,14 @@ __global__ void k_loop_ctl(LoopCtl *ctl, const unsigned long long *counters, cud
     if (next != LS_DONE && st != LS_PCHECK)
         for (int k = 0; k < 4; k++)
             if (c.cc[k] > c.cap[k]) c.overflow = 1;
+    // counters[7]: set by the update when it changed something; a path round
+    // counts only if its detection had records (counters[5], [6])
+    if (c.break_stalls && next != LS_DONE && counters[7] == 0 &&
+        (st == LS_CP || ((st == LS_PDF || st == LS_PFIX) && counters[5] + counters[6] > 0)))
+        c.stalled = 1;
     c.state = next;
     *ctl = c;
-    cudaGraphSetConditional(hwhile, (next != LS_DONE && !c.overflow) ? 1u : 0u);
+    cudaGraphSetConditional(hwhile, (next != LS_DONE && !c.overflow && !c.stalled) ? 1u : 0u);
 }
 
 // ----------------------------------------------------------------------------- phase timers
@@ -1713,6 +1818,7 @@ static dmtz_status run_graph_loop(dmtz_ctx *ctx, const Grid &g, const RuleCtx &r
             if (state == LS_PDF || state == LS_PCHECK) launch_detect(ctx, g, rc, PR, pgrid, conn);
             if (state != LS_PCHECK) {
                 cudaMemsetAsync(ctx->counters + 4, 0, sizeof(unsigned long long), st);
+                cudaMemsetAsync(ctx->counters + 7, 0, sizeof(unsigned long long), st);
                 if (state == LS_CP) k_fix_cp<<<pgrid, kBlock, 0, st>>>(rc, L, ps);
                 else k_fix_path<<<pgrid, kBlock, 0, st>>>(rc, PR);
                 k_apply<<<pgrid, kBlock, 0, st>>>(rc, range, pt, 1, ctx->changed, nullptr);
@@ -1785,6 +1891,31 @@ static dmtz_status learned_start(dmtz_ctx *ctx, dmtz_cnn *net, const Grid &g, do
                                                               (double)min_drop_of(net) * bound, ctx->changed);
     ctx->launches += 5;
     run_pairing(ctx, g, view(ctx->Q, ctx->g), ctx->P.crit, 1);
+    CK(cudaGetLastError());
+    return DMTZ_OK;
+}
+
+// a round made no progress: reset the values around the remaining mismatched
+// cells (cp = 1) or separatrix records (cp = 0) to the original ones, re-pair
+// there, and clear the request bits (see k_snap_cells)
+static dmtz_status break_stall(dmtz_ctx *ctx, const Grid &g, const RuleCtx &rc, const PathRec &PR,
+                               const FieldState &Qs, int cp, int want_saddles, int64_t nbreaks) {
+    cudaStream_t st = ctx->stream;
+    const unsigned pgrid = persistent_grid();
+    // the k-th break resets the box of half-width k around the seeds (the
+    // seeds alone first), up to the whole grid, where g = f and every run ends
+    const int radius = (int)std::min<int64_t>(nbreaks, std::max(g.W, std::max(g.H, g.D)));
+    CK(cudaMemsetAsync(ctx->counters + 4, 0, sizeof(unsigned long long), st));
+    if (cp) k_seed_cells<<<pgrid, kBlock, 0, st>>>(g, cp_lists(ctx), ctx->changed);
+    else k_seed_paths<<<pgrid, kBlock, 0, st>>>(g, PR, ctx->changed);
+    for (int axis = 0; axis < 3; axis++) {
+        const int n = axis == 0 ? g.W : axis == 1 ? g.H : g.D;
+        k_dilate_axis<<<grid_for(g.V / n), kBlock, 0, st>>>(g, ctx->changed, axis, std::min(radius, n));
+    }
+    k_snap_mask<<<pgrid, kBlock, 0, st>>>(rc, ctx->changed);
+    repair_dirty(ctx, g, Qs, ctx->P.crit, want_saddles);
+    k_clear_req<<<pgrid, kBlock, 0, st>>>(ctx->reqlist, ctx->counters + 4, g.V, ctx->reqbits);
+    ctx->launches += 6;
     CK(cudaGetLastError());
     return DMTZ_OK;
 }
@@ -1871,6 +2002,7 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
         c.converged = 1;
         c.max_rounds = max_rounds;
         c.outer = 1;
+        c.break_stalls = opts->break_stalls ? 1 : 0;
         for (int k = 0; k < 4; k++) c.cc[k] = cc[k];
         c.state = cp_any() ? LS_CP : (pvp ? LS_PDF : LS_DONE);
         LoopCtl fin = c;
@@ -1881,13 +2013,33 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
                 for (int k = 0; k < 4; k++) cur.cap[k] = ctx->capL[k];
                 if ((s = run_graph_loop(ctx, g, rc, cp_lists(ctx), PR, Qs, range, ps, pt, conn, cur, &fin)) != DMTZ_OK)
                     return s;
-                if (!fin.overflow) break;
+                if (!fin.overflow && !fin.stalled) break;
                 // a scan outgrew a list: grow it, rebuild the lists and resume
                 unsigned long long h4[4];
                 for (int k = 0; k < 4; k++) h4[k] = (unsigned long long)fin.cc[k];
                 if ((s = fit_lists(ctx, g, fin.last == LS_CP ? (ps == 1) : 1, h4)) != DMTZ_OK) return s;
                 cur = fin;
                 cur.overflow = 0;
+                if (fin.stalled) {  // the round changed nothing: break the stall, then go on
+                    const int cpst = fin.last == LS_CP;
+                    if ((s = break_stall(ctx, g, rc, PR, Qs, cpst, cpst ? (ps == 1) : 1, R.stall_breaks)) != DMTZ_OK)
+                        return s;
+                    R.stall_breaks++;
+                    if ((s = read_fit(cpst ? (ps == 1) : 1)) != DMTZ_OK) return s;
+                    cur.stalled = 0;
+                    for (int k = 0; k < 4; k++) cur.cc[k] = (long long)hc[k];
+                    const bool any = hc[0] || hc[1] || hc[2] || hc[3];
+                    if (cpst) {  // on with the critical-point loop, or to a separatrix round
+                        cur.state = any ? LS_CP : (pvp ? LS_PDF : LS_DONE);
+                    } else {  // a new outer iteration, or the separatrix re-check
+                        cur.state = any ? LS_CP : LS_PCHECK;
+                        if (any) cur.outer++;
+                    }
+                    if (cur.state == LS_DONE) {
+                        fin = cur;
+                        break;
+                    }
+                }
             }
             pt_.end();
             // kernels per body run: switch + control, plus each state's own
@@ -1918,6 +2070,7 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
             R.cp_rounds++;
             paths_fresh = false;
             CK(cudaMemsetAsync(ctx->counters + 4, 0, sizeof(unsigned long long), st));
+            CK(cudaMemsetAsync(ctx->counters + 7, 0, sizeof(unsigned long long), st));
             pt_.begin(PH_FIXCP);
             k_fix_cp<<<pgrid, kBlock, 0, st>>>(rc, cp_lists(ctx), ps);
             pt_.end();
@@ -1929,6 +2082,11 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
             repair_dirty(ctx, g, Qs, ctx->P.crit, ps == 1);
             pt_.end();
             if ((s = read_fit(ps == 1)) != DMTZ_OK) return s;
+            if (opts->break_stalls && hc[7] == 0 && rounds < max_rounds && (hc[0] || hc[1] || hc[2] || hc[3])) {
+                if ((s = break_stall(ctx, g, rc, PR, Qs, 1, ps == 1, R.stall_breaks)) != DMTZ_OK) return s;
+                R.stall_breaks++;
+                if ((s = read_fit(ps == 1)) != DMTZ_OK) return s;
+            }
             for (int k = 0; k < 4; k++) cc[k] = (i64)hc[k];
         }
         if (rounds >= max_rounds) {
@@ -1946,6 +2104,7 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
         }
         paths_fresh = false;
         CK(cudaMemsetAsync(ctx->counters + 4, 0, sizeof(unsigned long long), st));
+        CK(cudaMemsetAsync(ctx->counters + 7, 0, sizeof(unsigned long long), st));
         pt_.begin(PH_FIXPATH);
         k_fix_path<<<pgrid, kBlock, 0, st>>>(rc, PR);
         pt_.end();
@@ -1957,6 +2116,11 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
         repair_dirty(ctx, g, Qs, ctx->P.crit, 1);
         pt_.end();
         if ((s = read_fit(1)) != DMTZ_OK) return s;
+        if (opts->break_stalls && hc[7] == 0 && rounds < max_rounds && hc[5] + hc[6] > 0) {
+            if ((s = break_stall(ctx, g, rc, PR, Qs, 0, 1, R.stall_breaks)) != DMTZ_OK) return s;
+            R.stall_breaks++;
+            if ((s = read_fit(1)) != DMTZ_OK) return s;
+        }
         for (int k = 0; k < 4; k++) cc[k] = (i64)hc[k];
         n_as = n_ds = n_wall = 0;
         if (!cp_any()) {

@@ -290,6 +290,10 @@ int main(int argc, char **argv) {
     o.edit_type = r.flags[6];
     o.max_rounds = 0;
     o.use_graph = 0;
+    // where the reference would loop forever, finish instead (DMTZ_REFERENCE_STALLS=1: keep looping
+    // until DMTZ_MAX_ROUNDS, as the reference does)
+    const char *ref_stalls = std::getenv("DMTZ_REFERENCE_STALLS");
+    o.break_stalls = (ref_stalls && std::atoi(ref_stalls) == 1) ? 0 : 1;
     const char *cap = std::getenv("DMTZ_MAX_ROUNDS");
     if (cap) o.max_rounds = std::atoi(cap);
     dmtz_report rep;

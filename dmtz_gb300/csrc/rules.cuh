@@ -37,6 +37,7 @@ struct RuleCtx {
     unsigned long long *reqn;
     i64 reqcap;
     int *err;
+    unsigned long long *progress;  // set when an update changes a value or an edit counter
 };
 
 // --------------------------------------------------------------- literal id arithmetic

@@ -70,8 +70,9 @@ def make_trace(ctx: Context, f, g, rel_eps, flags=FULL_MSC, max_rounds=2000, use
     ctx.features(fd.data_ptr(), gd.data_ptr(), dims, rel_eps, feat.data_ptr(), active.data_ptr())
     gfix = gd.clone()
     torch.cuda.synchronize()
+    # traces follow the reference's rules only: a stalled field is skipped
     rep = ctx.correct_ptr(fd.data_ptr(), gfix.data_ptr(), dims, rel_eps, flags, True, max_rounds, use_graph,
-                          allow_nonconverged=True)
+                          allow_nonconverged=True, break_stalls=False)
     if not rep["converged"]:
         return None
     bound = rel_eps * float(f.max() - f.min())

@@ -57,6 +57,12 @@ typedef struct {
     int max_rounds;           /* cap on fix/apply rounds; 0 = 100000 */
     int use_graph;            /* 1: run the loop as a CUDA graph with a device-side
                                  convergence flag; 0: host-driven loop */
+    int break_stalls;         /* 1: when a round changes no value and no edit counter
+                                 (a state the reference's loop repeats forever), set the
+                                 values around the remaining mismatches back to the
+                                 original ones (always within the bound) and go on;
+                                 0: keep going until max_rounds, as the reference would.
+                                 Rounds that make progress are the same either way. */
 } dmtz_opts;
 
 typedef struct {
@@ -78,6 +84,7 @@ typedef struct {
                                    (main_3d.cu:6419-6436): gradient pairing + mismatch
                                    detection, critical-point fixes, separatrix detection,
                                    separatrix fixes, value update, set-up */
+    int64_t stall_breaks;       /* rounds in which break_stalls reset values */
 } dmtz_report;
 
 /* Context: owns the device, a stream and all scratch memory.

@@ -1529,25 +1529,66 @@ static void fix_ds_vpath(ctx_t *c, int v_idx) {
 /* ---------------------------------------------------------------------------
  * A7: applyDeltaBuffer1, main_3d.cu:1122-1164
  * ------------------------------------------------------------------------- */
-static void apply_buffer(const grid_t *G, const double *f, double *g, int *cnt, const double *buf, double bound,
-                         double range, int preserve_type) {
+/* returns 1 when some value or edit counter changed (0: the round was a fixed point) */
+static int apply_buffer(const grid_t *G, const double *f, double *g, int *cnt, const double *buf, double bound,
+                        double range, int preserve_type) {
     const double sentinel = -2000.0 * range;
+    int progress = 0;
     for (int v = 0; v < G->V; v++) {
         if (buf[v] != sentinel) {
-            if (preserve_type == 0) {
-                if (fabs(buf[v]) > 1e-15 * range && cnt[v] < 5 && fabs(f[v] - (g[v] + buf[v])) <= bound) {
-                    g[v] += buf[v];
-                    cnt[v] += 1;
-                } else {
-                    cnt[v] = 6;
-                    g[v] = f[v] - bound;
-                }
+            if (preserve_type == 0 && fabs(buf[v]) > 1e-15 * range && cnt[v] < 5 &&
+                fabs(f[v] - (g[v] + buf[v])) <= bound) {
+                g[v] += buf[v];
+                cnt[v] += 1;
+                progress = 1;
             } else {
+                if (cnt[v] != 6 || g[v] != f[v] - bound) progress = 1;
                 cnt[v] = 6;
                 g[v] = f[v] - bound;
             }
         }
     }
+    return progress;
+}
+
+/* Stall breaking (not in the reference, whose loop repeats a round that
+ * changed nothing forever): every vertex within `radius` per axis of a seed
+ * goes back to its original value.  Seeds are marked 1 in m; the box is grown
+ * axis by axis (a vertex joins when a seed of its grid line is within radius). */
+static void snap_box(const grid_t *G, const double *f, double *g, unsigned char *m, int radius) {
+    const int n3[3] = {G->W, G->H, G->D};
+    const long long st3[3] = {1, G->W, (long long)G->W * G->H};
+    unsigned char *grow = (unsigned char *)malloc((size_t)G->V);
+    for (int ax = 0; ax < 3; ax++) {
+        const int n = n3[ax];
+        const long long step = st3[ax];
+        const int r = radius < n ? radius : n;
+        memset(grow, 0, (size_t)G->V);
+        for (long long base = 0; base < G->V; base++) {
+            /* base runs over the vertices whose coordinate along ax is 0 */
+            const int x = (int)(base % G->W), y = (int)((base / G->W) % G->H), z = (int)(base / ((long long)G->W * G->H));
+            if ((ax == 0 && x) || (ax == 1 && y) || (ax == 2 && z)) continue;
+            for (int i = 0; i < n; i++) {
+                if (!m[base + i * step]) continue;
+                const int lo = i - r < 0 ? 0 : i - r, hi = i + r > n - 1 ? n - 1 : i + r;
+                for (int j = lo; j <= hi; j++) grow[base + j * step] = 1;
+            }
+        }
+        memcpy(m, grow, (size_t)G->V);
+    }
+    free(grow);
+    for (int v = 0; v < G->V; v++)
+        if (m[v]) g[v] = f[v];
+}
+
+/* the k-th break (k = 0, 1, ...) resets the box of half-width k: the seeds
+ * alone first, then growing by one per break, up to the whole grid (where g = f
+ * and nothing can mismatch, so every run ends) */
+static int stall_radius(const grid_t *G, long long nbreaks) {
+    long long span = G->W;
+    if (G->H > span) span = G->H;
+    if (G->D > span) span = G->D;
+    return (int)(nbreaks < span ? nbreaks : span);
 }
 
 /* ---------------------------------------------------------------------------
@@ -1555,9 +1596,19 @@ static void apply_buffer(const grid_t *G, const double *f, double *g, int *cnt, 
  * ------------------------------------------------------------------------- */
 int orc_correct(int W, int H, int D, const double *f, double *g, double rel_eps, const int flags[7], int max_outer,
                 int nthreads, long long stats[8], int *cnt_out) {
+    long long st9[9];
+    const int rc = orc_correct_ex(W, H, D, f, g, rel_eps, flags, max_outer, nthreads, 0, st9, cnt_out);
+    memcpy(stats, st9, 8 * sizeof(long long));
+    return rc;
+}
+
+int orc_correct_ex(int W, int H, int D, const double *f, double *g, double rel_eps, const int flags[7], int max_outer,
+                   int nthreads, int break_stalls, long long stats[9], int *cnt_out) {
     const int ps = flags[0], pv = flags[1], pg = flags[2], filt = flags[3], pc = flags[4], pt = flags[5],
               et = flags[6];
-    for (int i = 0; i < 8; i++) stats[i] = 0;
+    for (int i = 0; i < 9; i++) stats[i] = 0;
+    long long breaks = 0;
+    unsigned char *mark = NULL;
     if (pc == 1) return -1;
     const int conn = pv == 1 && pg == 0; /* connectivity-mode separatrices */
     if (max_outer <= 0) max_outer = 100000;
@@ -1663,10 +1714,37 @@ int orc_correct(int W, int H, int D, const double *f, double *g, double rel_eps,
                 for (int i = 0; i < cc4[2]; i++) fix_2saddle(&c, l2s[i]);
             for (int i = 0; i < cc4[3]; i++) fix_maximum(&c, lmax[i]);
             oob += c.oob;
-            apply_buffer(&G, f, g, cnt, buf, bound, range, pt);
+            const int progress = apply_buffer(&G, f, g, cnt, buf, bound, range, pt);
             oob += pair_all(&G, g, QV, QE, QF, QT, nthreads);
             orc_cp_mismatch(W, H, D, PV, PE, PF, PT, QV, QE, QF, QT, cc4, lmin, lsad, l2s, lmax);
             if (ps != 1) cc4[1] = cc4[2] = 0;
+            if (break_stalls && !progress && rounds < round_cap &&
+                (cc4[0] > 0 || cc4[1] > 0 || cc4[2] > 0 || cc4[3] > 0)) {
+                /* seeds: the vertices of the remaining mismatched cells */
+                if (!mark) mark = (unsigned char *)malloc(V);
+                memset(mark, 0, V);
+                for (int i = 0; i < cc4[0]; i++) mark[lmin[i]] = 1;
+                for (int i = 0; i < cc4[1]; i++) {
+                    int a, b;
+                    edge_verts(&G, lsad[i], &a, &b);
+                    mark[a] = mark[b] = 1;
+                }
+                for (int i = 0; i < cc4[2]; i++) {
+                    int a, b, c3;
+                    tri_verts(&G, l2s[i], &a, &b, &c3);
+                    mark[a] = mark[b] = mark[c3] = 1;
+                }
+                for (int i = 0; i < cc4[3]; i++) {
+                    int a, b, c3, d;
+                    tet_verts(&G, lmax[i], &a, &b, &c3, &d);
+                    mark[a] = mark[b] = mark[c3] = mark[d] = 1;
+                }
+                snap_box(&G, f, g, mark, stall_radius(&G, breaks));
+                breaks++;
+                oob += pair_all(&G, g, QV, QE, QF, QT, nthreads);
+                orc_cp_mismatch(W, H, D, PV, PE, PF, PT, QV, QE, QF, QT, cc4, lmin, lsad, l2s, lmax);
+                if (ps != 1) cc4[1] = cc4[2] = 0;
+            }
         }
         if (rounds >= round_cap) {
             converged = 0;
@@ -1691,9 +1769,25 @@ int orc_correct(int W, int H, int D, const double *f, double *g, double rel_eps,
         for (int i = 0; i < n_as; i++) fix_as_vpath(&c, as_cur[i]);
         for (int i = 0; i < n_ds; i++) fix_ds_vpath(&c, ds_v[i]);
         oob += c.oob;
-        apply_buffer(&G, f, g, cnt, buf, bound, range, pt);
+        const int progress = apply_buffer(&G, f, g, cnt, buf, bound, range, pt);
         oob += pair_all(&G, g, QV, QE, QF, QT, nthreads);
         orc_cp_mismatch(W, H, D, PV, PE, PF, PT, QV, QE, QF, QT, cc4, lmin, lsad, l2s, lmax);
+        if (break_stalls && !progress && rounds < round_cap && n_as + n_ds > 0) {
+            /* seeds: the records' current tetrahedra and trouble makers */
+            if (!mark) mark = (unsigned char *)malloc(V);
+            memset(mark, 0, V);
+            for (int i = 0; i < n_as; i++) {
+                int a, b, c3, d;
+                tet_verts(&G, as_cur[i], &a, &b, &c3, &d);
+                mark[a] = mark[b] = mark[c3] = mark[d] = 1;
+            }
+            for (int i = 0; i < n_ds; i++)
+                if (ds_v[i] >= 0 && ds_v[i] < G.V) mark[ds_v[i]] = 1;
+            snap_box(&G, f, g, mark, stall_radius(&G, breaks));
+            breaks++;
+            oob += pair_all(&G, g, QV, QE, QF, QT, nthreads);
+            orc_cp_mismatch(W, H, D, PV, PE, PF, PT, QV, QE, QF, QT, cc4, lmin, lsad, l2s, lmax);
+        }
         n_as = n_ds = 0;
         if (cc4[0] == 0 && cc4[1] == 0 && cc4[2] == 0 && cc4[3] == 0) {
             if (conn) {
@@ -1711,7 +1805,9 @@ int orc_correct(int W, int H, int D, const double *f, double *g, double rel_eps,
     stats[1] = cp_ite;
     stats[2] = oob;
     stats[3] = converged;
+    stats[8] = breaks;
     if (cnt_out) memcpy(cnt_out, cnt, sizeof(int) * V);
+    free(mark);
     free(P); free(Q); free(lmin); free(lsad); free(l2s); free(lmax);
     free(as_tet); free(as_cur); free(ds_e); free(ds_v); free(cnt); free(buf);
     free(cmin); free(cmax);

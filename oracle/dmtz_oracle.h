@@ -81,6 +81,11 @@ int orc_path_detect(int W, int H, int D,
 int orc_correct(int W, int H, int D, const double *f, double *g,
                 double rel_eps, const int flags[7], int max_outer,
                 int nthreads, long long stats[8], int *cnt_out);
+/* orc_correct with stall breaking (break_stalls = 1: a round that changes no
+ * value and no edit counter resets a box around the remaining mismatches to
+ * the original values; stats[8] = such breaks). */
+int orc_correct_ex(int W, int H, int D, const double *f, double *g, double rel_eps, const int flags[7],
+                   int max_outer, int nthreads, int break_stalls, long long stats[9], int *cnt_out);
 
 /* Manifold labels: desc[v] = minimum reached along the steepest-descent
  * pairing, asc[t] = maximum reached by the ascending tetrahedron walk, -1 if

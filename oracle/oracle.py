@@ -51,6 +51,9 @@ def lib():
         L.orc_correct.argtypes = [ctypes.c_int] * 3 + [_f64p, _f64p, ctypes.c_double, _i32p, ctypes.c_int,
                                                         ctypes.c_int, _i64p, _i32p]
         L.orc_correct.restype = ctypes.c_int
+        L.orc_correct_ex.argtypes = [ctypes.c_int] * 3 + [_f64p, _f64p, ctypes.c_double, _i32p, ctypes.c_int,
+                                                           ctypes.c_int, ctypes.c_int, _i64p, _i32p]
+        L.orc_correct_ex.restype = ctypes.c_int
         L.orc_labels.argtypes = [ctypes.c_int] * 3 + [_f64p, _i32p, _i32p, ctypes.c_int]
         L.orc_labels.restype = ctypes.c_int
         L.orc_face_cofaces.argtypes = [ctypes.c_int] * 4 + [_i32p, _i32p]
@@ -124,21 +127,25 @@ def path_detect(P, Q, dims, connectivity=False):
     return a_t[:na].copy(), a_c[:na].copy(), d_e[:nd].copy(), d_v[:nd].copy(), oob
 
 
-def correct(f, g, dims, rel_eps, flags, max_outer=0, threads=1):
-    """Run the full correction loop.  Returns (corrected g, stats dict, cnt)."""
+def correct(f, g, dims, rel_eps, flags, max_outer=0, threads=1, break_stalls=False):
+    """Run the full correction loop.  Returns (corrected g, stats dict, cnt).
+    break_stalls: reset a box around the remaining mismatches to the original
+    values when a round changes nothing (not in the reference, whose loop
+    repeats such a round forever); stats["stall_breaks"] counts them."""
     W, H, D = dims
     V = counts(dims)[0]
     ff = np.ascontiguousarray(f, np.float64).reshape(-1)
     gg = np.array(g, np.float64).reshape(-1)
     assert ff.size == V and gg.size == V
     fl = np.ascontiguousarray(flags, np.int32)
-    st = np.zeros(8, np.int64)
+    st = np.zeros(9, np.int64)
     cnt = np.empty(V, np.int32)
-    rc = lib().orc_correct(W, H, D, ff, gg, float(rel_eps), fl, int(max_outer), int(threads), st, cnt)
+    rc = lib().orc_correct_ex(W, H, D, ff, gg, float(rel_eps), fl, int(max_outer), int(threads), int(bool(break_stalls)),
+                              st, cnt)
     if rc != 0:
         raise ValueError("flag combination not supported by the oracle (preserve_connectors=1)")
     stats = dict(outer_iterations=int(st[0]), cp_iterations=int(st[1]), oob=int(st[2]), converged=bool(st[3]),
-                 initial_mismatch=[int(x) for x in st[4:8]])
+                 initial_mismatch=[int(x) for x in st[4:8]], stall_breaks=int(st[8]))
     return gg, stats, cnt
 
 
