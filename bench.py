@@ -451,12 +451,13 @@ def run_learned(args):
 
 
 def run_big(args):
-    """The largest single-GPU case: a power-law field of size^3 (default
-    1024^3, seed 11, f32 values widened to f64), SZ-style decompression at
-    eps = 1e-4 x range, full-MSC flags, generated on the GPU.  The reference
-    cannot run it (its int32 edge and triangle counts overflow).  Times the
-    correction on the device (inputs resident in HBM) and reports the device
-    memory the context held."""
+    """The largest single-GPU cases, generated on the GPU: a power-law field of
+    size^3 (default 1024^3, seed 11, f32 values widened to f64), or with
+    --big-kind gauss a float64 Gaussian mixture of 4096 Gaussians with widths
+    U[4, 32] (768^3, seed 12); SZ-style decompression at eps = 1e-4 x range,
+    full-MSC flags.  The reference cannot run either (its int32 edge and
+    triangle counts overflow).  Times the correction on the device (inputs
+    resident in HBM) and reports the device memory the context held."""
     import torch
 
     import dmtz_gb300 as dm
@@ -464,12 +465,14 @@ def run_big(args):
 
     n = args.big_size
     dims = (n, n, n)
+    gauss = args.big_kind == "gauss"
+    seed = 12 if gauss else 11
     t0 = time.perf_counter()
-    f = synth.power_law_device(dims, 11)
+    f = synth.gaussian_mix_device(dims, seed) if gauss else synth.power_law_device(dims, seed)
     torch.cuda.empty_cache()  # the generator's temporaries go back to the device
     ctx = dm.Context(0)
     g0 = torch.empty_like(f)
-    ctx.quantize_ptr(f.data_ptr(), g0.data_ptr(), dims, REL_EPS, 0.05, 11)  # SZ-style model on the GPU
+    ctx.quantize_ptr(f.data_ptr(), g0.data_ptr(), dims, REL_EPS, 0.05, seed)  # SZ-style model on the GPU
     eps = REL_EPS * float(f.max() - f.min())
     gen_s = time.perf_counter() - t0
     free0, total = torch.cuda.mem_get_info()
@@ -482,10 +485,12 @@ def run_big(args):
     free1, _ = torch.cuda.mem_get_info()
     within = bool(((g - f).abs() <= eps * (1 + 1e-12)).all().item())
     V = n ** 3
-    line = {"metric": f"Mvox/s to full MSC match ({n}^3 power-law, eps=1e-4 x range, full-MSC flags)",
+    kind = "f64 Gaussian-mix (4096 Gaussians)" if gauss else "power-law"
+    line = {"metric": f"Mvox/s to full MSC match ({n}^3 {kind}, eps=1e-4 x range, full-MSC flags)",
             "value": V / rep["seconds"] / 1e6, "unit": "Mvox/s", "n_gpus": 1, "steps": 1, "warmup": 0,
             "ms_per_step": rep["seconds"] * 1e3, "higher_is_better": True, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"powerlaw {n}^3 seed 11 generated on the GPU, decompressed by the library's "
+            "config": {"workload": f"{'gauss-mix 4096 x U[4,32]' if gauss else 'powerlaw'} {n}^3 seed {seed} "
+                                   f"generated on the GPU, decompressed by the library's "
                                    f"quantiser (bin 2 eps, 5% noise), eps=1e-4 x range, "
                                    f"flags {''.join(map(str, FLAGS))}", "voxels": V, "generation_s": gen_s,
                        "wall_s": wall, "converged": rep["converged"], "within_bound": within,
@@ -523,7 +528,9 @@ def main():
     ap.add_argument("--sweep-only", type=int, default=0, metavar="SIZE",
                     help="profiling aid: only time the gradient sweep on a SIZE^3 field of the same kind")
     ap.add_argument("--workload", choices=["field256", "batch", "cnn", "learned", "big"], default="field256")
-    ap.add_argument("--big-size", type=int, default=1024, help="big workload: grid size")
+    ap.add_argument("--big-size", type=int, default=0, help="big workload: grid size (default 1024 power-law, "
+                    "768 gauss)")
+    ap.add_argument("--big-kind", choices=["powerlaw", "gauss"], default="powerlaw", help="big workload: field kind")
     ap.add_argument("--max-rounds", type=int, default=2000)
     ap.add_argument("--cnn-size", type=int, default=256, help="cnn workload: grid size")
     ap.add_argument("--traces", type=int, default=64, help="learned workload: training traces")
@@ -544,6 +551,8 @@ def main():
         run_learned(args)
         return
     if args.workload == "big":
+        if args.big_size <= 0:
+            args.big_size = 768 if args.big_kind == "gauss" else 1024
         run_big(args)
         return
     if args.sweep_only:

@@ -151,3 +151,44 @@ def power_law_device(dims, seed: int, slope: float = -3.0):
     f = ((f - f.min()) / (f.max() - f.min())).reshape(-1).double()
     torch.cuda.synchronize()
     return f
+
+
+def gaussian_mix_device(dims, seed: int, n_gauss: int = 4096, sigma=(4.0, 32.0), noise: float = 1e-3,
+                        device: str = "cuda"):
+    """Large Gaussian-mixture field generated on the GPU, kept in float64:
+    n_gauss isotropic Gaussians with centres U[0, dims), widths U[sigma) and
+    amplitudes U[-1, 1], plus N(0, noise).  A Gaussian is separable, so each is
+    added as an outer product of three 1-D profiles over its box of +-6 sigma
+    (the tail left out is below 2e-8 of its amplitude).  torch's CUDA generator
+    draws the parameters and the noise.  Returns a float64 device tensor of
+    shape (D*H*W,)."""
+    import torch
+
+    W, H, D = dims
+    dev = device
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(int(seed))
+    c = torch.rand((n_gauss, 3), generator=gen, device=dev, dtype=torch.float64) * torch.tensor(
+        [W, H, D], dtype=torch.float64, device=dev)
+    s = sigma[0] + (sigma[1] - sigma[0]) * torch.rand(n_gauss, generator=gen, device=dev, dtype=torch.float64)
+    a = 2.0 * torch.rand(n_gauss, generator=gen, device=dev, dtype=torch.float64) - 1.0
+    f = torch.randn((D, H, W), generator=gen, device=dev, dtype=torch.float64) * noise
+    cc, ss, aa = c.cpu().numpy(), s.cpu().numpy(), a.cpu().numpy()
+    axes = [torch.arange(n, dtype=torch.float64, device=dev) for n in (W, H, D)]
+
+    def profile(k, ax, n):
+        lo = max(0, int(np.floor(cc[k, ax] - 6.0 * ss[k])))
+        hi = min(n, int(np.ceil(cc[k, ax] + 6.0 * ss[k])) + 1)
+        d = axes[ax][lo:hi] - float(cc[k, ax])
+        return lo, hi, torch.exp(-(d * d) / (2.0 * float(ss[k]) ** 2))
+
+    for k in range(n_gauss):
+        x0, x1, gx = profile(k, 0, W)
+        y0, y1, gy = profile(k, 1, H)
+        z0, z1, gz = profile(k, 2, D)
+        if x0 >= x1 or y0 >= y1 or z0 >= z1:
+            continue
+        f[z0:z1, y0:y1, x0:x1].add_((float(aa[k]) * gz)[:, None, None] * gy[None, :, None] * gx[None, None, :])
+    if dev != "cpu":
+        torch.cuda.synchronize()
+    return f.reshape(-1)
