@@ -46,7 +46,7 @@ class Report(ctypes.Structure):
                 ("final_paths", ctypes.c_int64 * 2), ("edited_vertices", ctypes.c_int64),
                 ("converged", ctypes.c_int32), ("error_flags", ctypes.c_int32), ("seconds", ctypes.c_double),
                 ("kernel_launches", ctypes.c_int64), ("phase_ms", ctypes.c_double * 6),
-                ("stall_breaks", ctypes.c_int64)]
+                ("stall_breaks", ctypes.c_int64), ("final_walls", ctypes.c_int64)]
 
     PHASES = ("pairing", "fix_cp", "path_detect", "fix_path", "apply", "setup")
 
@@ -56,7 +56,7 @@ class Report(ctypes.Structure):
                     final_paths=list(self.final_paths), edited_vertices=self.edited_vertices,
                     converged=bool(self.converged),
                     error_flags=self.error_flags, seconds=self.seconds, kernel_launches=self.kernel_launches,
-                    stall_breaks=self.stall_breaks,
+                    stall_breaks=self.stall_breaks, final_walls=self.final_walls,
                     phase_ms=dict(zip(self.PHASES, [round(x, 4) for x in self.phase_ms])))
 
 
@@ -90,6 +90,8 @@ def load_library(build_if_missing: bool = True):
     L.dmtz_path_detect_connectivity.argtypes = [_vp, _int, _int, _int, _f64p, _f64p, _i64p, _i32p, _i32p, _i32p,
                                                 _i32p]
     L.dmtz_path_detect_connectivity.restype = _int
+    L.dmtz_wall_detect.argtypes = [_vp, _int, _int, _int, _f64p, _f64p, _i64p, _i32p, _i32p]
+    L.dmtz_wall_detect.restype = _int
     L.dmtz_correct.argtypes = [_vp, _int, _int, _int, _vp, _vp, _int, ctypes.c_double, ctypes.POINTER(Opts),
                                ctypes.POINTER(Report), _vp]
     L.dmtz_profile_sweep.argtypes = [_vp, _int, _int, _int, _vp, _vp, _int, _int, _f64p]
@@ -230,6 +232,17 @@ class Context:
         self._check(self._L.dmtz_fix_round(self._h, *dims, _flat(f), _flat(g), np.ascontiguousarray(cnt, np.int32),
                                            float(rel_eps), int(preserve_saddles), int(edit_type), out))
         return out
+
+    def wall_detect(self, f, g, dims=None):
+        """Wall records of preserve_connectors = 1: (2-saddle faces, first
+        differing edges of their walls), sorted by face."""
+        dims = _dims_of(np.asarray(f), dims)
+        V, E, F, T = cell_counts(dims)
+        c = np.zeros(1, np.int64)
+        ws, we = np.empty(F, np.int32), np.empty(F, np.int32)
+        self._check(self._L.dmtz_wall_detect(self._h, *dims, _flat(f), _flat(g), c, ws, we))
+        n = int(c[0])
+        return ws[:n].copy(), we[:n].copy()
 
     def path_detect(self, f, g, dims=None, connectivity=False):
         """Separatrix records (as_tet, as_cur, ds_edge, ds_vert), sorted: geometry

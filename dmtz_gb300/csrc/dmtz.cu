@@ -342,6 +342,120 @@ __global__ void k_path_as(Grid g, const i64 *sad2, const unsigned long long *nsa
     }
 }
 
+// ------------------------------------------------------------------- walls
+// preserve_connectors = 1: get_false_ds_wall (main_3d.cu:5064-5121) restated
+// without its races.  Every original 2-saddle face runs its own depth-first
+// search over the faces reachable by original V-paths, in the reference's
+// order: pop a face; if it was not visited, take its edges (v1 v2), (v1 v3),
+// (v2 v3) of its descending vertex triple; skip an originally critical edge;
+// the first edge whose original and decompressed pairings differ is the
+// record; otherwise push the face the edge is originally paired with (when
+// it is a face and not this one).
+//
+// Visited marks are a direct-mapped cache of face ids.  A face found there was
+// visited and is skipped; a visited face that fell out of the cache is
+// searched again, which never changes the record: V-paths have no cycles and
+// the stack finishes a face's descendants before the entries below it, so
+// every face reachable from a visited face was visited before it comes back,
+// and a repeat only re-checks edges that passed and pushes visited faces.  The
+// cache size bounds only the work.  A search that passes its pop limit or
+// outgrows its stack is handed to the next tier (larger stack, cache and pop
+// limit in device scratch memory); the record does not depend on the tier.
+struct WallRec {
+    i64 *sad, *edge;        // record: 2-saddle face, first differing edge of its wall
+    unsigned long long *n;
+    i64 cap;
+};
+constexpr int kWallStack1 = 24, kWallCacheBits1 = 6;
+constexpr long long kWallPops1 = 1024;
+
+__device__ __forceinline__ unsigned wall_slot(i64 t, int bits) {
+    return (unsigned)(((unsigned long long)t * 0x9E3779B97F4A7C15ull) >> (64 - bits));
+}
+// 0: no differing edge, 1: record in rec, 2: stack or pop limit reached
+__device__ int wall_dfs(const RuleCtx &c, i64 sad, i64 *stack, int stack_cap, i64 *cache, int cache_bits,
+                        long long pop_cap, i64 &rec) {
+    const Grid &G = c.g;
+    int top = 0;
+    stack[top++] = sad;
+    long long pops = 0;
+    while (top > 0) {
+        const i64 t = stack[--top];
+        if (++pops > pop_cap) return 2;
+        const unsigned slot = wall_slot(t, cache_bits);
+        if (cache[slot] == t) continue;
+        cache[slot] = t;
+        i64 v1, v2, v3;
+        tri_verts(G, t, v1, v2, v3);
+        const i64 es[3] = {edge_ref_pair(G, v1, v2), edge_ref_pair(G, v1, v3), edge_ref_pair(G, v2, v3)};
+        for (int k = 0; k < 3; k++) {
+            const i64 j = es[k];
+            const i64 pe = pe_ref(c, c.P, j);
+            if (pe == -1) continue;
+            if (pe != pe_ref(c, c.Q, j)) {
+                rec = j;
+                return 1;
+            }
+            if (pe != t && pe >= 0 && pe < G.F && pf_ref(c, c.P, pe) == j) {
+                if (top == stack_cap) return 2;
+                stack[top++] = pe;
+            }
+        }
+    }
+    return 0;
+}
+__device__ __forceinline__ void wall_emit(const WallRec &W, i64 s, i64 e) {
+    const unsigned long long k = atomicAdd(W.n, 1ull);
+    if ((i64)k < W.cap) {
+        W.sad[k] = s;
+        W.edge[k] = e;
+    }
+}
+__device__ __forceinline__ void wall_defer(i64 *list, unsigned long long *n, i64 cap, i64 s) {
+    const unsigned long long k = atomicAdd(n, 1ull);
+    if ((i64)k < cap) list[k] = s;
+}
+// first tier: every original 2-saddle (sad2 codes anchor * 12 + slot), stack
+// and cache in per-thread local memory
+__global__ void k_wall_t1(RuleCtx c, const i64 *sad2, const unsigned long long *nsad, i64 capsad, WallRec W,
+                          i64 *next, unsigned long long *nnext, i64 capnext) {
+    const i64 n = min((i64)*nsad, capsad);
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+        const i64 code = sad2[i];
+        int x, y, z;
+        decode_v(c.g, code / 12, x, y, z);
+        const i64 sf = face_ref(c.g, x, y, z, (int)(code % 12));
+        i64 stack[kWallStack1], cache[1 << kWallCacheBits1];
+#pragma unroll
+        for (int k = 0; k < (1 << kWallCacheBits1); k++) cache[k] = -1;
+        i64 rec = -1;
+        const int r = wall_dfs(c, sf, stack, kWallStack1, cache, kWallCacheBits1, kWallPops1, rec);
+        if (r == 1) wall_emit(W, sf, rec);
+        else if (r == 2) wall_defer(next, nnext, capnext, sf);
+    }
+}
+// a larger tier for list[first, first + count): one thread per 2-saddle face,
+// its stack and cache in scratch (stack_cap + 2^cache_bits entries each)
+__global__ void k_wall_tn(RuleCtx c, const i64 *list, i64 first, i64 count, WallRec W, i64 *next,
+                          unsigned long long *nnext, i64 capnext, i64 *scratch, int stack_cap, int cache_bits,
+                          long long pop_cap) {
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (i64)gridDim.x * blockDim.x) {
+        const i64 sf = list[first + i];
+        i64 *stack = scratch + i * ((i64)stack_cap + ((i64)1 << cache_bits));
+        i64 *cache = stack + stack_cap;
+        for (i64 k = 0; k < ((i64)1 << cache_bits); k++) cache[k] = -1;
+        i64 rec = -1;
+        const int r = wall_dfs(c, sf, stack, stack_cap, cache, cache_bits, pop_cap, rec);
+        if (r == 1) wall_emit(W, sf, rec);
+        else if (r == 2) wall_defer(next, nnext, capnext, sf);
+    }
+}
+__global__ void k_fix_wall(RuleCtx c, WallRec W) {
+    const i64 n = min((i64)*W.n, W.cap);
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x)
+        rule_ds_wall(c, W.edge[i]);
+}
+
 // get_false_ds_vpath (main_3d.cu:4837-4959): the reference's walk never
 // advances past the first vertex (dec_current_id stays at the start), so each
 // endpoint's steepest-descent pairing is compared once, v1 (higher id) first.
@@ -646,6 +760,15 @@ __global__ void k_seed_paths(Grid g, PathRec R, uint8_t *m) {
         if (i < na) tet_verts(g, R.as_cur[i], vs[0], vs[1], vs[2], vs[3]);
         else vs[0] = R.ds_vert[i - na];
         for (int k = 0; k < 4; k++) seed_vertex(g, m, vs[k]);
+    }
+}
+__global__ void k_seed_walls(Grid g, WallRec W, uint8_t *m) {
+    const i64 n = min((i64)*W.n, W.cap);
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+        i64 a, b;
+        edge_verts(g, W.edge[i], a, b);
+        seed_vertex(g, m, a);
+        seed_vertex(g, m, b);
     }
 }
 // one thread per line along `axis` (0 = x, 1 = y, 2 = z): every position
@@ -973,9 +1096,15 @@ struct dmtz_ctx {
     unsigned long long *brick_n = nullptr;  // their lengths
     i64 *sad2 = nullptr;      // original 2-saddle triangles
     i64 *as_res = nullptr;    // per (2-saddle, coface) walk results, 2 x capSad2
-    unsigned long long *counters = nullptr;  // [0..3] cp lists, [4] requests, [5,6] paths, [8,9] min/max
-                                             // keys, [10] original 2-saddles, [11] dirty bricks,
-                                             // [12] edited vertices
+    i64 *wall_sad = nullptr, *wall_edge = nullptr;  // wall records (preserve_connectors = 1), capWall each
+    i64 *wall_next[2] = {nullptr, nullptr};          // 2-saddles handed to the next search tier
+    i64 capWall = 0;
+    i64 *wall_scratch = nullptr;  // stacks and caches of the larger wall-search tiers
+    i64 capWS = 0;
+    unsigned long long *counters = nullptr;  // [0..3] cp lists, [4] requests, [5,6] paths, [7] progress,
+                                             // [8,9] min/max keys, [10] original 2-saddles, [12] edited
+                                             // vertices, [13,14] saddle counts, [15] surface anchors,
+                                             // [16] wall records, [17,18] deferred wall searches
     int *errword = nullptr;
     uint8_t *changed = nullptr;
     int64_t launches = 0;  // kernels launched by the current call
@@ -1024,6 +1153,10 @@ void free_all(dmtz_ctx *c) {
     cudaFree(c->succ); cudaFree(c->sad2); cudaFree(c->brick_flags); cudaFree(c->brick_list);
     cudaFree(c->as_res);
     c->as_res = nullptr;
+    cudaFree(c->wall_sad); cudaFree(c->wall_edge); cudaFree(c->wall_next[0]); cudaFree(c->wall_next[1]);
+    cudaFree(c->wall_scratch);
+    c->wall_sad = c->wall_edge = c->wall_next[0] = c->wall_next[1] = c->wall_scratch = nullptr;
+    c->capWall = c->capWS = 0;
     cudaFree(c->brick_n);
     c->brick_n = nullptr;
     c->succ = nullptr; c->sad2 = nullptr; c->brick_flags = nullptr; c->brick_list = nullptr;
@@ -1080,7 +1213,7 @@ dmtz_status ensure(dmtz_ctx *ctx, const Grid &g) {
     CK(dalloc(&ctx->brick_n, 8));
     CK(cudaMemset(ctx->brick_flags, 0, sizeof(uint32_t) * (size_t)((nbr + 3) / 4)));
     ctx->capB = nbr;
-    CK(dalloc(&ctx->counters, 16)); CK(dalloc(&ctx->errword, 1)); CK(dalloc(&ctx->changed, V));
+    CK(dalloc(&ctx->counters, 24)); CK(dalloc(&ctx->errword, 1)); CK(dalloc(&ctx->changed, V));
     ctx->capV = g.V; ctx->capE = g.E; ctx->capF = g.F; ctx->capT = g.T;
     return ensure_lists(ctx, g);
 }
@@ -1393,6 +1526,83 @@ void detect_paths(dmtz_ctx *ctx, const Grid &g, const RuleCtx &rc, const PathRec
     ctx->launches += conn ? 2 : 3;
 }
 
+// Wall records (preserve_connectors = 1) of the current decompressed gradient:
+// every original 2-saddle searched by tiers (see wall_dfs).  Record arrays
+// hold one entry per original 2-saddle; the deferred lists likewise.
+dmtz_status ensure_walls(dmtz_ctx *ctx) {
+    const i64 need = std::max<i64>(ctx->capSad2, 1);
+    if (ctx->capWall >= need) return DMTZ_OK;
+    cudaFree(ctx->wall_sad); cudaFree(ctx->wall_edge); cudaFree(ctx->wall_next[0]); cudaFree(ctx->wall_next[1]);
+    ctx->wall_sad = ctx->wall_edge = ctx->wall_next[0] = ctx->wall_next[1] = nullptr;
+    ctx->capWall = 0;
+    CK(dalloc(&ctx->wall_sad, need));
+    CK(dalloc(&ctx->wall_edge, need));
+    CK(dalloc(&ctx->wall_next[0], need));
+    CK(dalloc(&ctx->wall_next[1], need));
+    ctx->capWall = need;
+    return DMTZ_OK;
+}
+WallRec wall_rec(dmtz_ctx *ctx) {
+    WallRec W;
+    W.sad = ctx->wall_sad;
+    W.edge = ctx->wall_edge;
+    W.n = ctx->counters + 16;
+    W.cap = ctx->capWall;
+    return W;
+}
+unsigned persistent_grid();
+dmtz_status detect_walls(dmtz_ctx *ctx, const Grid &g, const RuleCtx &rc, i64 &n_wall) {
+    struct Tier {
+        int stack_cap, cache_bits;
+        long long pop_cap;
+    };
+    static const Tier tiers[3] = {{2048, 13, 1ll << 16}, {1 << 16, 18, 1ll << 22}, {1 << 21, 23, 1ll << 28}};
+    const i64 budget = (i64)32 << 20;  // scratch entries (256 MB)
+    cudaStream_t st = ctx->stream;
+    dmtz_status s;
+    if ((s = ensure_walls(ctx)) != DMTZ_OK) return s;
+    const WallRec W = wall_rec(ctx);
+    CK(cudaMemsetAsync(ctx->counters + 16, 0, 3 * sizeof(unsigned long long), st));
+    k_wall_t1<<<persistent_grid(), kBlock, 0, st>>>(rc, ctx->sad2, ctx->counters + 10, ctx->capSad2, W,
+                                                     ctx->wall_next[0], ctx->counters + 17, ctx->capWall);
+    ctx->launches++;
+    unsigned long long nd = 0;
+    CK(cudaMemcpyAsync(&nd, ctx->counters + 17, sizeof(nd), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    int cur = 0;
+    for (int t = 0; t < 3 && nd > 0; t++) {
+        const Tier &T = tiers[t];
+        const i64 per = (i64)T.stack_cap + ((i64)1 << T.cache_bits);
+        const i64 chunk = std::max<i64>(1, std::min<i64>((i64)nd, budget / per));
+        if (ctx->capWS < chunk * per) {
+            cudaFree(ctx->wall_scratch);
+            ctx->wall_scratch = nullptr;
+            ctx->capWS = 0;
+            CK(dalloc(&ctx->wall_scratch, chunk * per));
+            ctx->capWS = chunk * per;
+        }
+        unsigned long long *nnext = ctx->counters + 17 + (cur ^ 1);
+        CK(cudaMemsetAsync(nnext, 0, sizeof(unsigned long long), st));
+        for (i64 first = 0; first < (i64)nd; first += chunk) {
+            const i64 cnt = std::min<i64>(chunk, (i64)nd - first);
+            k_wall_tn<<<grid_for(cnt), kBlock, 0, st>>>(rc, ctx->wall_next[cur], first, cnt, W, ctx->wall_next[cur ^ 1],
+                                                        nnext, ctx->capWall, ctx->wall_scratch, T.stack_cap,
+                                                        T.cache_bits, T.pop_cap);
+            ctx->launches++;
+        }
+        CK(cudaMemcpyAsync(&nd, nnext, sizeof(nd), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        cur ^= 1;
+    }
+    if (nd > 0) return fail(ctx, DMTZ_ERR_TOO_LARGE, "a wall search outgrew its largest tier (2^21 stack entries)");
+    unsigned long long nw = 0;
+    CK(cudaMemcpyAsync(&nw, ctx->counters + 16, sizeof(nw), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    CK(cudaGetLastError());
+    n_wall = (i64)nw;
+    return DMTZ_OK;
+}
+
 unsigned persistent_grid() {
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
@@ -1641,6 +1851,38 @@ dmtz_status dmtz_path_detect_connectivity(dmtz_ctx *ctx, int W, int H, int D, co
                                           const double *decp, int64_t counts[2], int32_t *as_tet, int32_t *as_cur,
                                           int32_t *ds_edge, int32_t *ds_vert) {
     return path_detect_impl(ctx, W, H, D, orig, decp, 1, counts, as_tet, as_cur, ds_edge, ds_vert);
+}
+
+dmtz_status dmtz_wall_detect(dmtz_ctx *ctx, int W, int H, int D, const double *orig, const double *decp,
+                             int64_t *count, int32_t *w_sad, int32_t *w_edge) {
+    Grid g;
+    dmtz_status s = check_dims(ctx, W, H, D, g);
+    if (s != DMTZ_OK) return s;
+    if (!count) return fail(ctx, DMTZ_ERR_ARG, "null count");
+    CK(cudaSetDevice(ctx->device));
+    if ((s = setup_pair(ctx, g, orig, decp)) != DMTZ_OK) return s;
+    CK(cudaMemsetAsync(ctx->errword, 0, sizeof(int), ctx->stream));
+    RuleCtx rc = rule_ctx(ctx, g, 0.0, 0);
+    if ((s = prep_paths(ctx, g)) != DMTZ_OK) return s;
+    i64 n = 0;
+    if ((s = detect_walls(ctx, g, rc, n)) != DMTZ_OK) return s;
+    *count = (int64_t)n;
+    if (n > 0 && w_sad) {
+        std::vector<i64> a(n), b(n);
+        CK(cudaMemcpy(a.data(), ctx->wall_sad, sizeof(i64) * n, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(b.data(), ctx->wall_edge, sizeof(i64) * n, cudaMemcpyDeviceToHost));
+        std::vector<std::pair<i64, i64>> p(n);
+        for (i64 i = 0; i < n; i++) p[i] = {a[i], b[i]};
+        std::sort(p.begin(), p.end());
+        for (i64 i = 0; i < n; i++) {
+            w_sad[i] = (int32_t)p[i].first;
+            if (w_edge) w_edge[i] = (int32_t)p[i].second;
+        }
+    }
+    int err = 0;
+    CK(cudaMemcpy(&err, ctx->errword, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err & ERR_OOB) return fail(ctx, DMTZ_ERR_OOB, "a wall search indexed out of range");
+    return DMTZ_OK;
 }
 
 // ----------------------------------------------------------------------------- graph-driven loop
@@ -1899,7 +2141,8 @@ static dmtz_status learned_start(dmtz_ctx *ctx, dmtz_cnn *net, const Grid &g, do
 // cells (cp = 1) or separatrix records (cp = 0) to the original ones, re-pair
 // there, and clear the request bits (see k_snap_cells)
 static dmtz_status break_stall(dmtz_ctx *ctx, const Grid &g, const RuleCtx &rc, const PathRec &PR,
-                               const FieldState &Qs, int cp, int want_saddles, int64_t nbreaks) {
+                               const FieldState &Qs, int cp, int want_saddles, int64_t nbreaks,
+                               const WallRec *WR = nullptr) {
     cudaStream_t st = ctx->stream;
     const unsigned pgrid = persistent_grid();
     // the k-th break resets the box of half-width k around the seeds (the
@@ -1908,6 +2151,10 @@ static dmtz_status break_stall(dmtz_ctx *ctx, const Grid &g, const RuleCtx &rc, 
     CK(cudaMemsetAsync(ctx->counters + 4, 0, sizeof(unsigned long long), st));
     if (cp) k_seed_cells<<<pgrid, kBlock, 0, st>>>(g, cp_lists(ctx), ctx->changed);
     else k_seed_paths<<<pgrid, kBlock, 0, st>>>(g, PR, ctx->changed);
+    if (!cp && WR) {  // and the wall records' edges
+        k_seed_walls<<<pgrid, kBlock, 0, st>>>(g, *WR, ctx->changed);
+        ctx->launches++;
+    }
     for (int axis = 0; axis < 3; axis++) {
         const int n = axis == 0 ? g.W : axis == 1 ? g.H : g.D;
         k_dilate_axis<<<grid_for(g.V / n), kBlock, 0, st>>>(g, ctx->changed, axis, std::min(radius, n));
@@ -1930,7 +2177,10 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
     const int ps = opts->preserve_saddles, pvp = opts->preserve_vpath, pg = opts->preserve_geometry,
               filt = opts->filtration, pc = opts->preserve_connectors, pt = opts->preserve_type,
               et = opts->edit_type;
-    if (pc == 1) return fail(ctx, DMTZ_ERR_UNSUPPORTED, "preserve_connectors=1 is not supported");
+    // wall checks (preserve_connectors = 1) run in the separatrix phase; their
+    // searches are sized on the host, so such runs use the host-driven loop
+    const bool walls = pc == 1 && pvp == 1;
+    const bool use_graph = opts->use_graph && !walls;
     const int conn = (pvp == 1 && pg == 0) ? 1 : 0;  // connectivity-mode separatrices
     if (!(rel_eps >= 0.0) || !std::isfinite(rel_eps)) return fail(ctx, DMTZ_ERR_ARG, "rel_eps must be finite and >= 0");
     const i64 max_rounds = opts->max_rounds > 0 ? opts->max_rounds : 100000;
@@ -1992,9 +2242,12 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
     int converged = 1;
     const unsigned pgrid = persistent_grid();
     RuleCtx rc = rule_ctx(ctx, g, bound, et);
+    rc.range = range;
     const PathRec PR = path_rec(ctx);
+    if (walls && (s = ensure_walls(ctx)) != DMTZ_OK) return s;
+    const WallRec WR = wall_rec(ctx);
     auto cp_any = [&]() { return cc[0] > 0 || cc[1] > 0 || cc[2] > 0 || cc[3] > 0; };
-    if (opts->use_graph) {
+    if (use_graph) {
         // same loop, decided on the device (see run_graph_loop)
         LoopCtl c;
         memset(&c, 0, sizeof(c));
@@ -2058,7 +2311,7 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
     }
     // separatrix records of the last re-check, still valid while no round ran since
     bool paths_fresh = false;
-    while (!opts->use_graph && (n_as > 0 || n_ds > 0 || n_wall > 0 || cp_any())) {
+    while (!use_graph && (n_as > 0 || n_ds > 0 || n_wall > 0 || cp_any())) {
         if (rounds >= max_rounds) {
             converged = 0;
             break;
@@ -2100,13 +2353,19 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
         if (!paths_fresh) {  // else the last re-check ran on this same state
             pt_.begin(PH_PATH);
             detect_paths(ctx, g, rc, PR, pgrid, conn);
+            if (walls && (s = detect_walls(ctx, g, rc, n_wall)) != DMTZ_OK) return s;
             pt_.end();
         }
+        const i64 walls_fixed = walls ? n_wall : 0;
         paths_fresh = false;
         CK(cudaMemsetAsync(ctx->counters + 4, 0, sizeof(unsigned long long), st));
         CK(cudaMemsetAsync(ctx->counters + 7, 0, sizeof(unsigned long long), st));
         pt_.begin(PH_FIXPATH);
         k_fix_path<<<pgrid, kBlock, 0, st>>>(rc, PR);
+        if (walls_fixed > 0) {
+            k_fix_wall<<<pgrid, kBlock, 0, st>>>(rc, WR);
+            ctx->launches++;
+        }
         pt_.end();
         pt_.begin(PH_APPLY);
         k_apply<<<pgrid, kBlock, 0, st>>>(rc, range, pt, 1, ctx->changed, nullptr);
@@ -2116,8 +2375,10 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
         repair_dirty(ctx, g, Qs, ctx->P.crit, 1);
         pt_.end();
         if ((s = read_fit(1)) != DMTZ_OK) return s;
-        if (opts->break_stalls && hc[7] == 0 && rounds < max_rounds && hc[5] + hc[6] > 0) {
-            if ((s = break_stall(ctx, g, rc, PR, Qs, 0, 1, R.stall_breaks)) != DMTZ_OK) return s;
+        if (opts->break_stalls && hc[7] == 0 && rounds < max_rounds && hc[5] + hc[6] + walls_fixed > 0) {
+            if ((s = break_stall(ctx, g, rc, PR, Qs, 0, 1, R.stall_breaks, walls_fixed > 0 ? &WR : nullptr)) !=
+                DMTZ_OK)
+                return s;
             R.stall_breaks++;
             if ((s = read_fit(1)) != DMTZ_OK) return s;
         }
@@ -2130,6 +2391,7 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
             if ((s = read_counts()) != DMTZ_OK) return s;
             n_as = (i64)hc[5];
             n_ds = (i64)hc[6];
+            if (walls && (s = detect_walls(ctx, g, rc, n_wall)) != DMTZ_OK) return s;
             paths_fresh = true;
         }
     }
@@ -2153,6 +2415,7 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
     for (int k = 0; k < 4; k++) R.final_mismatch[k] = cc[k];
     R.final_paths[0] = n_as;
     R.final_paths[1] = n_ds;
+    R.final_walls = walls ? n_wall : 0;
     R.converged = converged;
     R.edited_vertices = (int64_t)n_edited;
     R.error_flags = err;
@@ -2188,7 +2451,7 @@ dmtz_status dmtz_quantize(dmtz_ctx *ctx, int W, int H, int D, const double *orig
         return fail(ctx, DMTZ_ERR_ARG, "rel_eps must be finite and >= 0, noise_frac in [0, 1]");
     CK(cudaSetDevice(ctx->device));
     if (!ctx->counters) {
-        CK(dalloc(&ctx->counters, 16));
+        CK(dalloc(&ctx->counters, 24));
         CK(dalloc(&ctx->errword, 1));
     }
     cudaStream_t st = ctx->stream;

@@ -38,6 +38,7 @@ struct RuleCtx {
     i64 reqcap;
     int *err;
     unsigned long long *progress;  // set when an update changes a value or an edit counter
+    double range;                  // max - min of the original field
 };
 
 // --------------------------------------------------------------- literal id arithmetic
@@ -721,6 +722,37 @@ __device__ inline void rule_ds_path(const RuleCtx &c, i64 v_idx) {
     i64 v1, v2;
     edge_verts(c.g, tpe, v1, v2);
     lower(c, v_idx == v1 ? v2 : v1);
+}
+
+// fix_ds_wall (main_3d.cu:5297-5413) for the wall record edge e: the edge's
+// original and decompressed pairings differ
+__device__ inline void rule_ds_wall(const RuleCtx &c, i64 e) {
+    const Grid &G = c.g;
+    const i64 tf = pe_ref(c, c.P, e), ff = pe_ref(c, c.Q, e);
+    if (tf == ff) return;
+    i64 v1, v2;
+    edge_verts(G, e, v1, v2);
+    if (tf >= 0 && ff >= 0 && tf < G.F && pf_ref(c, c.P, tf) == e && ff < G.F && pf_ref(c, c.Q, ff) == e) {
+        // both pair the edge with a face: lower the original face's third vertex,
+        // or both endpoints when that vertex has no room left
+        i64 a, b, v3;
+        tri_verts(G, tf, a, b, v3);
+        if (a != v1 && a != v2) v3 = a;
+        if (b != v1 && b != v2) v3 = b;
+        if (fabs(get_delta(c, v3)) > 1e-16 * c.range) {
+            lower(c, v3);
+        } else {
+            lower(c, v1);
+            lower(c, v2);
+        }
+    } else if (tf == -1 || tf >= G.F || (tf >= 0 && pf_ref(c, c.P, tf) != e)) {
+        lower(c, v1);
+        lower(c, v2);
+    } else if (ff == -1 || ff >= G.F || (ff >= 0 && pf_ref(c, c.Q, ff) != e)) {
+        i64 a, b, v3;
+        tri_verts(G, tf, a, b, v3);
+        lower(c, third_of(a, b, v3, v1, v2));
+    }
 }
 
 }  // namespace dmtz

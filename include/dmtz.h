@@ -39,7 +39,8 @@ typedef enum {
     DMTZ_ERR_BOUND = 6,         /* an output value violates the error bound */
     DMTZ_ERR_UNSUPPORTED = 7,   /* flag combination not implemented */
     DMTZ_ERR_OOB = 8,           /* the reference rules would index out of range here */
-    DMTZ_ERR_TOO_LARGE = 9      /* grid exceeds the fixed scratch of dmtz_extract_noalloc */
+    DMTZ_ERR_TOO_LARGE = 9      /* grid exceeds the fixed scratch of dmtz_extract_noalloc, or a
+                                   wall search outgrew its largest tier */
 } dmtz_status;
 
 typedef struct dmtz_ctx dmtz_ctx;
@@ -51,7 +52,9 @@ typedef struct {
     int preserve_vpath;       /* argv[5] */
     int preserve_geometry;    /* argv[6] */
     int filtration;           /* argv[7] */
-    int preserve_connectors;  /* argv[8]; 1 is rejected (DMTZ_ERR_UNSUPPORTED) */
+    int preserve_connectors;  /* argv[8]; 1 (with preserve_vpath = 1): wall checks of the
+                                 original 2-saddles in the separatrix phase (see
+                                 dmtz_wall_detect); such runs use the host-driven loop */
     int preserve_type;        /* argv[9] */
     int edit_type;            /* argv[10] */
     int max_rounds;           /* cap on fix/apply rounds; 0 = 100000 */
@@ -85,6 +88,7 @@ typedef struct {
                                    detection, critical-point fixes, separatrix detection,
                                    separatrix fixes, value update, set-up */
     int64_t stall_breaks;       /* rounds in which break_stalls reset values */
+    int64_t final_walls;        /* wall records left (preserve_connectors = 1) */
 } dmtz_report;
 
 /* Context: owns the device, a stream and all scratch memory.
@@ -142,6 +146,19 @@ dmtz_status dmtz_path_detect(dmtz_ctx *ctx, int W, int H, int D, const double *o
 dmtz_status dmtz_path_detect_connectivity(dmtz_ctx *ctx, int W, int H, int D, const double *orig,
                                           const double *decp, int64_t counts[2], int32_t *as_tet, int32_t *as_cur,
                                           int32_t *ds_edge, int32_t *ds_vert);
+
+/* Wall check of preserve_connectors = 1.  Replaces get_false_ds_wall
+ * (main_3d.cu:5064-5121), restated without its races (shared per-block stack,
+ * shared spill buffer, visited marks shared by all 2-saddles, record-index
+ * array aliasing the record array, launch covering only the first V faces):
+ * every original 2-saddle face runs its own depth-first search, in the
+ * reference's order, over the faces its original V-paths reach, and records
+ * the first edge whose original and decompressed pairings differ.
+ * count: records; w_sad / w_edge (capacity: the number of original
+ * 2-saddles, or the number of triangles) receive (2-saddle face, edge) pairs
+ * sorted by face.  Either array may be null. */
+dmtz_status dmtz_wall_detect(dmtz_ctx *ctx, int W, int H, int D, const double *orig, const double *decp,
+                             int64_t *count, int32_t *w_sad, int32_t *w_edge);
 
 /* The whole correction (main_3d.cu:6255-7149): extracts both complexes and
  * edits `decp` in place until they agree.  bound = (max(orig) - min(orig)) *

@@ -1527,6 +1527,124 @@ static void fix_ds_vpath(ctx_t *c, int v_idx) {
 }
 
 /* ---------------------------------------------------------------------------
+ * Walls (preserve_connectors = 1): get_false_ds_wall, main_3d.cu:5064-5121,
+ * and fix_ds_wall, main_3d.cu:5297-5413, restated without the races of the
+ * reference's detection (all threads of a block share one stack, all threads
+ * one spill buffer and one visited array; the record index array aliases the
+ * record array; the launch covers only the first V face ids).  Here every
+ * original 2-saddle face runs its own depth-first search with its own stack
+ * and visited marks, in the reference's order: pop a face; if it was not
+ * visited yet, check its edges (v1 v2), (v1 v3), (v2 v3) of its descending
+ * vertex triple; an originally critical edge is skipped; the first edge whose
+ * original and decompressed pairings differ is the record; otherwise the face
+ * the edge is originally paired with (if any, and not this face) is pushed.
+ * ------------------------------------------------------------------------- */
+static int wall_edges(const grid_t *G, int t, int e[3]) {
+    int v1, v2, v3, x1, y1, z1, x2, y2, z2, x3, y3, z3;
+    tri_verts(G, t, &v1, &v2, &v3);
+    coords(G, v1, &x1, &y1, &z1);
+    coords(G, v2, &x2, &y2, &z2);
+    coords(G, v3, &x3, &y3, &z3);
+    e[0] = edge_id(G, x1, y1, z1, x2, y2, z2);
+    e[1] = edge_id(G, x1, y1, z1, x3, y3, z3);
+    e[2] = edge_id(G, x2, y2, z2, x3, y3, z3);
+    return 3;
+}
+
+/* the record edge of 2-saddle `sad`, or -1; stamp[] holds sad + 1 on the
+ * faces this search visited */
+static int wall_search(ctx_t *c, int sad, int *stamp, int **stack, long long *cap, long long *pops) {
+    const grid_t *G = &c->G;
+    long long top = 0;
+    (*stack)[top++] = sad;
+    while (top > 0) {
+        const int t = (*stack)[--top];
+        (*pops)++;
+        if (stamp[t] == sad + 1) continue;
+        stamp[t] = sad + 1;
+        int e[3];
+        wall_edges(G, t, e);
+        for (int k = 0; k < 3; k++) {
+            const int j = e[k];
+            const int pe = PEa(j);
+            if (pe == -1) continue;
+            if (pe != QEa(j)) return j;
+            if (pe != t && pe >= 0 && pe < G->F && PFa(pe) == j) {
+                if (top == *cap) {
+                    *cap *= 2;
+                    *stack = (int *)realloc(*stack, sizeof(int) * (size_t)*cap);
+                }
+                (*stack)[top++] = pe;
+            }
+        }
+    }
+    return -1;
+}
+
+static int wall_detect(ctx_t *c, int *w_sad, int *w_edge, long long *pops) {
+    const grid_t *G = &c->G;
+    int *stamp = (int *)calloc((size_t)G->F, sizeof(int));
+    long long cap = 1024;
+    int *stack = (int *)malloc(sizeof(int) * (size_t)cap);
+    int n = 0;
+    for (int i = 0; i < G->F; i++) {
+        if (c->PF[i] != -1) continue;
+        const int j = wall_search(c, i, stamp, &stack, &cap, pops);
+        if (j >= 0) {
+            if (w_sad) w_sad[n] = i;
+            if (w_edge) w_edge[n] = j;
+            n++;
+        }
+    }
+    free(stamp);
+    free(stack);
+    return n;
+}
+
+int orc_wall_detect(int W, int H, int D, const int *PV, const int *PE, const int *PF, const int *PT, const int *QV,
+                    const int *QE, const int *QF, const int *QT, int *count, int *w_sad, int *w_edge,
+                    long long *pops) {
+    ctx_t cc;
+    ctx_t *c = &cc;
+    memset(c, 0, sizeof(*c));
+    grid_init(&c->G, W, H, D);
+    c->PV = PV; c->PE = PE; c->PF = PF; c->PT = PT;
+    c->QV = QV; c->QE = QE; c->QF = QF; c->QT = QT;
+    long long p = 0;
+    *count = wall_detect(c, w_sad, w_edge, &p);
+    if (pops) *pops = p;
+    return c->oob;
+}
+
+/* fix_ds_wall, main_3d.cu:5297-5413, for the record edge e */
+static void fix_ds_wall(ctx_t *c, int e) {
+    const grid_t *G = &c->G;
+    const int tf = PEa(e), ff = QEa(e);
+    if (tf == ff) return;
+    int v1, v2;
+    edge_verts(G, e, &v1, &v2);
+    if (tf >= 0 && ff >= 0 && tf < G->F && PFa(tf) == e && ff < G->F && QFa(ff) == e) {
+        int a, b, v3;
+        tri_verts(G, tf, &a, &b, &v3);
+        if (a != v1 && a != v2) v3 = a;
+        if (b != v1 && b != v2) v3 = b;
+        if (fabs(get_delta(c, v3)) > 1e-16 * c->range) {
+            lower(c, v3);
+        } else {
+            lower(c, v1);
+            lower(c, v2);
+        }
+    } else if (tf == -1 || tf >= G->F || (tf >= 0 && PFa(tf) != e)) {
+        lower(c, v1);
+        lower(c, v2);
+    } else if (ff == -1 || ff >= G->F || (ff >= 0 && QFa(ff) != e)) {
+        int a, b, v3;
+        tri_verts(G, tf, &a, &b, &v3);
+        lower(c, third_of(a, b, v3, v1, v2));
+    }
+}
+
+/* ---------------------------------------------------------------------------
  * A7: applyDeltaBuffer1, main_3d.cu:1122-1164
  * ------------------------------------------------------------------------- */
 /* returns 1 when some value or edit counter changed (0: the round was a fixed point) */
@@ -1609,7 +1727,7 @@ int orc_correct_ex(int W, int H, int D, const double *f, double *g, double rel_e
     for (int i = 0; i < 9; i++) stats[i] = 0;
     long long breaks = 0;
     unsigned char *mark = NULL;
-    if (pc == 1) return -1;
+    const int walls = pc == 1 && pv == 1; /* wall checks run in the separatrix phase */
     const int conn = pv == 1 && pg == 0; /* connectivity-mode separatrices */
     if (max_outer <= 0) max_outer = 100000;
     grid_t G;
@@ -1636,6 +1754,9 @@ int orc_correct_ex(int W, int H, int D, const double *f, double *g, double rel_e
     int *as_cur = (int *)malloc(sizeof(int) * (size_t)G.F);
     int *ds_e = (int *)malloc(sizeof(int) * (size_t)G.E);
     int *ds_v = (int *)malloc(sizeof(int) * (size_t)G.E);
+    int *w_sad = walls ? (int *)malloc(sizeof(int) * (size_t)G.F) : NULL;
+    int *w_edge = walls ? (int *)malloc(sizeof(int) * (size_t)G.F) : NULL;
+    long long wall_pops = 0;
     int *cnt = (int *)malloc(sizeof(int) * V);
     double *buf = (double *)malloc(sizeof(double) * V);
     long long oob = 0;
@@ -1762,17 +1883,18 @@ int orc_correct_ex(int W, int H, int D, const double *f, double *g, double rel_e
         }
         n_as = pc2[0];
         n_ds = pc2[1];
-        n_wall = 0;
+        n_wall = walls ? wall_detect(&c, w_sad, w_edge, &wall_pops) : 0;
         rounds++;
         for (size_t i = 0; i < V; i++) buf[i] = sentinel;
         c.oob = 0;
         for (int i = 0; i < n_as; i++) fix_as_vpath(&c, as_cur[i]);
         for (int i = 0; i < n_ds; i++) fix_ds_vpath(&c, ds_v[i]);
+        for (int i = 0; i < n_wall; i++) fix_ds_wall(&c, w_edge[i]);
         oob += c.oob;
         const int progress = apply_buffer(&G, f, g, cnt, buf, bound, range, pt);
         oob += pair_all(&G, g, QV, QE, QF, QT, nthreads);
         orc_cp_mismatch(W, H, D, PV, PE, PF, PT, QV, QE, QF, QT, cc4, lmin, lsad, l2s, lmax);
-        if (break_stalls && !progress && rounds < round_cap && n_as + n_ds > 0) {
+        if (break_stalls && !progress && rounds < round_cap && n_as + n_ds + n_wall > 0) {
             /* seeds: the records' current tetrahedra and trouble makers */
             if (!mark) mark = (unsigned char *)malloc(V);
             memset(mark, 0, V);
@@ -1783,12 +1905,17 @@ int orc_correct_ex(int W, int H, int D, const double *f, double *g, double rel_e
             }
             for (int i = 0; i < n_ds; i++)
                 if (ds_v[i] >= 0 && ds_v[i] < G.V) mark[ds_v[i]] = 1;
+            for (int i = 0; i < n_wall; i++) {
+                int a, b;
+                edge_verts(&G, w_edge[i], &a, &b);
+                mark[a] = mark[b] = 1;
+            }
             snap_box(&G, f, g, mark, stall_radius(&G, breaks));
             breaks++;
             oob += pair_all(&G, g, QV, QE, QF, QT, nthreads);
             orc_cp_mismatch(W, H, D, PV, PE, PF, PT, QV, QE, QF, QT, cc4, lmin, lsad, l2s, lmax);
         }
-        n_as = n_ds = 0;
+        n_as = n_ds = n_wall = 0;
         if (cc4[0] == 0 && cc4[1] == 0 && cc4[2] == 0 && cc4[3] == 0) {
             if (conn) {
                 c.oob = 0;
@@ -1799,6 +1926,7 @@ int orc_correct_ex(int W, int H, int D, const double *f, double *g, double rel_e
             }
             n_as = pc2[0];
             n_ds = pc2[1];
+            n_wall = walls ? wall_detect(&c, w_sad, w_edge, &wall_pops) : 0;
         }
     }
     stats[0] = total_ite;
@@ -1810,6 +1938,7 @@ int orc_correct_ex(int W, int H, int D, const double *f, double *g, double rel_e
     free(mark);
     free(P); free(Q); free(lmin); free(lsad); free(l2s); free(lmax);
     free(as_tet); free(as_cur); free(ds_e); free(ds_v); free(cnt); free(buf);
+    free(w_sad); free(w_edge);
     free(cmin); free(cmax);
     return 0;
 }
@@ -1882,6 +2011,23 @@ void orc_face_cofaces(int W, int H, int D, int n, const int *faces, int *out2) {
         cell_tetra(&c, faces[i], &x, &y);
         out2[2 * i] = x;
         out2[2 * i + 1] = y;
+    }
+}
+
+void orc_tri_verts(int W, int H, int D, int n, const int *faces, int *out3) {
+    grid_t G;
+    grid_init(&G, W, H, D);
+    for (int i = 0; i < n; i++) tri_verts(&G, faces[i], &out3[3 * i], &out3[3 * i + 1], &out3[3 * i + 2]);
+}
+
+void orc_edge_ids(int W, int H, int D, int n, const int *pairs, int *out) {
+    grid_t G;
+    grid_init(&G, W, H, D);
+    for (int i = 0; i < n; i++) {
+        int x, y, z, x1, y1, z1;
+        coords(&G, pairs[2 * i], &x, &y, &z);
+        coords(&G, pairs[2 * i + 1], &x1, &y1, &z1);
+        out[i] = edge_id(&G, x, y, z, x1, y1, z1);
     }
 }
 

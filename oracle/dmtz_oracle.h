@@ -76,11 +76,22 @@ int orc_path_detect(int W, int H, int D,
  *                out-of-bounds events, converged(1/0), initial mismatch
  *                counts min, saddle, 2saddle, max
  *   cnt_out    : out (optional): final per-vertex edit counter
- * preserve_connectors=1 is not supported (the reference path is racy);
- * returns -1 for it, else 0. */
+ * preserve_connectors=1 runs the wall checks of orc_wall_detect in the
+ * separatrix phase (with preserve_vpath=1).  Returns 0. */
 int orc_correct(int W, int H, int D, const double *f, double *g,
                 double rel_eps, const int flags[7], int max_outer,
                 int nthreads, long long stats[8], int *cnt_out);
+/* id helpers: descending vertex triples of faces; edge ids of vertex pairs */
+void orc_tri_verts(int W, int H, int D, int n, const int *faces, int *out3);
+void orc_edge_ids(int W, int H, int D, int n, const int *pairs, int *out);
+/* Walls of the original 2-saddles (get_false_ds_wall without its races):
+ * per 2-saddle face, its own depth-first search over faces reachable by
+ * original V-paths; the first edge whose original and decompressed pairings
+ * differ is the record (w_sad[k], w_edge[k]); *count records, pops = stack
+ * pops of all searches.  Returns the number of out-of-range reads. */
+int orc_wall_detect(int W, int H, int D, const int *PV, const int *PE, const int *PF, const int *PT, const int *QV,
+                    const int *QE, const int *QF, const int *QT, int *count, int *w_sad, int *w_edge,
+                    long long *pops);
 /* orc_correct with stall breaking (break_stalls = 1: a round that changes no
  * value and no edit counter resets a box around the remaining mismatches to
  * the original values; stats[8] = such breaks). */

@@ -54,6 +54,10 @@ def lib():
         L.orc_correct_ex.argtypes = [ctypes.c_int] * 3 + [_f64p, _f64p, ctypes.c_double, _i32p, ctypes.c_int,
                                                            ctypes.c_int, ctypes.c_int, _i64p, _i32p]
         L.orc_correct_ex.restype = ctypes.c_int
+        L.orc_tri_verts.argtypes = [ctypes.c_int] * 4 + [_i32p, _i32p]
+        L.orc_edge_ids.argtypes = [ctypes.c_int] * 4 + [_i32p, _i32p]
+        L.orc_wall_detect.argtypes = [ctypes.c_int] * 3 + [_i32p] * 8 + [_i32p, _i32p, _i32p, _i64p]
+        L.orc_wall_detect.restype = ctypes.c_int
         L.orc_labels.argtypes = [ctypes.c_int] * 3 + [_f64p, _i32p, _i32p, ctypes.c_int]
         L.orc_labels.restype = ctypes.c_int
         L.orc_face_cofaces.argtypes = [ctypes.c_int] * 4 + [_i32p, _i32p]
@@ -147,6 +151,35 @@ def correct(f, g, dims, rel_eps, flags, max_outer=0, threads=1, break_stalls=Fal
     stats = dict(outer_iterations=int(st[0]), cp_iterations=int(st[1]), oob=int(st[2]), converged=bool(st[3]),
                  initial_mismatch=[int(x) for x in st[4:8]], stall_breaks=int(st[8]))
     return gg, stats, cnt
+
+
+def tri_verts(faces, dims):
+    """Descending vertex triples of faces -> (n, 3) int32."""
+    f = np.ascontiguousarray(faces, np.int32)
+    out = np.empty((max(f.size, 1), 3), np.int32)
+    lib().orc_tri_verts(*dims, int(f.size), f if f.size else np.zeros(1, np.int32), out)
+    return out[: f.size]
+
+
+def edge_ids(pairs, dims):
+    """Edge ids of adjacent vertex pairs ((n, 2) array)."""
+    p = np.ascontiguousarray(pairs, np.int32).reshape(-1, 2)
+    out = np.empty(max(len(p), 1), np.int32)
+    lib().orc_edge_ids(*dims, len(p), p if len(p) else np.zeros((1, 2), np.int32), out)
+    return out[: len(p)]
+
+
+def wall_detect(P, Q, dims):
+    """Wall records of the original 2-saddles: (saddle faces, record edges,
+    stack pops of all searches, out-of-range reads)."""
+    W, H, D = dims
+    V, E, F, T = counts(dims)
+    c = np.zeros(1, np.int32)
+    ws, we = np.empty(max(F, 1), np.int32), np.empty(max(F, 1), np.int32)
+    pops = np.zeros(1, np.int64)
+    oob = lib().orc_wall_detect(W, H, D, *P, *Q, c, ws, we, pops)
+    n = int(c[0])
+    return ws[:n].copy(), we[:n].copy(), int(pops[0]), oob
 
 
 def labels(data, dims, threads: int = 1):

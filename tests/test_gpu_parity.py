@@ -158,9 +158,6 @@ def test_rejects_bad_input(gpu_ctx):
     with pytest.raises(dm.DmtzError) as e:
         gpu_ctx.correct(f, g, 0.1, dims=(3, 3, 3))
     assert e.value.status == 2
-    with pytest.raises(dm.DmtzError) as e:
-        gpu_ctx.correct(f, f, 0.1, flags=(1, 1, 1, 0, 1, 0, 0), dims=(3, 3, 3))
-    assert e.value.status == 7
     with pytest.raises(dm.DmtzError):
         gpu_ctx.extract(np.zeros(4), dims=(1, 2, 2))
 
