@@ -147,7 +147,7 @@ def correct(f, g, dims, rel_eps, flags, max_outer=0, threads=1, break_stalls=Fal
     rc = lib().orc_correct_ex(W, H, D, ff, gg, float(rel_eps), fl, int(max_outer), int(threads), int(bool(break_stalls)),
                               st, cnt)
     if rc != 0:
-        raise ValueError("flag combination not supported by the oracle (preserve_connectors=1)")
+        raise ValueError(f"oracle correction failed ({rc})")
     stats = dict(outer_iterations=int(st[0]), cp_iterations=int(st[1]), oob=int(st[2]), converged=bool(st[3]),
                  initial_mismatch=[int(x) for x in st[4:8]], stall_breaks=int(st[8]))
     return gg, stats, cnt
