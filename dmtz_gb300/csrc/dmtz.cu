@@ -46,7 +46,7 @@ struct Lists {
 };
 
 __device__ __forceinline__ void push_list(const Lists &L, int k, i64 id) {
-    const unsigned long long at = atomicAdd(&L.n[k], 1ull);
+    const unsigned long long at = agg_slot(&L.n[k]);
     if ((i64)at < L.cap[k]) L.l[k][at] = id;
 }
 
@@ -232,6 +232,27 @@ __device__ __forceinline__ uint8_t asc_step(const Grid &g, int x, int y, int z, 
     if (!cell_ok(g, x + dx, y + dy, z + dz, 1, 1, 1)) return 255;
     return (uint8_t)(((dx + 1) + 3 * (dy + 1) + 9 * (dz + 1)) * 6 + oc[3]);
 }
+// asc_step with the tetrahedron slot TS fixed at compile time: the facet and
+// coface tables become immediates (runtime-indexed table reads with different
+// indices across a warp are served one index at a time)
+template <int TS>
+__device__ __forceinline__ uint8_t asc_step_c(const Grid &g, int x, int y, int z, uint32_t tc) {
+    const int j = (tc >> (3 * TS)) & 7;
+    uint8_t out = 255;
+    DMTZ_FOR(4, J, {
+        constexpr int jj = decltype(J)::value;
+        constexpr int fs = cxt::TOPO_TET_FACE[TS][jj][3], other = 1 - cxt::TOPO_TET_FACE[TS][jj][4];
+        if constexpr (other < cxt::TOPO_FACE_NCOF[fs]) {
+            constexpr int dx = cxt::TOPO_TET_FACE[TS][jj][0] + cxt::TOPO_FACE_COF[fs][other][0],
+                          dy = cxt::TOPO_TET_FACE[TS][jj][1] + cxt::TOPO_FACE_COF[fs][other][1],
+                          dz = cxt::TOPO_TET_FACE[TS][jj][2] + cxt::TOPO_FACE_COF[fs][other][2],
+                          os = cxt::TOPO_FACE_COF[fs][other][3];
+            constexpr uint8_t code = (uint8_t)(((dx + 1) + 3 * (dy + 1) + 9 * (dz + 1)) * 6 + os);
+            if (j == jj) out = cell_ok(g, x + dx, y + dy, z + dz, 1, 1, 1) ? code : (uint8_t)255;
+        }
+    });
+    return out;
+}
 __global__ void k_path_succ(Grid g, const uint32_t *tcodeP, uint8_t *succ) {
     i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= g.V) return;
@@ -240,37 +261,63 @@ __global__ void k_path_succ(Grid g, const uint32_t *tcodeP, uint8_t *succ) {
     const bool cube = cell_ok(g, x, y, z, 1, 1, 1);
     const uint32_t tc = tcodeP[v];
     uint64_t packed = 0xFFFF000000000000ull;
-    for (int ts = 0; ts < 6; ts++) {
-        const uint8_t out = cube ? asc_step(g, x, y, z, ts, tc) : (uint8_t)255;
+    DMTZ_FOR(6, TS, {
+        constexpr int ts = decltype(TS)::value;
+        const uint8_t out = cube ? asc_step_c<ts>(g, x, y, z, tc) : (uint8_t)255;
         packed |= (uint64_t)out << (8 * ts);
-    }
+    });
     reinterpret_cast<uint64_t *>(succ)[v] = packed;
 }
 
 // compact list of the original 2-saddle triangles (anchor * 12 + slot)
 __global__ void k_sad2_list(Grid g, const uint32_t *critP, i64 *list, i64 cap, unsigned long long *n) {
-    // every lane of every warp takes part (block size is a multiple of 32);
-    // lanes past the end contribute nothing.  One atomic per warp: a single
-    // counter takes every append.
-    const i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t m = v < g.V ? (critP[v] >> 8) & 0xFFFu : 0u;
-    const unsigned lane = threadIdx.x & 31, full = 0xffffffffu;
-    const unsigned mine = __popc(m);
-    unsigned incl = mine;
-    for (int off = 1; off < 32; off <<= 1) {
-        const unsigned y = __shfl_up_sync(full, incl, off);
-        if (lane >= (unsigned)off) incl += y;
-    }
-    const unsigned total = __shfl_sync(full, incl, 31);
-    unsigned long long base = 0;
-    if (lane == 31 && total) base = atomicAdd(n, (unsigned long long)total);
-    base = __shfl_sync(full, base, 31);
-    unsigned long long at = base + incl - mine;
-    while (m) {
-        const int sl = __ffs(m) - 1;
-        m &= m - 1;
-        if ((i64)at < cap) list[at] = v * 12 + sl;
-        at++;
+    // a block takes kBlock x 8 consecutive anchors per step: each thread
+    // counts its 8 anchors' 2-saddles, a block scan places them in anchor
+    // order, and one atomic per block step reserves the block's range (one
+    // atomic per warp over the whole grid serialised this kernel on the
+    // counter)
+    __shared__ unsigned wtot[kBlock / 32];
+    __shared__ unsigned long long bbase;
+    const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5, full = 0xffffffffu;
+    const i64 per = (i64)kBlock * 8;
+    for (i64 b0 = (i64)blockIdx.x * per; b0 < g.V; b0 += (i64)gridDim.x * per) {
+        const i64 v0 = b0 + (i64)threadIdx.x * 8;
+        uint32_t m[8];
+        unsigned mine = 0;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            m[j] = v0 + j < g.V ? (critP[v0 + j] >> 8) & 0xFFFu : 0u;
+            mine += __popc(m[j]);
+        }
+        unsigned incl = mine;
+        for (int off = 1; off < 32; off <<= 1) {
+            const unsigned y = __shfl_up_sync(full, incl, off);
+            if (lane >= (unsigned)off) incl += y;
+        }
+        if (lane == 31) wtot[warp] = incl;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned long long t = 0;
+            for (int w = 0; w < kBlock / 32; w++) {
+                const unsigned c = wtot[w];
+                wtot[w] = (unsigned)t;
+                t += c;
+            }
+            bbase = t ? atomicAdd(n, t) : 0ull;
+        }
+        __syncthreads();
+        unsigned long long at = bbase + wtot[warp] + incl - mine;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            uint32_t mm = m[j];
+            while (mm) {
+                const int sl = __ffs(mm) - 1;
+                mm &= mm - 1;
+                if ((i64)at < cap) list[at] = (v0 + j) * 12 + sl;
+                at++;
+            }
+        }
+        __syncthreads();  // wtot and bbase are reused by the next step
     }
 }
 
@@ -1498,7 +1545,7 @@ dmtz_status prep_paths(dmtz_ctx *ctx, const Grid &g) {
     }
     CK(cudaMemsetAsync(ctx->counters + 10, 0, sizeof(unsigned long long), st));
     k_path_succ<<<grid_for(g.V), kBlock, 0, st>>>(g, ctx->P.tcode, ctx->succ);
-    k_sad2_list<<<grid_for(g.V), kBlock, 0, st>>>(g, ctx->P.crit, ctx->sad2, ctx->capSad2, ctx->counters + 10);
+    k_sad2_list<<<persistent_grid(), kBlock, 0, st>>>(g, ctx->P.crit, ctx->sad2, ctx->capSad2, ctx->counters + 10);
     ctx->launches += 3;
     CK(cudaGetLastError());
     return DMTZ_OK;

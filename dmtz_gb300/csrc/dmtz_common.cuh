@@ -25,6 +25,37 @@ namespace dmtz {
 
 typedef long long i64;
 
+// Unsigned division by a divisor fixed for the whole grid, as a multiply-high
+// and two shifts (Granlund and Montgomery, "Division by Invariant Integers
+// using Multiplication", PLDI 1994, the N-bit round-up method of their
+// Figure 4.1 with N = 64): with l = ceil(log2 d), m = floor(2^64 (2^l - d) / d)
+// + 1, t = mulhi(m, n), q = (t + ((n - t) >> min(l, 1))) >> max(l - 1, 0) for
+// every 64-bit n.  The id decodes below divide by grid extents; a 64-bit
+// hardware division is a long instruction sequence on the GPU.
+struct FDiv {
+    unsigned long long d, m;
+    int s1, s2;
+};
+static inline FDiv make_fdiv(unsigned long long d) {
+    int l = 0;
+    while (l < 64 && (1ull << l) < d) l++;
+    const unsigned __int128 num = ((unsigned __int128)1 << 64) * (((unsigned __int128)1 << l) - d);
+    FDiv f;
+    f.d = d;
+    f.m = (unsigned long long)(num / d) + 1;
+    f.s1 = l < 1 ? l : 1;
+    f.s2 = l > 1 ? l - 1 : 0;
+    return f;
+}
+__host__ __device__ __forceinline__ unsigned long long fdiv(const FDiv &f, unsigned long long n) {
+#ifdef __CUDA_ARCH__
+    const unsigned long long t = __umul64hi(f.m, n);
+#else
+    const unsigned long long t = (unsigned long long)(((unsigned __int128)f.m * n) >> 64);
+#endif
+    return (t + ((n - t) >> f.s1)) >> f.s2;
+}
+
 struct Grid {
     int W, H, D;
     i64 WH, V, E, F, T;
@@ -38,6 +69,9 @@ struct Grid {
     int WHi;
     int doff32[14];
     int coff32[8];
+    // divisors of the id decodes: W, H, W-1, H-1, D-1, and the plane sizes
+    // (W-1)H, W(H-1), W(D-1), (H-1)(D-1), (W-1)(D-1), (W-1)(H-1)
+    FDiv dW, dH, dW1, dH1, dD1, dW1H, dWH1, dWD1, dH1D1, dW1D1, dW1H1;
 };
 
 static inline Grid make_grid(int W, int H, int D) {
@@ -65,6 +99,10 @@ static inline Grid make_grid(int W, int H, int D) {
     g.WHi = g.small ? (int)g.WH : 0;
     for (int i = 0; i < 14; i++) g.doff32[i] = g.small ? (int)g.doff[i] : 0;
     for (int c8 = 0; c8 < 8; c8++) g.coff32[c8] = g.small ? (int)g.coff[c8] : 0;
+    g.dW = make_fdiv(w); g.dH = make_fdiv(h); g.dW1 = make_fdiv(w - 1); g.dH1 = make_fdiv(h - 1);
+    g.dD1 = make_fdiv(d - 1); g.dW1H = make_fdiv((w - 1) * h); g.dWH1 = make_fdiv(w * (h - 1));
+    g.dWD1 = make_fdiv(w * (d - 1)); g.dH1D1 = make_fdiv((h - 1) * (d - 1)); g.dW1D1 = make_fdiv((w - 1) * (d - 1));
+    g.dW1H1 = make_fdiv((w - 1) * (h - 1));
     return g;
 }
 
@@ -87,10 +125,19 @@ __host__ __device__ __forceinline__ uint64_t okey(double v) {
 #define DMTZ_KEY_DBL_MAX 0xFFEFFFFFFFFFFFFFull  // okey(DBL_MAX)
 
 __device__ __forceinline__ void decode_v(const Grid &g, i64 v, int &x, int &y, int &z) {
-    x = (int)(v % g.W);
-    i64 r = v / g.W;
-    y = (int)(r % g.H);
-    z = (int)(r / g.H);
+    const unsigned long long u = (unsigned long long)v, r = fdiv(g.dW, u), q = fdiv(g.dH, r);
+    x = (int)(u - r * g.dW.d);
+    y = (int)(r - q * g.dH.d);
+    z = (int)q;
+}
+// n = (hi * B + mid) * C + lo with 0 <= mid < B, 0 <= lo < C, by the plane
+// size BC and the row size C
+__device__ __forceinline__ void split3(unsigned long long n, const FDiv &bc, const FDiv &c, int &hi, int &mid,
+                                       int &lo) {
+    const unsigned long long h = fdiv(bc, n), r = n - h * bc.d, m = fdiv(c, r);
+    hi = (int)h;
+    mid = (int)m;
+    lo = (int)(r - m * c.d);
 }
 __device__ __forceinline__ bool inb(const Grid &g, int x, int y, int z) {
     return x >= 0 && x < g.W && y >= 0 && y < g.H && z >= 0 && z < g.D;
@@ -145,42 +192,57 @@ __host__ __device__ __forceinline__ i64 tet_ref(const Grid &g, i64 x, i64 y, i64
 }
 // valid edge id -> anchor + family
 __device__ __forceinline__ void edge_unref(const Grid &g, i64 e, int &x, int &y, int &z, int &k) {
-    const i64 W = g.W, H = g.H, D = g.D;
     k = 0;
     while (k < 6 && e >= g.eoff[k + 1]) k++;
-    i64 r = e - g.eoff[k];
+    const unsigned long long r = (unsigned long long)(e - g.eoff[k]);
     switch (k) {
-    case 0: z = (int)(r / ((W - 1) * H)); y = (int)((r % ((W - 1) * H)) / (W - 1)); x = (int)(r % (W - 1)); break;
-    case 1: z = (int)(r / (W * (H - 1))); x = (int)((r % (W * (H - 1))) / (H - 1)); y = (int)(r % (H - 1)); break;
-    case 2: y = (int)(r / (W * (D - 1))); x = (int)((r % (W * (D - 1))) / (D - 1)); z = (int)(r % (D - 1)); break;
-    case 4: x = (int)(r / ((H - 1) * (D - 1))); y = (int)((r % ((H - 1) * (D - 1))) / (D - 1)); z = (int)(r % (D - 1)); break;
-    case 5: y = (int)(r / ((W - 1) * (D - 1))); z = (int)((r % ((W - 1) * (D - 1))) / (W - 1)); x = (int)(r % (W - 1)); break;
-    default: z = (int)(r / ((W - 1) * (H - 1))); y = (int)((r % ((W - 1) * (H - 1))) / (W - 1)); x = (int)(r % (W - 1)); break;
+    case 0: split3(r, g.dW1H, g.dW1, z, y, x); break;
+    case 1: split3(r, g.dWH1, g.dH1, z, x, y); break;
+    case 2: split3(r, g.dWD1, g.dD1, y, x, z); break;
+    case 4: split3(r, g.dH1D1, g.dD1, x, y, z); break;
+    case 5: split3(r, g.dW1D1, g.dW1, y, z, x); break;
+    default: split3(r, g.dW1H1, g.dW1, z, y, x); break;
     }
 }
 __device__ __forceinline__ void face_unref(const Grid &g, i64 t, int &x, int &y, int &z, int &s) {
-    const i64 W = g.W, H = g.H, D = g.D;
     if (t < g.bxy) {
-        i64 b = t / 2; s = (int)(t % 2);
-        z = (int)(b / ((W - 1) * (H - 1))); y = (int)((b % ((W - 1) * (H - 1))) / (W - 1)); x = (int)(b % (W - 1));
+        const unsigned long long u = (unsigned long long)t;
+        s = (int)(u & 1);
+        split3(u >> 1, g.dW1H1, g.dW1, z, y, x);
     } else if (t < g.byz) {
-        i64 r = t - g.bxy, b = r / 2; s = 2 + (int)(r % 2);
-        x = (int)(b / ((H - 1) * (D - 1))); y = (int)((b % ((H - 1) * (D - 1))) / (D - 1)); z = (int)(b % (D - 1));
+        const unsigned long long r = (unsigned long long)(t - g.bxy);
+        s = 2 + (int)(r & 1);
+        split3(r >> 1, g.dH1D1, g.dD1, x, y, z);
     } else if (t < g.bxz) {
-        i64 r = t - g.byz, b = r / 2; s = 4 + (int)(r % 2);
-        y = (int)(b / ((W - 1) * (D - 1))); z = (int)((b % ((W - 1) * (D - 1))) / (W - 1)); x = (int)(b % (W - 1));
+        const unsigned long long r = (unsigned long long)(t - g.byz);
+        s = 4 + (int)(r & 1);
+        split3(r >> 1, g.dW1D1, g.dW1, y, z, x);
     } else {
-        i64 r = t - g.bxz, b = r / 6; s = 6 + (int)(r % 6);
-        z = (int)(b / ((W - 1) * (H - 1))); y = (int)((b % ((W - 1) * (H - 1))) / (W - 1)); x = (int)(b % (W - 1));
+        const unsigned long long r = (unsigned long long)(t - g.bxz), b = r / 6;
+        s = 6 + (int)(r - 6 * b);
+        split3(b, g.dW1H1, g.dW1, z, y, x);
     }
 }
 __device__ __forceinline__ void tet_unref(const Grid &g, i64 t, int &x, int &y, int &z, int &s) {
-    const i64 W = g.W, H = g.H;
-    i64 b = t / 6; s = (int)(t % 6);
-    z = (int)(b / ((W - 1) * (H - 1))); y = (int)((b % ((W - 1) * (H - 1))) / (W - 1)); x = (int)(b % (W - 1));
+    const unsigned long long u = (unsigned long long)t, b = u / 6;
+    s = (int)(u - 6 * b);
+    split3(b, g.dW1H1, g.dW1, z, y, x);
 }
 
 // packed field accessors
+// A slot in a list whose length is *n: the converged lanes appending to the
+// same counter take one atomic between them (the leader's), so that a list
+// filled from every warp does not serialise on one address.
+__device__ __forceinline__ unsigned long long agg_slot(unsigned long long *n) {
+    const unsigned act = __activemask();
+    const unsigned peers = __match_any_sync(act, (unsigned long long)(uintptr_t)n);
+    const int leader = __ffs(peers) - 1;
+    const unsigned lane = threadIdx.x & 31u;
+    unsigned long long base = 0;
+    if ((int)lane == leader) base = atomicAdd(n, (unsigned long long)__popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    return base + (unsigned long long)__popc(peers & ((1u << lane) - 1u));
+}
 __device__ __forceinline__ int eup_get(uint32_t w, int k) { return (w >> (3 * k)) & 7; }
 __device__ __forceinline__ int fup_get(uint32_t w, int s) { return (w >> (2 * s)) & 3; }
 

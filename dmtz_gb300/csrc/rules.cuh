@@ -271,7 +271,7 @@ __device__ __forceinline__ void lower(const RuleCtx &c, i64 v) {
     const uint32_t bit = 1u << (v & 31);
     const uint32_t old = atomicOr(&c.reqbits[v >> 5], bit);
     if (!(old & bit)) {
-        const unsigned long long k = atomicAdd(c.reqn, 1ull);
+        const unsigned long long k = agg_slot(c.reqn);
         if ((i64)k < c.reqcap) c.reqlist[k] = v;
     }
 }
