@@ -674,30 +674,87 @@ __global__ void k_conn_as(Grid g, const uint32_t *critP, const uint32_t *critQ, 
     }
 }
 
-// k_path_as split in two for parallelism: one thread per (2-saddle, coface)
-// walks (res = the first differing tetrahedron, -1 none, -2 no coface), then
-// one thread per 2-saddle keeps the first coface in search order that has
-// one: the same records.
+// k_path_as split in two for parallelism: (2-saddle, coface) walks (res = the
+// first differing tetrahedron, -1 none, -2 no coface), then one thread per
+// 2-saddle keeps the first coface in search order that has one: the same
+// records.  Walk lengths vary a lot, so a lane whose walk ends takes the next
+// walk of its warp's contiguous range of walks instead of idling until the
+// warp's longest walk ends (one step per loop turn; the warp refills its free
+// lanes together, without atomics).
 __global__ void k_path_as_walk(Grid g, const i64 *sad2, const unsigned long long *nsad, const uint32_t *tcP,
                                const uint32_t *tcQ, const uint8_t *succ, i64 *res, i64 cap, int *err) {
     const i64 n = 2 * (i64)*nsad;
-    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
-        const i64 code = sad2[i >> 1];
-        const int j = (int)(i & 1);
-        const i64 v = code / 12;
-        const int sl = (int)(code % 12);
-        i64 r = -2;
-        if (j < TOPO_FACE_NCOF[sl]) {
-            int x, y, z;
-            decode_v(g, v, x, y, z);
-            const signed char *tc = TOPO_FACE_COF[sl][j];
-            const int cx = x + tc[0], cy = y + tc[1], cz = z + tc[2], cs = tc[3];
-            if (cell_ok(g, cx, cy, cz, 1, 1, 1)) {
-                i64 cur;
-                r = first_diff(g, tcP, tcQ, succ, cx, cy, cz, cs, cap, err, cur) ? cur : -1;
+    const unsigned full = 0xffffffffu, lane = threadIdx.x & 31u;
+    const i64 nwarps = ((i64)gridDim.x * blockDim.x) >> 5;
+    const i64 warp = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const i64 chunk = (n + nwarps - 1) / nwarps;
+    i64 pos = warp * chunk;                      // next walk of this warp's range (same in every lane)
+    const i64 end = min(n, pos + chunk);
+    i64 item = -1, steps = 0;
+    int x = 0, y = 0, z = 0, s = 0;
+    bool drained = false;
+    while (true) {
+        const unsigned want = __ballot_sync(full, item < 0 && !drained);
+        if (want) {
+            if (item < 0 && !drained) {
+                const i64 my = pos + __popc(want & ((1u << lane) - 1u));
+                if (my < end) {
+                    item = my;
+                    steps = 0;
+                    const i64 code = sad2[my >> 1];
+                    const int j = (int)(my & 1);
+                    int vx, vy, vz;
+                    decode_v(g, code / 12, vx, vy, vz);
+                    const int sl = (int)(code % 12);
+                    bool ok = false;
+                    if (j < TOPO_FACE_NCOF[sl]) {
+                        const signed char *tc = TOPO_FACE_COF[sl][j];
+                        x = vx + tc[0];
+                        y = vy + tc[1];
+                        z = vz + tc[2];
+                        s = tc[3];
+                        ok = cell_ok(g, x, y, z, 1, 1, 1);
+                    }
+                    if (!ok) {
+                        res[item] = -2;
+                        item = -1;
+                    }
+                } else {
+                    drained = true;
+                }
+            }
+            pos += __popc(want);
+        }
+        if (__all_sync(full, item < 0 && drained)) break;
+        if (item >= 0) {  // one step of the walk
+            const i64 ci = x + (i64)y * g.W + (i64)z * g.WH;
+            const uint32_t wp = tcP[ci], wq = tcQ[ci];
+            const int s8 = succ[ci * 8 + s];
+            const int p = (wp >> (3 * s)) & 7;
+            i64 r = 0;
+            bool fin = true;
+            if (p == 7) {
+                r = -1;
+            } else if (p != (int)((wq >> (3 * s)) & 7)) {
+                r = tet_ref(g, x, y, z, s);
+            } else if (s8 == 255) {
+                r = -1;
+            } else if (++steps > cap) {
+                atomicOr(err, ERR_WALK);
+                r = -1;
+            } else {
+                const int d = s8 / 6;
+                s = s8 - 6 * d;
+                x += d % 3 - 1;
+                y += (d / 3) % 3 - 1;
+                z += d / 9 - 1;
+                fin = false;
+            }
+            if (fin) {
+                res[item] = r;
+                item = -1;
             }
         }
-        res[i] = r;
     }
 }
 __global__ void k_path_as_pick(Grid g, const i64 *sad2, const unsigned long long *nsad, const i64 *res, PathRec R) {
@@ -1562,7 +1619,7 @@ void launch_detect(dmtz_ctx *ctx, const Grid &g, const RuleCtx &rc, const PathRe
                                            g.T + 16, ctx->errword);
         k_conn_ds<<<grid, kBlock, 0, st>>>(rc, R, g.V + 16);
     } else {
-        k_path_as_walk<<<2 * grid, kBlock, 0, st>>>(g, ctx->sad2, ctx->counters + 10, ctx->P.tcode, ctx->Q.tcode,
+        k_path_as_walk<<<grid, kBlock, 0, st>>>(g, ctx->sad2, ctx->counters + 10, ctx->P.tcode, ctx->Q.tcode,
                                                     ctx->succ, ctx->as_res, g.T + 16, ctx->errword);
         k_path_as_pick<<<grid, kBlock, 0, st>>>(g, ctx->sad2, ctx->counters + 10, ctx->as_res, R);
         k_path_ds<<<grid, kBlock, 0, st>>>(rc, R);
