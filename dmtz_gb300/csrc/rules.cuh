@@ -23,6 +23,12 @@ namespace dmtz {
 
 enum { ERR_OOB = 1, ERR_WALK = 2 };
 
+// The fix rules are long, branchy code run by few lanes of a warp at a time;
+// with their id and pairing accessors inlined at every call site the fix
+// kernel outgrew the instruction cache (ncu: warps stalled on instruction
+// fetch).  The accessors are therefore compiled once and called.
+#define DMTZ_SHARED_CODE __noinline__
+
 struct RuleCtx {
     Grid g;
     FieldState P;      // original field gradient
@@ -43,7 +49,7 @@ struct RuleCtx {
 
 // --------------------------------------------------------------- literal id arithmetic
 // getVertexIDsFromEdgeID (main_3d.cu:1760-1900) for any id; (a > b)
-__device__ inline void edge_verts(const Grid &g, i64 e, i64 &a, i64 &b) {
+__device__ DMTZ_SHARED_CODE void edge_verts(const Grid &g, i64 e, i64 &a, i64 &b) {
     const i64 W = g.W, H = g.H, D = g.D;
     int k = -1;
     for (int i = 0; i < 7; i++)
@@ -86,7 +92,7 @@ __device__ __forceinline__ void sort_desc3(i64 &a, i64 &b, i64 &c) {
 }
 
 // getVerticesFromTriangleID (main_3d.cu:425-565) for any id, sorted descending
-__device__ inline void tri_verts(const Grid &g, i64 t, i64 &a, i64 &b, i64 &c) {
+__device__ DMTZ_SHARED_CODE void tri_verts(const Grid &g, i64 t, i64 &a, i64 &b, i64 &c) {
     const i64 W = g.W, H = g.H, D = g.D, WH = W * H;
     i64 v1 = 0, v2 = 0, v3 = 0, base, mx, my, mz;
     if (t < 2 * D * (W - 1) * (H - 1)) {
@@ -120,7 +126,7 @@ __device__ inline void tri_verts(const Grid &g, i64 t, i64 &a, i64 &b, i64 &c) {
 }
 
 // getVerticesFromTetrahedraID (main_3d.cu:672-740) for any id, sorted descending
-__device__ inline void tet_verts(const Grid &g, i64 t, i64 &a, i64 &b, i64 &c, i64 &d) {
+__device__ DMTZ_SHARED_CODE void tet_verts(const Grid &g, i64 t, i64 &a, i64 &b, i64 &c, i64 &d) {
     const i64 W = g.W, H = g.H, WH = W * H;
     const i64 base = t / 6;
     const i64 cz = base / ((W - 1) * (H - 1)), cy = (base % ((W - 1) * (H - 1))) / (W - 1), cx = base % (W - 1);
@@ -162,7 +168,7 @@ __device__ __forceinline__ i64 edge_ref_pair(const Grid &g, i64 a, i64 b) {
 }
 
 // paired_vertices[v]
-__device__ inline i64 pv_ref(const RuleCtx &c, const FieldState &s, i64 v) {
+__device__ DMTZ_SHARED_CODE i64 pv_ref(const RuleCtx &c, const FieldState &s, i64 v) {
     if (v < 0 || v >= c.g.V) {
         atomicOr(c.err, ERR_OOB);
         return -1;
@@ -172,7 +178,7 @@ __device__ inline i64 pv_ref(const RuleCtx &c, const FieldState &s, i64 v) {
     return edge_ref_pair(c.g, v, v + c.g.doff[d]);
 }
 // paired_edges[e]
-__device__ inline i64 pe_ref(const RuleCtx &c, const FieldState &s, i64 e) {
+__device__ DMTZ_SHARED_CODE i64 pe_ref(const RuleCtx &c, const FieldState &s, i64 e) {
     if (e < 0 || e >= c.g.E) {
         atomicOr(c.err, ERR_OOB);
         return -1;
@@ -192,7 +198,7 @@ __device__ inline i64 pe_ref(const RuleCtx &c, const FieldState &s, i64 e) {
     return -1;
 }
 // paired_faces[t]
-__device__ inline i64 pf_ref(const RuleCtx &c, const FieldState &s, i64 t) {
+__device__ DMTZ_SHARED_CODE i64 pf_ref(const RuleCtx &c, const FieldState &s, i64 t) {
     if (t < 0 || t >= c.g.F) {
         atomicOr(c.err, ERR_OOB);
         return -1;
@@ -213,7 +219,7 @@ __device__ inline i64 pf_ref(const RuleCtx &c, const FieldState &s, i64 t) {
     return -1;
 }
 // paired_tetrahedras[t]
-__device__ inline i64 pt_ref(const RuleCtx &c, const FieldState &s, i64 t) {
+__device__ DMTZ_SHARED_CODE i64 pt_ref(const RuleCtx &c, const FieldState &s, i64 t) {
     if (t < 0 || t >= c.g.T) {
         atomicOr(c.err, ERR_OOB);
         return -1;
@@ -298,7 +304,7 @@ __device__ __forceinline__ bool adjacent(const Grid &g, i64 a, i64 b, int &d) {
 
 // argmin over the common neighbours n of (v1, v2) with exactly one of v1, v2
 // above n in the ORIGINAL field (the rescan of fix_saddle, main_3d.cu:2942-3015)
-__device__ inline i64 rescan_edge(const RuleCtx &c, i64 v1, i64 v2) {
+__device__ DMTZ_SHARED_CODE i64 rescan_edge(const RuleCtx &c, i64 v1, i64 v2) {
     int x1, y1, z1, x2, y2, z2;
     decode_v(c.g, v1, x1, y1, z1);
     decode_v(c.g, v2, x2, y2, z2);
@@ -324,7 +330,7 @@ __device__ inline i64 rescan_edge(const RuleCtx &c, i64 v1, i64 v2) {
 
 // get_smallest_vertex (main_3d.cu:2115-2194): common neighbours of a triangle
 // below exactly two of its vertices in the ORIGINAL field, argmin
-__device__ inline i64 smallest_vertex(const RuleCtx &c, i64 v1, i64 v2, i64 v3) {
+__device__ DMTZ_SHARED_CODE i64 smallest_vertex(const RuleCtx &c, i64 v1, i64 v2, i64 v3) {
     int x1, y1, z1, x2, y2, z2, x3, y3, z3;
     decode_v(c.g, v1, x1, y1, z1);
     decode_v(c.g, v2, x2, y2, z2);
