@@ -509,28 +509,33 @@ __global__ void k_fix_wall(RuleCtx c, WallRec W) {
 __global__ void k_path_ds(RuleCtx c, PathRec R) {
     const Grid &g = c.g;
     for (i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x; v < g.V; v += (i64)gridDim.x * blockDim.x) {
-        uint32_t m = (c.P.crit[v] >> 1) & 0x7Fu;
+        const uint32_t m = (c.P.crit[v] >> 1) & 0x7Fu;
         if (!m) continue;
-        int x, y, z;
-        decode_v(g, v, x, y, z);
-        while (m) {
-            const int k = __ffs(m) - 1;
-            m &= m - 1;
-            const i64 ends[2] = {v + g.coff[TOPO_EDGE_V[k][0]], v + g.coff[TOPO_EDGE_V[k][1]]};
-            for (int j = 0; j < 2; j++) {
-                const i64 e = ends[j];
-                const int po = c.P.pv[e];
-                if (po == 15) continue;
-                if (po != c.Q.pv[e]) {
-                    const unsigned long long at = atomicAdd(&R.n[1], 1ull);
-                    if ((i64)at < R.cap_ds) {
-                        R.ds_edge[at] = edge_ref(g, x, y, z, k);
-                        R.ds_vert[at] = e;
+        // edge families unrolled: corner offsets from immediates, not from
+        // tables indexed by a per-lane family
+        DMTZ_FOR(7, K, {
+            constexpr int k = decltype(K)::value;
+            constexpr int c0 = cxt::TOPO_EDGE_V[k][0], c1 = cxt::TOPO_EDGE_V[k][1];
+            if ((m >> k) & 1u) {
+                const i64 ends[2] = {v + cxt::ccx(c0) + cxt::ccy(c0) * (i64)g.W + cxt::ccz(c0) * g.WH,
+                                     v + cxt::ccx(c1) + cxt::ccy(c1) * (i64)g.W + cxt::ccz(c1) * g.WH};
+                for (int j = 0; j < 2; j++) {
+                    const i64 e = ends[j];
+                    const int po = c.P.pv[e];
+                    if (po == 15) continue;
+                    if (po != c.Q.pv[e]) {
+                        const unsigned long long at = atomicAdd(&R.n[1], 1ull);
+                        if ((i64)at < R.cap_ds) {
+                            int x, y, z;
+                            decode_v(g, v, x, y, z);
+                            R.ds_edge[at] = edge_ref(g, x, y, z, k);
+                            R.ds_vert[at] = e;
+                        }
+                        break;
                     }
-                    break;
                 }
             }
-        }
+        });
     }
 }
 
@@ -674,6 +679,32 @@ __global__ void k_conn_as(Grid g, const uint32_t *critP, const uint32_t *critQ, 
     }
 }
 
+// start tetrahedron (anchor offset, slot) of coface j of a triangle of slot
+// sl, from four immediates (9 bits per (sl, j): dx+1, dy+1, dz+1, slot)
+// instead of a table read whose index differs across the warp
+__host__ __device__ constexpr unsigned long long cof_word(int w) {
+    unsigned long long r = 0;
+    for (int i = 0; i < 7; i++) {
+        const int q = w * 7 + i;
+        if (q >= 24) break;
+        const signed char *t = cxt::TOPO_FACE_COF[q / 2][q % 2];
+        r |= (unsigned long long)((t[0] + 1) | ((t[1] + 1) << 2) | ((t[2] + 1) << 4) | (t[3] << 6)) << (9 * i);
+    }
+    return r;
+}
+__device__ __forceinline__ void face_cof_start(int sl, int j, int &dx, int &dy, int &dz, int &ts) {
+    constexpr unsigned long long W0 = cof_word(0), W1 = cof_word(1), W2 = cof_word(2), W3 = cof_word(3);
+    const int q = 2 * sl + j, w = q / 7, i = q - 7 * w;
+    const unsigned long long word = w == 0 ? W0 : (w == 1 ? W1 : (w == 2 ? W2 : W3));
+    const unsigned v = (unsigned)(word >> (9 * i)) & 511u;
+    dx = (int)(v & 3u) - 1;
+    dy = (int)((v >> 2) & 3u) - 1;
+    dz = (int)((v >> 4) & 3u) - 1;
+    ts = (int)(v >> 6);
+}
+static_assert(cxt::TOPO_FACE_NCOF[0] == 2 && cxt::TOPO_FACE_NCOF[5] == 2 && cxt::TOPO_FACE_NCOF[11] == 2,
+              "every triangle slot has two cofaces");
+
 // k_path_as split in two for parallelism: (2-saddle, coface) walks (res = the
 // first differing tetrahedron, -1 none, -2 no coface), then one thread per
 // 2-saddle keeps the first coface in search order that has one: the same
@@ -703,18 +734,13 @@ __global__ void k_path_as_walk(Grid g, const i64 *sad2, const unsigned long long
                     steps = 0;
                     const i64 code = sad2[my >> 1];
                     const int j = (int)(my & 1);
-                    int vx, vy, vz;
+                    int vx, vy, vz, dx, dy, dz;
                     decode_v(g, code / 12, vx, vy, vz);
-                    const int sl = (int)(code % 12);
-                    bool ok = false;
-                    if (j < TOPO_FACE_NCOF[sl]) {
-                        const signed char *tc = TOPO_FACE_COF[sl][j];
-                        x = vx + tc[0];
-                        y = vy + tc[1];
-                        z = vz + tc[2];
-                        s = tc[3];
-                        ok = cell_ok(g, x, y, z, 1, 1, 1);
-                    }
+                    face_cof_start((int)(code % 12), j, dx, dy, dz, s);
+                    x = vx + dx;
+                    y = vy + dy;
+                    z = vz + dz;
+                    const bool ok = cell_ok(g, x, y, z, 1, 1, 1);
                     if (!ok) {
                         res[item] = -2;
                         item = -1;
