@@ -283,7 +283,7 @@ def run(out_dir, only=None, timeout=240, big=False):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("cmd", choices=["prepare", "build", "run"])
-    ap.add_argument("--out", default=os.path.join(REPO, "gpurun_out", "ref"))
+    ap.add_argument("--out", default=os.path.join(REPO, "ref_runs"))
     ap.add_argument("--only", nargs="*")
     ap.add_argument("--timeout", type=float, default=240)
     ap.add_argument("--big", action="store_true", help="run the large timing cases (no dumps)")

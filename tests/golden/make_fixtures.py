@@ -18,7 +18,7 @@ tests/golden/ref_<case>.npz per case holding
   file_*      (small cases) the reference's edit-index and edit-value files
               (data1<name>.bin or data<name>.bin, data_edits<name>.bin)
 
-Usage: python tests/golden/make_fixtures.py gpurun_out/ref
+Usage: python tests/golden/make_fixtures.py <directory of oracle/ref_harness.py run dumps>
 """
 import glob
 import hashlib
@@ -74,6 +74,6 @@ def convert(src, dst_dir=HERE):
 
 
 if __name__ == "__main__":
-    src_dir = sys.argv[1] if len(sys.argv) > 1 else "gpurun_out/ref"
+    src_dir = sys.argv[1] if len(sys.argv) > 1 else "ref_runs"
     for fn in sorted(glob.glob(os.path.join(src_dir, "*.npz"))):
         print(convert(fn))
