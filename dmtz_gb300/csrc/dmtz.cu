@@ -1201,6 +1201,8 @@ struct DevField {
 struct dmtz_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;      // copies that overlap the context stream's work
+    cudaEvent_t side_done = nullptr;
     std::string err;
     // sized buffers
     i64 capV = 0, capE = 0, capF = 0, capT = 0, capB = 0;
@@ -1749,6 +1751,18 @@ dmtz_status check_dims(dmtz_ctx *ctx, int W, int H, int D, Grid &g) {
     return DMTZ_OK;
 }
 
+// NaN / Inf test of a device field (the reference assumes finite input)
+dmtz_status check_finite(dmtz_ctx *ctx, const double *d, i64 n) {
+    CK(cudaMemsetAsync(ctx->errword, 0, sizeof(int), ctx->stream));
+    k_check_finite<<<persistent_grid(), kBlock, 0, ctx->stream>>>(d, n, ctx->errword);
+    ctx->launches++;
+    int bad = 0;
+    CK(cudaMemcpyAsync(&bad, ctx->errword, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (bad) return fail(ctx, DMTZ_ERR_ARG, "input contains NaN or Inf");
+    return DMTZ_OK;
+}
+
 dmtz_status upload(dmtz_ctx *ctx, double *dst, const double *src, i64 n, int on_device) {
     CK(cudaMemcpyAsync(dst, src, sizeof(double) * (size_t)n, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
                        ctx->stream));
@@ -1794,6 +1808,8 @@ void dmtz_ctx_destroy(dmtz_ctx *ctx) {
     cudaFree(ctx->bnd);
     cudaFree(ctx->loopctl);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    if (ctx->side) cudaStreamDestroy(ctx->side);
+    if (ctx->side_done) cudaEventDestroy(ctx->side_done);
     delete ctx;
 }
 
@@ -2321,7 +2337,15 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
     if ((s = upload(ctx, ctx->f, orig, g.V, on_device)) != DMTZ_OK) return s;
-    if ((s = upload(ctx, ctx->g, decp, g.V, on_device)) != DMTZ_OK) return s;
+    // the decompressed field travels on a second stream while the original
+    // field's gradient is computed; the work that reads it waits for it
+    if (!ctx->side) {
+        CK(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&ctx->side_done, cudaEventDisableTiming));
+    }
+    CK(cudaMemcpyAsync(ctx->g, decp, sizeof(double) * (size_t)g.V,
+                       on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, ctx->side));
+    CK(cudaEventRecord(ctx->side_done, ctx->side));
     // range and bound exactly as the reference computes them (main_3d.cu:6303-6323)
     double mn, mx;
     ctx->launches = 0;
@@ -2337,6 +2361,9 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
     const FieldState Ps = view(ctx->P, ctx->f), Qs = view(ctx->Q, ctx->g);
     run_pairing(ctx, g, Ps, nullptr, 1);
     if (pvp == 1 && (s = prep_paths(ctx, g)) != DMTZ_OK) return s;
+    CK(cudaStreamWaitEvent(st, ctx->side_done, 0));
+    if ((s = check_finite(ctx, ctx->g, g.V)) != DMTZ_OK) return s;
+    CK(cudaMemsetAsync(ctx->errword, 0, sizeof(int), st));
     if (filt == 1) {
         k_filter<<<grid_for(g.V), kBlock, 0, st>>>(g, ctx->P.crit, ctx->f, ctx->g, bound);
         ctx->launches++;
