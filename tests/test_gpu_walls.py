@@ -49,3 +49,25 @@ def test_wall_correction_matches_oracle(gpu_ctx, kind, dims, seed, rel, flags, u
     assert rep["outer_iterations"] == st["outer_iterations"] and rep["stall_breaks"] == st["stall_breaks"]
     P, Q = O.pair(f, dims), O.pair(out, dims)
     assert len(O.wall_detect(P, Q, dims)[0]) == 0
+
+
+@pytest.mark.parametrize("flags", [(1, 1, 1, 0, 1, 0, 0), (1, 1, 0, 0, 1, 0, 0), (0, 0, 0, 0, 0, 0, 0)])
+@pytest.mark.parametrize("case", range(6), ids=["tiny2", "tiny3", "noncubic", "flat", "ties", "thin"])
+def test_edge_cases_with_walls_and_breaking(gpu_ctx, case, flags):
+    """The parity edge cases (2^3 and 3^3 grids, non-cubic and thin grids, a
+    constant field, many ties) with walls and stall breaking, against the
+    oracle bit for bit; every run converges."""
+    from test_gpu_parity import EDGE_CASES, _edge_field
+
+    name, dims, kind, seed = EDGE_CASES[case]
+    f = _edge_field(kind, dims, seed)
+    rng = float(f.max() - f.min()) or 1.0
+    r = np.random.Generator(np.random.PCG64(seed + 99))
+    g = f + r.uniform(-0.05 * rng, 0.05 * rng, size=f.size)
+    want, st, wcnt = O.correct(f, g, dims, 0.05, list(flags), max_outer=300, break_stalls=True)
+    assert st["converged"] and st["oob"] == 0
+    for use_graph in (0, 1):
+        out, rep, cnt = gpu_ctx.correct(f, g, 0.05, flags, dims=dims, max_rounds=50000, use_graph=use_graph,
+                                        return_counter=True)
+        assert rep["converged"] and rep["stall_breaks"] == st["stall_breaks"]
+        assert np.array_equal(out, want) and np.array_equal(cnt, wcnt)
