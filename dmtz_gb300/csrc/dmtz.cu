@@ -103,6 +103,23 @@ __global__ void k_mark_dirty(Grid g, int nbx, int nby, int nbz, int sx, int sy, 
         }
     }
 }
+// Walk-cache tiles: 16^3 anchors.  Every brick the criticality pass re-pairs
+// marks the tiles it overlaps (a brick spans at most 3 tiles per axis).
+constexpr int kTile = 16, kTileShift = 4;
+__global__ void k_mark_tiles(const uint32_t *list, const unsigned long long *n, int sx, int sy, int sz, int ntx,
+                             int nty, int ntz, uint8_t *dirty) {
+    const i64 nb = (i64)*n;
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < nb; i += (i64)gridDim.x * blockDim.x) {
+        const uint32_t e = list[i];
+        const int bx = e & 0x7FF, by = (e >> 11) & 0x7FF, bz = e >> 22;
+        const int x0 = (bx * sx) >> kTileShift, x1 = min((bx * sx + sx - 1) >> kTileShift, ntx - 1);
+        const int y0 = (by * sy) >> kTileShift, y1 = min((by * sy + sy - 1) >> kTileShift, nty - 1);
+        const int z0 = (bz * sz) >> kTileShift, z1 = min((bz * sz + sz - 1) >> kTileShift, ntz - 1);
+        for (int tz = z0; tz <= z1; tz++)
+            for (int ty = y0; ty <= y1; ty++)
+                for (int tx = x0; tx <= x1; tx++) dirty[tx + (i64)ntx * (ty + (i64)nty * tz)] = 1;
+    }
+}
 // one compacted brick list per radius (list r-1 holds the bricks with bit
 // r-1), and the flags cleared for the next round
 __global__ void k_compact_bricks(int nbx, int nby, int nbz, uint32_t *flags, uint32_t *lists, i64 stride,
@@ -679,6 +696,59 @@ __global__ void k_conn_as(Grid g, const uint32_t *critP, const uint32_t *critQ, 
     }
 }
 
+// 3-D prefix sum of the dirty tiles (sat = number of dirty tiles in the box
+// from the origin to the tile), one thread per line per axis; the x pass
+// also clears the dirty marks for the next detection
+__global__ void k_sat_x(uint8_t *dirty, uint32_t *sat, int ntx, int nty, int ntz) {
+    const i64 lines = (i64)nty * ntz;
+    for (i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x; t < lines; t += (i64)gridDim.x * blockDim.x) {
+        uint32_t run = 0;
+        for (int x = 0; x < ntx; x++) {
+            const i64 i = t * ntx + x;
+            run += dirty[i];
+            dirty[i] = 0;
+            sat[i] = run;
+        }
+    }
+}
+__global__ void k_sat_yz(uint32_t *sat, int ntx, int nty, int ntz, int axis) {
+    const i64 lines = axis == 1 ? (i64)ntx * ntz : (i64)ntx * nty;
+    const int n = axis == 1 ? nty : ntz;
+    const i64 step = axis == 1 ? (i64)ntx : (i64)ntx * nty;
+    for (i64 t = (i64)blockIdx.x * blockDim.x + threadIdx.x; t < lines; t += (i64)gridDim.x * blockDim.x) {
+        const i64 base = axis == 1 ? (t % ntx) + (t / ntx) * (i64)ntx * nty : t;
+        uint32_t run = 0;
+        for (int k = 0; k < n; k++) {
+            run += sat[base + k * step];
+            sat[base + k * step] = run;
+        }
+    }
+}
+// a walk's tile box: x0 x1 y0 y1 z0 z1 in 10-bit fields, bit 63 = known
+// (a box with x0 > x1 is empty: the walk reads nothing that can change)
+constexpr unsigned long long kBoxKnown = 1ull << 63;
+__device__ __forceinline__ unsigned long long box_pack(int x0, int x1, int y0, int y1, int z0, int z1) {
+    return kBoxKnown | (unsigned long long)x0 | ((unsigned long long)x1 << 10) | ((unsigned long long)y0 << 20) |
+           ((unsigned long long)y1 << 30) | ((unsigned long long)z0 << 40) | ((unsigned long long)z1 << 50);
+}
+struct TileSat {
+    const uint32_t *sat;
+    int ntx, nty, ntz;
+};
+__device__ __forceinline__ uint32_t sat_at(const TileSat &T, int x, int y, int z) {
+    if (x < 0 || y < 0 || z < 0) return 0u;
+    return T.sat[x + (i64)T.ntx * (y + (i64)T.nty * z)];
+}
+// dirty tiles in a known box (0 for an empty box)
+__device__ __forceinline__ uint32_t box_dirty(const TileSat &T, unsigned long long b) {
+    const int x0 = (int)(b & 1023), x1 = (int)((b >> 10) & 1023), y0 = (int)((b >> 20) & 1023),
+              y1 = (int)((b >> 30) & 1023), z0 = (int)((b >> 40) & 1023), z1 = (int)((b >> 50) & 1023);
+    if (x0 > x1) return 0u;
+    return sat_at(T, x1, y1, z1) - sat_at(T, x0 - 1, y1, z1) - sat_at(T, x1, y0 - 1, z1) - sat_at(T, x1, y1, z0 - 1) +
+           sat_at(T, x0 - 1, y0 - 1, z1) + sat_at(T, x0 - 1, y1, z0 - 1) + sat_at(T, x1, y0 - 1, z0 - 1) -
+           sat_at(T, x0 - 1, y0 - 1, z0 - 1);
+}
+
 // start tetrahedron (anchor offset, slot) of coface j of a triangle of slot
 // sl, from four immediates (9 bits per (sl, j): dx+1, dy+1, dz+1, slot)
 // instead of a table read whose index differs across the warp
@@ -712,8 +782,15 @@ static_assert(cxt::TOPO_FACE_NCOF[0] == 2 && cxt::TOPO_FACE_NCOF[5] == 2 && cxt:
 // walk of its warp's contiguous range of walks instead of idling until the
 // warp's longest walk ends (one step per loop turn; the warp refills its free
 // lanes together, without atomics).
+//
+// Walk cache: a walk's result depends only on the decompressed pairing of the
+// tetrahedra it visited (up to its first differing one, or to its end), and
+// those sit at anchors inside the box of tiles the walk recorded.  A walk
+// whose box holds no tile re-paired since the last detection keeps its
+// result and is not walked again.
 __global__ void k_path_as_walk(Grid g, const i64 *sad2, const unsigned long long *nsad, const uint32_t *tcP,
-                               const uint32_t *tcQ, const uint8_t *succ, i64 *res, i64 cap, int *err) {
+                               const uint32_t *tcQ, const uint8_t *succ, i64 *res, i64 cap, int *err,
+                               unsigned long long *wbox, TileSat T) {
     const i64 n = 2 * (i64)*nsad;
     const unsigned full = 0xffffffffu, lane = threadIdx.x & 31u;
     const i64 nwarps = ((i64)gridDim.x * blockDim.x) >> 5;
@@ -723,6 +800,7 @@ __global__ void k_path_as_walk(Grid g, const i64 *sad2, const unsigned long long
     const i64 end = min(n, pos + chunk);
     i64 item = -1, steps = 0;
     int x = 0, y = 0, z = 0, s = 0;
+    int bx0 = 0, bx1 = 0, by0 = 0, by1 = 0, bz0 = 0, bz1 = 0;  // tile box of the current walk
     bool drained = false;
     while (true) {
         const unsigned want = __ballot_sync(full, item < 0 && !drained);
@@ -730,20 +808,27 @@ __global__ void k_path_as_walk(Grid g, const i64 *sad2, const unsigned long long
             if (item < 0 && !drained) {
                 const i64 my = pos + __popc(want & ((1u << lane) - 1u));
                 if (my < end) {
-                    item = my;
-                    steps = 0;
-                    const i64 code = sad2[my >> 1];
-                    const int j = (int)(my & 1);
-                    int vx, vy, vz, dx, dy, dz;
-                    decode_v(g, code / 12, vx, vy, vz);
-                    face_cof_start((int)(code % 12), j, dx, dy, dz, s);
-                    x = vx + dx;
-                    y = vy + dy;
-                    z = vz + dz;
-                    const bool ok = cell_ok(g, x, y, z, 1, 1, 1);
-                    if (!ok) {
-                        res[item] = -2;
-                        item = -1;
+                    const unsigned long long b = wbox[my];
+                    if (!(b & kBoxKnown) || box_dirty(T, b) != 0u) {
+                        item = my;
+                        steps = 0;
+                        const i64 code = sad2[my >> 1];
+                        const int j = (int)(my & 1);
+                        int vx, vy, vz, dx, dy, dz;
+                        decode_v(g, code / 12, vx, vy, vz);
+                        face_cof_start((int)(code % 12), j, dx, dy, dz, s);
+                        x = vx + dx;
+                        y = vy + dy;
+                        z = vz + dz;
+                        bx0 = bx1 = x >> kTileShift;
+                        by0 = by1 = y >> kTileShift;
+                        bz0 = bz1 = z >> kTileShift;
+                        const bool ok = cell_ok(g, x, y, z, 1, 1, 1);
+                        if (!ok) {  // no coface there: static, never walked again
+                            res[item] = -2;
+                            wbox[item] = box_pack(1, 0, 0, 0, 0, 0);
+                            item = -1;
+                        }
                     }
                 } else {
                     drained = true;
@@ -774,10 +859,17 @@ __global__ void k_path_as_walk(Grid g, const i64 *sad2, const unsigned long long
                 x += d % 3 - 1;
                 y += (d / 3) % 3 - 1;
                 z += d / 9 - 1;
+                bx0 = min(bx0, x >> kTileShift);
+                bx1 = max(bx1, x >> kTileShift);
+                by0 = min(by0, y >> kTileShift);
+                by1 = max(by1, y >> kTileShift);
+                bz0 = min(bz0, z >> kTileShift);
+                bz1 = max(bz1, z >> kTileShift);
                 fin = false;
             }
             if (fin) {
                 res[item] = r;
+                wbox[item] = box_pack(bx0, bx1, by0, by1, bz0, bz1);
                 item = -1;
             }
         }
@@ -1228,6 +1320,14 @@ struct dmtz_ctx {
     unsigned long long *brick_n = nullptr;  // their lengths
     i64 *sad2 = nullptr;      // original 2-saddle triangles
     i64 *as_res = nullptr;    // per (2-saddle, coface) walk results, 2 x capSad2
+    // walk cache: per walk, the box of 16^3-anchor tiles its last walk visited
+    // (walk_box); per tile, whether the decompressed gradient was recomputed
+    // there since the last detection (tile_dirty) and its 3-D prefix sum
+    unsigned long long *walk_box = nullptr;
+    uint8_t *tile_dirty = nullptr;
+    uint32_t *tile_sat = nullptr;
+    i64 capWB = 0, capTile = 0;
+    int ntx = 0, nty = 0, ntz = 0;
     i64 *wall_sad = nullptr, *wall_edge = nullptr;  // wall records (preserve_connectors = 1), capWall each
     i64 *wall_next[2] = {nullptr, nullptr};          // 2-saddles handed to the next search tier
     i64 capWall = 0;
@@ -1285,6 +1385,9 @@ void free_all(dmtz_ctx *c) {
     cudaFree(c->succ); cudaFree(c->sad2); cudaFree(c->brick_flags); cudaFree(c->brick_list);
     cudaFree(c->as_res);
     c->as_res = nullptr;
+    cudaFree(c->walk_box); cudaFree(c->tile_dirty); cudaFree(c->tile_sat);
+    c->walk_box = nullptr; c->tile_dirty = nullptr; c->tile_sat = nullptr;
+    c->capWB = c->capTile = 0;
     cudaFree(c->wall_sad); cudaFree(c->wall_edge); cudaFree(c->wall_next[0]); cudaFree(c->wall_next[1]);
     cudaFree(c->wall_scratch);
     c->wall_sad = c->wall_edge = c->wall_next[0] = c->wall_next[1] = c->wall_scratch = nullptr;
@@ -1502,6 +1605,13 @@ void repair_dirty(dmtz_ctx *ctx, const Grid &g, const FieldState &s, const uint3
     k_compact_bricks<<<persistent_grid(), kBlock, 0, st>>>(nbx, nby, nbz, ctx->brick_flags, ctx->brick_list,
                                                             ctx->capB, ctx->brick_n);
     ctx->launches += 2;
+    if (ctx->tile_dirty && ctx->ntx > 0) {  // the criticality pass's bricks cover every anchor re-paired
+        k_mark_tiles<<<persistent_grid(), kBlock, 0, st>>>(ctx->brick_list + (i64)(kRadii - 1) * ctx->capB,
+                                                            ctx->brick_n + (kRadii - 1), DMTZ_SHAPES[shape][0],
+                                                            DMTZ_SHAPES[shape][1], DMTZ_SHAPES[shape][2], ctx->ntx,
+                                                            ctx->nty, ctx->ntz, ctx->tile_dirty);
+        ctx->launches++;
+    }
     static const int radius[6] = {1, 2, 3, 3, 4, 5};  // per pass
     BrickList bl[6];
     for (int p = 0; p < 6; p++) {
@@ -1628,6 +1738,31 @@ dmtz_status prep_paths(dmtz_ctx *ctx, const Grid &g) {
         CK(dalloc(&ctx->sad2, 1));
         CK(dalloc(&ctx->as_res, 2));
     }
+    // walk cache: every walk runs at the first detection
+    const i64 nw = std::max<i64>(2 * (i64)n[1], 2);
+    if (nw > ctx->capWB) {
+        cudaFree(ctx->walk_box);
+        ctx->walk_box = nullptr;
+        ctx->capWB = 0;
+        CK(dalloc(&ctx->walk_box, nw));
+        ctx->capWB = nw;
+    }
+    ctx->ntx = (g.W + kTile - 1) / kTile;
+    ctx->nty = (g.H + kTile - 1) / kTile;
+    ctx->ntz = (g.D + kTile - 1) / kTile;
+    const i64 nt = (i64)ctx->ntx * ctx->nty * ctx->ntz;
+    if (nt > ctx->capTile) {
+        cudaFree(ctx->tile_dirty);
+        cudaFree(ctx->tile_sat);
+        ctx->tile_dirty = nullptr;
+        ctx->tile_sat = nullptr;
+        ctx->capTile = 0;
+        CK(dalloc(&ctx->tile_dirty, nt));
+        CK(dalloc(&ctx->tile_sat, nt));
+        ctx->capTile = nt;
+    }
+    CK(cudaMemsetAsync(ctx->walk_box, 0, sizeof(unsigned long long) * (size_t)nw, st));
+    CK(cudaMemsetAsync(ctx->tile_dirty, 0, (size_t)nt, st));
     CK(cudaMemsetAsync(ctx->counters + 10, 0, sizeof(unsigned long long), st));
     k_path_succ<<<grid_for(g.V), kBlock, 0, st>>>(g, ctx->P.tcode, ctx->succ);
     k_sad2_list<<<persistent_grid(), kBlock, 0, st>>>(g, ctx->P.crit, ctx->sad2, ctx->capSad2, ctx->counters + 10);
@@ -1647,15 +1782,24 @@ void launch_detect(dmtz_ctx *ctx, const Grid &g, const RuleCtx &rc, const PathRe
                                            g.T + 16, ctx->errword);
         k_conn_ds<<<grid, kBlock, 0, st>>>(rc, R, g.V + 16);
     } else {
+        const int ntx = ctx->ntx, nty = ctx->nty, ntz = ctx->ntz;
+        k_sat_x<<<grid_for((i64)nty * ntz), kBlock, 0, st>>>(ctx->tile_dirty, ctx->tile_sat, ntx, nty, ntz);
+        k_sat_yz<<<grid_for((i64)ntx * ntz), kBlock, 0, st>>>(ctx->tile_sat, ntx, nty, ntz, 1);
+        k_sat_yz<<<grid_for((i64)ntx * nty), kBlock, 0, st>>>(ctx->tile_sat, ntx, nty, ntz, 2);
+        TileSat T;
+        T.sat = ctx->tile_sat;
+        T.ntx = ntx;
+        T.nty = nty;
+        T.ntz = ntz;
         k_path_as_walk<<<grid, kBlock, 0, st>>>(g, ctx->sad2, ctx->counters + 10, ctx->P.tcode, ctx->Q.tcode,
-                                                    ctx->succ, ctx->as_res, g.T + 16, ctx->errword);
+                                                ctx->succ, ctx->as_res, g.T + 16, ctx->errword, ctx->walk_box, T);
         k_path_as_pick<<<grid, kBlock, 0, st>>>(g, ctx->sad2, ctx->counters + 10, ctx->as_res, R);
         k_path_ds<<<grid, kBlock, 0, st>>>(rc, R);
     }
 }
 void detect_paths(dmtz_ctx *ctx, const Grid &g, const RuleCtx &rc, const PathRec &R, unsigned grid, int conn = 0) {
     launch_detect(ctx, g, rc, R, grid, conn);
-    ctx->launches += conn ? 2 : 3;
+    ctx->launches += conn ? 2 : 6;
 }
 
 // Wall records (preserve_connectors = 1) of the current decompressed gradient:
@@ -2453,7 +2597,7 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
             }
             pt_.end();
             // kernels per body run: switch + control, plus each state's own
-            const int64_t det = conn ? 2 : 3;  // separatrix detection kernels
+            const int64_t det = conn ? 2 : 6;  // separatrix detection kernels
             ctx->launches += 2 * (fin.runs[0] + fin.runs[1] + fin.runs[2] + fin.runs[3]) + 11 * fin.runs[LS_CP] +
                              (11 + det) * fin.runs[LS_PDF] + det * fin.runs[LS_PCHECK] + 11 * fin.runs[LS_PFIX];
         }
