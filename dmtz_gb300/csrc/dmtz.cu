@@ -71,6 +71,87 @@ __global__ void k_mismatch_scan(Grid g, const uint32_t *crit_d, const uint32_t *
     }
 }
 
+// Incremental mismatch lists.  A cell's mismatch status changes only where
+// its anchor's criticality mask was recomputed, i.e. in the bricks of the
+// round's criticality pass (marked fresh).  The new lists are the old entries
+// outside fresh bricks plus a scan of the fresh bricks' anchors, built in T
+// and copied back.  Valid when every scan of the run uses the same saddle
+// flag and the old lists were complete (an overflow is followed by a full
+// scan before the next round).
+__global__ void k_mark_fresh(const uint32_t *list, const unsigned long long *n, uint8_t *fresh, int nbx, int nby) {
+    const i64 nb = (i64)*n;
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < nb; i += (i64)gridDim.x * blockDim.x) {
+        const uint32_t e = list[i];
+        fresh[(e & 0x7FF) + (i64)nbx * (((e >> 11) & 0x7FF) + (i64)nby * (e >> 22))] = 1;
+    }
+}
+__global__ void k_list_keep(Grid g, Lists L, Lists T, const uint8_t *fresh, int sx, int sy, int sz, int nbx, int nby) {
+    const i64 n0 = min((i64)L.n[0], L.cap[0]), n1 = min((i64)L.n[1], L.cap[1]), n2 = min((i64)L.n[2], L.cap[2]),
+              n3 = min((i64)L.n[3], L.cap[3]);
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n0 + n1 + n2 + n3; i += (i64)gridDim.x * blockDim.x) {
+        int k, x, y, z, sl;
+        i64 id;
+        if (i < n0) {
+            k = 0;
+            id = L.l[0][i];
+            decode_v(g, id, x, y, z);
+        } else if (i < n0 + n1) {
+            k = 1;
+            id = L.l[1][i - n0];
+            edge_unref(g, id, x, y, z, sl);
+        } else if (i < n0 + n1 + n2) {
+            k = 2;
+            id = L.l[2][i - n0 - n1];
+            face_unref(g, id, x, y, z, sl);
+        } else {
+            k = 3;
+            id = L.l[3][i - n0 - n1 - n2];
+            tet_unref(g, id, x, y, z, sl);
+        }
+        if (fresh[x / sx + (i64)nbx * (y / sy + (i64)nby * (z / sz))]) continue;
+        push_list(T, k, id);
+    }
+}
+// the anchors of the fresh bricks (one block per listed brick step)
+__global__ void k_scan_fresh(Grid g, const uint32_t *crit_d, const uint32_t *crit_o, Lists T, const uint32_t *blist,
+                             const unsigned long long *bn, int sx, int sy, int sz, int want_saddles) {
+    const i64 nb = (i64)*bn;
+    const int per = sx * sy * sz;
+    for (i64 b = blockIdx.x; b < nb; b += gridDim.x) {
+        const uint32_t e = blist[b];
+        const int x0 = (e & 0x7FF) * sx, y0 = ((e >> 11) & 0x7FF) * sy, z0 = (e >> 22) * sz;
+        for (int t = threadIdx.x; t < per; t += blockDim.x) {
+            const int x = x0 + t % sx, y = y0 + (t / sx) % sy, z = z0 + t / (sx * sy);
+            if (x >= g.W || y >= g.H || z >= g.D) continue;
+            const i64 v = x + (i64)y * g.W + (i64)z * g.WH;
+            uint32_t d = crit_d[v] ^ crit_o[v];
+            if (!want_saddles) d &= 1u | (0x3Fu << 20);
+            while (d) {
+                const int bit = __ffs(d) - 1;
+                d &= d - 1;
+                if (bit == 0) push_list(T, 0, v);
+                else if (bit < 8) push_list(T, 1, edge_ref(g, x, y, z, bit - 1));
+                else if (bit < 20) push_list(T, 2, face_ref(g, x, y, z, bit - 8));
+                else push_list(T, 3, tet_ref(g, x, y, z, bit - 20));
+            }
+        }
+    }
+}
+// T back into L (counts included; entries past a list's capacity were not
+// stored, and the count shows the overflow)
+__global__ void k_list_back(Lists T, Lists L) {
+    const i64 n0 = min((i64)T.n[0], T.cap[0]), n1 = min((i64)T.n[1], T.cap[1]), n2 = min((i64)T.n[2], T.cap[2]),
+              n3 = min((i64)T.n[3], T.cap[3]);
+    const i64 tid = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+    for (i64 i = tid; i < n0 + n1 + n2 + n3; i += (i64)gridDim.x * blockDim.x) {
+        if (i < n0) L.l[0][i] = T.l[0][i];
+        else if (i < n0 + n1) L.l[1][i - n0] = T.l[1][i - n0];
+        else if (i < n0 + n1 + n2) L.l[2][i - n0 - n1] = T.l[2][i - n0 - n1];
+        else L.l[3][i - n0 - n1 - n2] = T.l[3][i - n0 - n1 - n2];
+    }
+    if (tid < 4) L.n[tid] = T.n[tid];
+}
+
 // Dirty bricks, per pass.  The gradient state of an anchor depends on values
 // at most r_p anchors away in pass p: r = 1 (vertex pass), 2 (edge pass),
 // 3 (first triangle pass, -3..2), 3 (second edge pass), 4 (second triangle
@@ -1316,6 +1397,9 @@ struct dmtz_ctx {
     i64 capAS = 0, capDS = 0, capSad2 = 0;
     uint8_t *succ = nullptr;  // original ascending-path successor of each tetrahedron
     uint32_t *brick_flags = nullptr;  // per brick (a byte each, four to a word): radius bits of the next sweep
+    uint8_t *brick_fresh = nullptr;   // per brick: re-paired by the current round's criticality pass
+    int inc_scan = 0;                 // repairs rebuild the mismatch lists incrementally (see k_list_keep)
+    i64 *list_tmp[4] = {nullptr, nullptr, nullptr, nullptr};  // rebuilt mismatch lists, capL entries each
     uint32_t *brick_list = nullptr;   // compacted lists per radius, capB entries each
     unsigned long long *brick_n = nullptr;  // their lengths
     i64 *sad2 = nullptr;      // original 2-saddle triangles
@@ -1378,6 +1462,9 @@ void free_all(dmtz_ctx *c) {
     cudaFree(c->f); cudaFree(c->g); free_field(c->P); free_field(c->Q);
     cudaFree(c->cnt); cudaFree(c->reqbits); cudaFree(c->reqlist);
     for (auto &l : c->lists) { cudaFree(l); l = nullptr; }
+    for (auto &l : c->list_tmp) { cudaFree(l); l = nullptr; }
+    cudaFree(c->brick_fresh);
+    c->brick_fresh = nullptr;
     for (auto &k : c->capL) k = 0;
     c->capAS = c->capDS = c->capSad2 = 0;
     cudaFree(c->as_tet); cudaFree(c->as_cur); cudaFree(c->ds_edge); cudaFree(c->ds_vert);
@@ -1421,7 +1508,10 @@ dmtz_status ensure_lists(dmtz_ctx *ctx, const Grid &g) {
     for (int k = 0; k < 4; k++) {
         if (ctx->lists[k]) continue;
         const i64 cap = lean_cap(ctx, cells[k]);
+        cudaFree(ctx->list_tmp[k]);
+        ctx->list_tmp[k] = nullptr;
         CK(dalloc(&ctx->lists[k], cap));
+        CK(dalloc(&ctx->list_tmp[k], cap));
         ctx->capL[k] = cap;
     }
     return DMTZ_OK;
@@ -1445,6 +1535,7 @@ dmtz_status ensure(dmtz_ctx *ctx, const Grid &g) {
     CK(dalloc(&ctx->reqlist, V));
     CK(dalloc(&ctx->succ, 8 * V));
     CK(dalloc(&ctx->brick_flags, (nbr + 3) / 4)); CK(dalloc(&ctx->brick_list, kRadii * nbr));
+    CK(dalloc(&ctx->brick_fresh, nbr));
     CK(dalloc(&ctx->brick_n, 8));
     CK(cudaMemset(ctx->brick_flags, 0, sizeof(uint32_t) * (size_t)((nbr + 3) / 4)));
     ctx->capB = nbr;
@@ -1459,9 +1550,11 @@ dmtz_status grow_list(dmtz_ctx *ctx, const Grid &g, int k, i64 need) {
     const i64 cells[4] = {g.V, g.E, g.F, g.T};
     const i64 cap = std::max<i64>(need, std::min<i64>(cells[k], std::max<i64>(need + need / 2, 2 * ctx->capL[k])));
     cudaFree(ctx->lists[k]);
-    ctx->lists[k] = nullptr;
+    cudaFree(ctx->list_tmp[k]);
+    ctx->lists[k] = ctx->list_tmp[k] = nullptr;
     ctx->capL[k] = 0;
     CK(dalloc(&ctx->lists[k], cap));
+    CK(dalloc(&ctx->list_tmp[k], cap));
     ctx->capL[k] = cap;
     return DMTZ_OK;
 }
@@ -1605,9 +1698,15 @@ void repair_dirty(dmtz_ctx *ctx, const Grid &g, const FieldState &s, const uint3
     k_compact_bricks<<<persistent_grid(), kBlock, 0, st>>>(nbx, nby, nbz, ctx->brick_flags, ctx->brick_list,
                                                             ctx->capB, ctx->brick_n);
     ctx->launches += 2;
+    const uint32_t *r5 = ctx->brick_list + (i64)(kRadii - 1) * ctx->capB;
+    const unsigned long long *r5n = ctx->brick_n + (kRadii - 1);
+    if (ctx->inc_scan) {
+        cudaMemsetAsync(ctx->brick_fresh, 0, (size_t)nb, st);
+        k_mark_fresh<<<persistent_grid(), kBlock, 0, st>>>(r5, r5n, ctx->brick_fresh, nbx, nby);
+        ctx->launches++;
+    }
     if (ctx->tile_dirty && ctx->ntx > 0) {  // the criticality pass's bricks cover every anchor re-paired
-        k_mark_tiles<<<persistent_grid(), kBlock, 0, st>>>(ctx->brick_list + (i64)(kRadii - 1) * ctx->capB,
-                                                            ctx->brick_n + (kRadii - 1), DMTZ_SHAPES[shape][0],
+        k_mark_tiles<<<persistent_grid(), kBlock, 0, st>>>(r5, r5n, DMTZ_SHAPES[shape][0],
                                                             DMTZ_SHAPES[shape][1], DMTZ_SHAPES[shape][2], ctx->ntx,
                                                             ctx->nty, ctx->ntz, ctx->tile_dirty);
         ctx->launches++;
@@ -1621,7 +1720,25 @@ void repair_dirty(dmtz_ctx *ctx, const Grid &g, const FieldState &s, const uint3
         bl[p].shape = shape;
     }
     sweep_passes(ctx, g, s, bl, nb);
-    scan_mismatch(ctx, g, s.crit, crit_o, want_saddles);
+    if (!ctx->inc_scan) {
+        scan_mismatch(ctx, g, s.crit, crit_o, want_saddles);
+        return;
+    }
+    Lists L, T;
+    for (int k = 0; k < 4; k++) {
+        L.l[k] = ctx->lists[k];
+        T.l[k] = ctx->list_tmp[k];
+        L.cap[k] = T.cap[k] = ctx->capL[k];
+    }
+    L.n = ctx->counters;
+    T.n = ctx->counters + 20;
+    const int sx = DMTZ_SHAPES[shape][0], sy = DMTZ_SHAPES[shape][1], sz = DMTZ_SHAPES[shape][2];
+    const unsigned pg = persistent_grid();
+    cudaMemsetAsync(ctx->counters + 20, 0, 4 * sizeof(unsigned long long), st);
+    k_list_keep<<<pg, kBlock, 0, st>>>(g, L, T, ctx->brick_fresh, sx, sy, sz, nbx, nby);
+    k_scan_fresh<<<pg, kBlock, 0, st>>>(g, s.crit, crit_o, T, r5, r5n, sx, sy, sz, want_saddles);
+    k_list_back<<<pg, kBlock, 0, st>>>(T, L);
+    ctx->launches += 3;
 }
 
 double key_to_double(unsigned long long k) {
@@ -2539,6 +2656,9 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
     }
     i64 cc[4] = {(i64)hc[0], (i64)hc[1], (i64)hc[2], (i64)hc[3]};
     i64 n_as = 1, n_ds = 1, n_wall = 1;
+    // every scan of the loop asks for saddles when preserve_saddles = 1: the
+    // repairs can then rebuild the lists from the re-paired bricks alone
+    ctx->inc_scan = ps == 1 ? 1 : 0;
     i64 rounds = 0;
     int converged = 1;
     const unsigned pgrid = persistent_grid();
@@ -2598,8 +2718,11 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
             pt_.end();
             // kernels per body run: switch + control, plus each state's own
             const int64_t det = conn ? 2 : 6;  // separatrix detection kernels
-            ctx->launches += 2 * (fin.runs[0] + fin.runs[1] + fin.runs[2] + fin.runs[3]) + 11 * fin.runs[LS_CP] +
-                             (11 + det) * fin.runs[LS_PDF] + det * fin.runs[LS_PCHECK] + 11 * fin.runs[LS_PFIX];
+            // a fix round: fix + update, then the repair (dirty marks, compaction,
+            // fresh and tile marks, six passes, the list rebuild)
+            const int64_t rnd = 2 + 2 + (ctx->inc_scan ? 1 : 0) + (ctx->tile_dirty ? 1 : 0) + 6 + (ctx->inc_scan ? 3 : 1);
+            ctx->launches += 2 * (fin.runs[0] + fin.runs[1] + fin.runs[2] + fin.runs[3]) + rnd * fin.runs[LS_CP] +
+                             (rnd + det) * fin.runs[LS_PDF] + det * fin.runs[LS_PCHECK] + rnd * fin.runs[LS_PFIX];
         }
         R.outer_iterations = fin.outer;
         R.cp_rounds = fin.cp_rounds;
@@ -2696,6 +2819,7 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
             paths_fresh = true;
         }
     }
+    ctx->inc_scan = 0;
     CK(cudaEventRecord(e1, st));
     CK(cudaMemsetAsync(ctx->counters + 12, 0, sizeof(unsigned long long), st));
     k_count_u8<<<persistent_grid(), kBlock, 0, st>>>(ctx->changed, g.V, ctx->counters + 12);
@@ -2878,7 +3002,8 @@ dmtz_status dmtz_set_list_reserve(dmtz_ctx *ctx, double fraction, int64_t min_en
     cudaSetDevice(ctx->device);
     for (int k = 0; k < 4; k++) {  // reallocated with the new reserve by the next call
         cudaFree(ctx->lists[k]);
-        ctx->lists[k] = nullptr;
+        cudaFree(ctx->list_tmp[k]);
+        ctx->lists[k] = ctx->list_tmp[k] = nullptr;
         ctx->capL[k] = 0;
     }
     return DMTZ_OK;
