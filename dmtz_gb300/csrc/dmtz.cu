@@ -2591,6 +2591,7 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
     const int conn = (pvp == 1 && pg == 0) ? 1 : 0;  // connectivity-mode separatrices
     if (!(rel_eps >= 0.0) || !std::isfinite(rel_eps)) return fail(ctx, DMTZ_ERR_ARG, "rel_eps must be finite and >= 0");
     const i64 max_rounds = opts->max_rounds > 0 ? opts->max_rounds : 100000;
+    ctx->inc_scan = 0;  // full scans until the loop starts
     CK(cudaSetDevice(ctx->device));
     if ((s = ensure(ctx, g)) != DMTZ_OK) return s;
     cudaStream_t st = ctx->stream;
