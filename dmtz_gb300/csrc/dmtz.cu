@@ -975,6 +975,90 @@ __global__ void k_path_as_pick(Grid g, const i64 *sad2, const unsigned long long
     }
 }
 
+// Incremental descending checks.  A 1-saddle's record depends on the
+// decompressed pairing at its endpoints (its anchor, or the anchor + 1 along
+// some axes).  Per anchor, C = "the tile box from the anchor's tile to the
+// tile of anchor + (1,1,1) holds a tile re-paired since the last detection".
+// Records of anchors with C false are kept; the anchors with C true are
+// checked again (in the tiles whose box from the tile to tile + (1,1,1) is
+// dirty); the first detection after the set-up checks every anchor.
+__device__ __forceinline__ bool ds_anchor_dirty(const Grid &g, const TileSat &T, int x, int y, int z) {
+    return box_dirty(T, box_pack(x >> kTileShift, min(x + 1, g.W - 1) >> kTileShift, y >> kTileShift,
+                                 min(y + 1, g.H - 1) >> kTileShift, z >> kTileShift,
+                                 min(z + 1, g.D - 1) >> kTileShift)) != 0u;
+}
+__global__ void k_ds_keep(Grid g, PathRec R, const unsigned long long *old_n, const unsigned long long *valid, i64 *te,
+                          i64 *tv, unsigned long long *tn, i64 tcap, TileSat T) {
+    if (!*valid) return;
+    const i64 n = min((i64)*old_n, R.cap_ds);
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+        const i64 e = R.ds_edge[i];
+        int x, y, z, k;
+        edge_unref(g, e, x, y, z, k);
+        if (ds_anchor_dirty(g, T, x, y, z)) continue;
+        const unsigned long long at = agg_slot(tn);
+        if ((i64)at < tcap) {
+            te[at] = e;
+            tv[at] = R.ds_vert[i];
+        }
+    }
+}
+__global__ void k_ds_tiles(RuleCtx c, const unsigned long long *valid, i64 *te, i64 *tv, unsigned long long *tn,
+                           i64 tcap, TileSat T) {
+    const Grid &g = c.g;
+    const bool all = *valid == 0;
+    const i64 nt = (i64)T.ntx * T.nty * T.ntz;
+    for (i64 t = blockIdx.x; t < nt; t += gridDim.x) {
+        const int tx = (int)(t % T.ntx), ty = (int)((t / T.ntx) % T.nty), tz = (int)(t / ((i64)T.ntx * T.nty));
+        if (!all && box_dirty(T, box_pack(tx, min(tx + 1, T.ntx - 1), ty, min(ty + 1, T.nty - 1), tz,
+                                          min(tz + 1, T.ntz - 1))) == 0u)
+            continue;  // the same for every thread of the block
+        for (int a = threadIdx.x; a < kTile * kTile * kTile; a += blockDim.x) {
+            const int x = tx * kTile + a % kTile, y = ty * kTile + (a / kTile) % kTile, z = tz * kTile + a / (kTile * kTile);
+            if (x >= g.W || y >= g.H || z >= g.D) continue;
+            if (!all && !ds_anchor_dirty(g, T, x, y, z)) continue;
+            const i64 v = x + (i64)y * g.W + (i64)z * g.WH;
+            const uint32_t m = (c.P.crit[v] >> 1) & 0x7Fu;
+            if (!m) continue;
+            DMTZ_FOR(7, K, {
+                constexpr int k = decltype(K)::value;
+                constexpr int c0 = cxt::TOPO_EDGE_V[k][0], c1 = cxt::TOPO_EDGE_V[k][1];
+                if ((m >> k) & 1u) {
+                    const i64 ends[2] = {v + cxt::ccx(c0) + cxt::ccy(c0) * (i64)g.W + cxt::ccz(c0) * g.WH,
+                                         v + cxt::ccx(c1) + cxt::ccy(c1) * (i64)g.W + cxt::ccz(c1) * g.WH};
+                    for (int j = 0; j < 2; j++) {
+                        const i64 e = ends[j];
+                        const int po = c.P.pv[e];
+                        if (po == 15) continue;
+                        if (po != c.Q.pv[e]) {
+                            const unsigned long long at = agg_slot(tn);
+                            if ((i64)at < tcap) {
+                                te[at] = edge_ref(g, x, y, z, k);
+                                tv[at] = e;
+                            }
+                            break;
+                        }
+                    }
+                }
+            });
+        }
+    }
+}
+__global__ void k_ds_back(PathRec R, const i64 *te, const i64 *tv, const unsigned long long *tn,
+                          unsigned long long *valid) {
+    const i64 n = min((i64)*tn, R.cap_ds);
+    const i64 tid = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+    for (i64 i = tid; i < n; i += (i64)gridDim.x * blockDim.x) {
+        R.ds_edge[i] = te[i];
+        R.ds_vert[i] = tv[i];
+    }
+    if (tid == 0) {
+        R.n[1] = *tn;
+        *valid = 1ull;
+    }
+}
+
+
 __global__ void k_fix_path(RuleCtx c, PathRec R) {
     const i64 na = min((i64)R.n[0], R.cap_as), nd = min((i64)R.n[1], R.cap_ds);
     for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < na + nd; i += (i64)gridDim.x * blockDim.x) {
@@ -1394,6 +1478,8 @@ struct dmtz_ctx {
     double list_frac = 1.0 / 16;
     i64 list_min = 1 << 20;
     i64 *as_tet = nullptr, *as_cur = nullptr, *ds_edge = nullptr, *ds_vert = nullptr;
+    i64 *ds_tmp_edge = nullptr, *ds_tmp_vert = nullptr;  // descending records being rebuilt, capDST each
+    i64 capDST = 0;
     i64 capAS = 0, capDS = 0, capSad2 = 0;
     uint8_t *succ = nullptr;  // original ascending-path successor of each tetrahedron
     uint32_t *brick_flags = nullptr;  // per brick (a byte each, four to a word): radius bits of the next sweep
@@ -1420,7 +1506,10 @@ struct dmtz_ctx {
     unsigned long long *counters = nullptr;  // [0..3] cp lists, [4] requests, [5,6] paths, [7] progress,
                                              // [8,9] min/max keys, [10] original 2-saddles, [12] edited
                                              // vertices, [13,14] saddle counts, [15] surface anchors,
-                                             // [16] wall records, [17,18] deferred wall searches
+                                             // [16] wall records, [17,18] deferred wall searches,
+                                             // [20..23] rebuilt mismatch lists, [24] descending
+                                             // records rebuildable, [25] their last count,
+                                             // [26] rebuilt descending records
     int *errword = nullptr;
     uint8_t *changed = nullptr;
     int64_t launches = 0;  // kernels launched by the current call
@@ -1484,6 +1573,9 @@ void free_all(dmtz_ctx *c) {
     c->succ = nullptr; c->sad2 = nullptr; c->brick_flags = nullptr; c->brick_list = nullptr;
     c->f = c->g = nullptr; c->cnt = nullptr; c->reqbits = nullptr; c->reqlist = nullptr;
     c->as_tet = c->as_cur = c->ds_edge = c->ds_vert = nullptr; c->counters = nullptr;
+    cudaFree(c->ds_tmp_edge); cudaFree(c->ds_tmp_vert);
+    c->ds_tmp_edge = c->ds_tmp_vert = nullptr;
+    c->capDST = 0;
     c->errword = nullptr; c->changed = nullptr;
     c->capV = c->capE = c->capF = c->capT = c->capB = 0;
 }
@@ -1539,7 +1631,7 @@ dmtz_status ensure(dmtz_ctx *ctx, const Grid &g) {
     CK(dalloc(&ctx->brick_n, 8));
     CK(cudaMemset(ctx->brick_flags, 0, sizeof(uint32_t) * (size_t)((nbr + 3) / 4)));
     ctx->capB = nbr;
-    CK(dalloc(&ctx->counters, 24)); CK(dalloc(&ctx->errword, 1)); CK(dalloc(&ctx->changed, V));
+    CK(dalloc(&ctx->counters, 32)); CK(dalloc(&ctx->errword, 1)); CK(dalloc(&ctx->changed, V));
     ctx->capV = g.V; ctx->capE = g.E; ctx->capF = g.F; ctx->capT = g.T;
     return ensure_lists(ctx, g);
 }
@@ -1815,8 +1907,23 @@ PathRec path_rec(const dmtz_ctx *ctx) {
 // and record buffers sized by the original saddle counts (each original
 // 2-saddle gives at most one ascending record, each 1-saddle at most one
 // descending record)
+// the rebuild buffers of the descending records, as large as the records
+dmtz_status ensure_ds_tmp(dmtz_ctx *ctx) {
+    const i64 need = std::max<i64>(ctx->capDS, 1);
+    if (ctx->capDST >= need) return DMTZ_OK;
+    cudaFree(ctx->ds_tmp_edge);
+    cudaFree(ctx->ds_tmp_vert);
+    ctx->ds_tmp_edge = ctx->ds_tmp_vert = nullptr;
+    ctx->capDST = 0;
+    CK(dalloc(&ctx->ds_tmp_edge, need));
+    CK(dalloc(&ctx->ds_tmp_vert, need));
+    ctx->capDST = need;
+    return DMTZ_OK;
+}
+
 dmtz_status prep_paths(dmtz_ctx *ctx, const Grid &g) {
     cudaStream_t st = ctx->stream;
+    dmtz_status s0;
     CK(cudaMemsetAsync(ctx->counters + 13, 0, 2 * sizeof(unsigned long long), st));
     k_count_saddles<<<persistent_grid(), kBlock, 0, st>>>(g.V, ctx->P.crit, ctx->counters + 13);
     unsigned long long n[2] = {0, 0};
@@ -1855,6 +1962,8 @@ dmtz_status prep_paths(dmtz_ctx *ctx, const Grid &g) {
         CK(dalloc(&ctx->sad2, 1));
         CK(dalloc(&ctx->as_res, 2));
     }
+    if ((s0 = ensure_ds_tmp(ctx)) != DMTZ_OK) return s0;
+    CK(cudaMemsetAsync(ctx->counters + 24, 0, 3 * sizeof(unsigned long long), st));
     // walk cache: every walk runs at the first detection
     const i64 nw = std::max<i64>(2 * (i64)n[1], 2);
     if (nw > ctx->capWB) {
@@ -1893,6 +2002,8 @@ dmtz_status prep_paths(dmtz_ctx *ctx, const Grid &g) {
 // (also used while capturing the graph loop)
 void launch_detect(dmtz_ctx *ctx, const Grid &g, const RuleCtx &rc, const PathRec &R, unsigned grid, int conn) {
     cudaStream_t st = ctx->stream;
+    // the last detection's descending record count, for the incremental rebuild
+    cudaMemcpyAsync(ctx->counters + 25, ctx->counters + 6, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, st);
     cudaMemsetAsync(ctx->counters + 5, 0, 2 * sizeof(unsigned long long), st);
     if (conn) {
         k_conn_as<<<grid, kBlock, 0, st>>>(g, ctx->P.crit, ctx->Q.crit, ctx->P.tcode, ctx->Q.tcode, ctx->succ, R,
@@ -1911,12 +2022,18 @@ void launch_detect(dmtz_ctx *ctx, const Grid &g, const RuleCtx &rc, const PathRe
         k_path_as_walk<<<grid, kBlock, 0, st>>>(g, ctx->sad2, ctx->counters + 10, ctx->P.tcode, ctx->Q.tcode,
                                                 ctx->succ, ctx->as_res, g.T + 16, ctx->errword, ctx->walk_box, T);
         k_path_as_pick<<<grid, kBlock, 0, st>>>(g, ctx->sad2, ctx->counters + 10, ctx->as_res, R);
-        k_path_ds<<<grid, kBlock, 0, st>>>(rc, R);
+        cudaMemsetAsync(ctx->counters + 26, 0, sizeof(unsigned long long), st);
+        k_ds_keep<<<grid, kBlock, 0, st>>>(g, R, ctx->counters + 25, ctx->counters + 24, ctx->ds_tmp_edge,
+                                           ctx->ds_tmp_vert, ctx->counters + 26, ctx->capDST, T);
+        k_ds_tiles<<<grid, kBlock, 0, st>>>(rc, ctx->counters + 24, ctx->ds_tmp_edge, ctx->ds_tmp_vert,
+                                            ctx->counters + 26, ctx->capDST, T);
+        k_ds_back<<<grid, kBlock, 0, st>>>(R, ctx->ds_tmp_edge, ctx->ds_tmp_vert, ctx->counters + 26,
+                                           ctx->counters + 24);
     }
 }
 void detect_paths(dmtz_ctx *ctx, const Grid &g, const RuleCtx &rc, const PathRec &R, unsigned grid, int conn = 0) {
     launch_detect(ctx, g, rc, R, grid, conn);
-    ctx->launches += conn ? 2 : 6;
+    ctx->launches += conn ? 2 : 8;
 }
 
 // Wall records (preserve_connectors = 1) of the current decompressed gradient:
@@ -2223,6 +2340,9 @@ static dmtz_status path_detect_impl(dmtz_ctx *ctx, int W, int H, int D, const do
             CK(dalloc(&ctx->ds_edge, (i64)hc[1]));
             CK(dalloc(&ctx->ds_vert, (i64)hc[1]));
             ctx->capDS = (i64)hc[1];
+            if ((s = ensure_ds_tmp(ctx)) != DMTZ_OK) return s;
+            // records past the old capacity were not kept: the next detection scans everything
+            CK(cudaMemsetAsync(ctx->counters + 24, 0, sizeof(unsigned long long), ctx->stream));
         }
     }
     counts[0] = (int64_t)hc[0];
@@ -2718,7 +2838,7 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
             }
             pt_.end();
             // kernels per body run: switch + control, plus each state's own
-            const int64_t det = conn ? 2 : 6;  // separatrix detection kernels
+            const int64_t det = conn ? 2 : 8;  // separatrix detection kernels
             // a fix round: fix + update, then the repair (dirty marks, compaction,
             // fresh and tile marks, six passes, the list rebuild)
             const int64_t rnd = 2 + 2 + (ctx->inc_scan ? 1 : 0) + (ctx->tile_dirty ? 1 : 0) + 6 + (ctx->inc_scan ? 3 : 1);
@@ -2877,7 +2997,7 @@ dmtz_status dmtz_quantize(dmtz_ctx *ctx, int W, int H, int D, const double *orig
         return fail(ctx, DMTZ_ERR_ARG, "rel_eps must be finite and >= 0, noise_frac in [0, 1]");
     CK(cudaSetDevice(ctx->device));
     if (!ctx->counters) {
-        CK(dalloc(&ctx->counters, 24));
+        CK(dalloc(&ctx->counters, 32));
         CK(dalloc(&ctx->errword, 1));
     }
     cudaStream_t st = ctx->stream;
