@@ -437,56 +437,6 @@ __global__ void k_count_saddles(i64 V, const uint32_t *critP, unsigned long long
     }
 }
 
-// get_false_as_vpath (main_3d.cu:4540-4610) with is_false: for each original
-// 2-saddle triangle, its cofaces in search order; along each one's original
-// ascending path, the first tetrahedron whose decompressed pairing differs is
-// recorded, for the first coface that has one.
-__global__ void k_path_as(Grid g, const i64 *sad2, const unsigned long long *nsad, const uint32_t *tcP,
-                          const uint32_t *tcQ, const uint8_t *succ, PathRec R, i64 cap, int *err) {
-    const i64 n = (i64)*nsad;
-    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
-        const i64 code = sad2[i];
-        const i64 v = code / 12;
-        const int sl = (int)(code % 12);
-        int x, y, z;
-        decode_v(g, v, x, y, z);
-        for (int j = 0; j < TOPO_FACE_NCOF[sl]; j++) {
-            const signed char *tc = TOPO_FACE_COF[sl][j];
-            int cx = x + tc[0], cy = y + tc[1], cz = z + tc[2], cs = tc[3];
-            if (!cell_ok(g, cx, cy, cz, 1, 1, 1)) continue;
-            const int sx = cx, sy = cy, sz = cz, ss = cs;
-            bool found = false;
-            i64 steps = 0;
-            while (true) {
-                const i64 ci = cx + (i64)cy * g.W + (i64)cz * g.WH;
-                const int p = (tcP[ci] >> (3 * cs)) & 7;
-                if (p == 7) break;  // an original maximum ends the path
-                if (p != (int)((tcQ[ci] >> (3 * cs)) & 7)) {
-                    const unsigned long long at = atomicAdd(&R.n[0], 1ull);
-                    if ((i64)at < R.cap_as) {
-                        R.as_tet[at] = tet_ref(g, sx, sy, sz, ss);
-                        R.as_cur[at] = tet_ref(g, cx, cy, cz, cs);
-                    }
-                    found = true;
-                    break;
-                }
-                const int s8 = succ[ci * 8 + cs];
-                if (s8 == 255) break;
-                const int d = s8 / 6;
-                cs = s8 - 6 * d;
-                cx += d % 3 - 1;
-                cy += (d / 3) % 3 - 1;
-                cz += d / 9 - 1;
-                if (++steps > cap) {
-                    atomicOr(err, ERR_WALK);
-                    break;
-                }
-            }
-            if (found) break;
-        }
-    }
-}
-
 // ------------------------------------------------------------------- walls
 // preserve_connectors = 1: get_false_ds_wall (main_3d.cu:5064-5121) restated
 // without its races.  Every original 2-saddle face runs its own depth-first
@@ -599,42 +549,6 @@ __global__ void k_fix_wall(RuleCtx c, WallRec W) {
     const i64 n = min((i64)*W.n, W.cap);
     for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x)
         rule_ds_wall(c, W.edge[i]);
-}
-
-// get_false_ds_vpath (main_3d.cu:4837-4959): the reference's walk never
-// advances past the first vertex (dec_current_id stays at the start), so each
-// endpoint's steepest-descent pairing is compared once, v1 (higher id) first.
-__global__ void k_path_ds(RuleCtx c, PathRec R) {
-    const Grid &g = c.g;
-    for (i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x; v < g.V; v += (i64)gridDim.x * blockDim.x) {
-        const uint32_t m = (c.P.crit[v] >> 1) & 0x7Fu;
-        if (!m) continue;
-        // edge families unrolled: corner offsets from immediates, not from
-        // tables indexed by a per-lane family
-        DMTZ_FOR(7, K, {
-            constexpr int k = decltype(K)::value;
-            constexpr int c0 = cxt::TOPO_EDGE_V[k][0], c1 = cxt::TOPO_EDGE_V[k][1];
-            if ((m >> k) & 1u) {
-                const i64 ends[2] = {v + cxt::ccx(c0) + cxt::ccy(c0) * (i64)g.W + cxt::ccz(c0) * g.WH,
-                                     v + cxt::ccx(c1) + cxt::ccy(c1) * (i64)g.W + cxt::ccz(c1) * g.WH};
-                for (int j = 0; j < 2; j++) {
-                    const i64 e = ends[j];
-                    const int po = c.P.pv[e];
-                    if (po == 15) continue;
-                    if (po != c.Q.pv[e]) {
-                        const unsigned long long at = atomicAdd(&R.n[1], 1ull);
-                        if ((i64)at < R.cap_ds) {
-                            int x, y, z;
-                            decode_v(g, v, x, y, z);
-                            R.ds_edge[at] = edge_ref(g, x, y, z, k);
-                            R.ds_vert[at] = e;
-                        }
-                        break;
-                    }
-                }
-            }
-        });
-    }
 }
 
 // ------------------------------------------------- connectivity-mode separatrices
@@ -856,10 +770,13 @@ __device__ __forceinline__ void face_cof_start(int sl, int j, int &dx, int &dy, 
 static_assert(cxt::TOPO_FACE_NCOF[0] == 2 && cxt::TOPO_FACE_NCOF[5] == 2 && cxt::TOPO_FACE_NCOF[11] == 2,
               "every triangle slot has two cofaces");
 
-// k_path_as split in two for parallelism: (2-saddle, coface) walks (res = the
-// first differing tetrahedron, -1 none, -2 no coface), then one thread per
-// 2-saddle keeps the first coface in search order that has one: the same
-// records.  Walk lengths vary a lot, so a lane whose walk ends takes the next
+// get_false_as_vpath (main_3d.cu:4540-4610) with is_false: for each original
+// 2-saddle triangle, its cofaces in search order; along each one's original
+// ascending path, the first tetrahedron whose decompressed pairing differs is
+// recorded, for the first coface that has one.  Done in two kernels for
+// parallelism: (2-saddle, coface) walks (res = the first differing
+// tetrahedron, -1 none, -2 no coface), then one thread per 2-saddle keeps the
+// first coface in search order that has one.  Walk lengths vary a lot, so a lane whose walk ends takes the next
 // walk of its warp's contiguous range of walks instead of idling until the
 // warp's longest walk ends (one step per loop turn; the warp refills its free
 // lanes together, without atomics).
@@ -975,6 +892,10 @@ __global__ void k_path_as_pick(Grid g, const i64 *sad2, const unsigned long long
     }
 }
 
+// get_false_ds_vpath (main_3d.cu:4837-4959): the reference's walk never
+// advances past the first vertex (dec_current_id stays at the start), so each
+// endpoint's steepest-descent pairing is compared once, v1 (higher id) first.
+//
 // Incremental descending checks.  A 1-saddle's record depends on the
 // decompressed pairing at its endpoints (its anchor, or the anchor + 1 along
 // some axes).  Per anchor, C = "the tile box from the anchor's tile to the
