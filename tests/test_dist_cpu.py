@@ -69,3 +69,28 @@ def test_reference_arm_prints_on_rank0_only():
     with redirect_stdout(buf):
         bench.run_reference(A, 1)
     assert buf.getvalue() == ""
+
+
+def test_reference_arm_line(monkeypatch):
+    """The reference arm's JSON line carries the keys of the bench contract
+    (a 24^3 sample here, to keep the CPU suite quick)."""
+    sys.path.insert(0, REPO)
+    import json
+
+    import bench
+
+    monkeypatch.setattr(bench, "SAMPLE", 24)
+
+    class A:
+        steps, warmup, gpus = 1, 0, 1
+
+    buf = io.StringIO()
+    with redirect_stdout(buf):
+        bench.run_reference(A, 0)
+    line = json.loads(buf.getvalue().strip().splitlines()[-1])
+    for k in ("impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+              "dtype", "config", "cpu_baseline", "e2e"):
+        assert k in line, k
+    assert line["impl"] == "reference" and line["value"] > 0
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
