@@ -1252,6 +1252,31 @@ static int is_false(ctx_t *c, int id, int *rec_cur) {
     return 0;
 }
 
+/* strict descending checks (not the reference's; see orc_set_strict_ds) */
+static int g_strict_ds = 0;
+void orc_set_strict_ds(int on) { g_strict_ds = on ? 1 : 0; }
+
+/* The whole original descending path from v (steepest-descent pairing PV,
+ * the loop of get_false_ds_vpath with dec_current_id advancing as
+ * current_id does): the first vertex whose decompressed pairing differs, or
+ * -1 when the path reaches a minimum clean. */
+static int ds_first_diff(ctx_t *c, int v) {
+    const grid_t *G = &c->G;
+    for (long long steps = 0;; steps++) {
+        const int pv = PVa(v);
+        if (pv == -1) return -1;
+        if (pv != QVa(v)) return v;
+        if (PEa(pv) == -1) return -1;
+        int a, b;
+        edge_verts(G, pv, &a, &b);
+        v = a == v ? b : a;
+        if (steps > (long long)G->V) {
+            c->oob++;
+            return -1;
+        }
+    }
+}
+
 int orc_path_detect(int W, int H, int D, const int *PV, const int *PE, const int *PF, const int *PT,
                     const int *QV, const int *QE, const int *QF, const int *QT, int counts[2], int *as_tet,
                     int *as_cur, int *ds_edge, int *ds_vert) {
@@ -1299,6 +1324,16 @@ int orc_path_detect(int W, int H, int D, const int *PV, const int *PE, const int
         int ends[2] = {v1, v2};
         for (int k = 0; k < 2; k++) {
             int v = ends[k];
+            if (g_strict_ds) {
+                const int u = ds_first_diff(c, v);
+                if (u >= 0) {
+                    if (ds_edge) ds_edge[nds] = i;
+                    if (ds_vert) ds_vert[nds] = u;
+                    nds++;
+                    break;
+                }
+                continue;
+            }
             int pv = PVa(v);
             if (pv == -1) continue;
             if (pv != QVa(v)) {
@@ -1722,6 +1757,12 @@ int orc_correct(int W, int H, int D, const double *f, double *g, double rel_eps,
 
 int orc_correct_ex(int W, int H, int D, const double *f, double *g, double rel_eps, const int flags[7], int max_outer,
                    int nthreads, int break_stalls, long long stats[9], int *cnt_out) {
+    return orc_correct_rounds(W, H, D, f, g, rel_eps, flags, max_outer, 0, nthreads, break_stalls, stats, cnt_out);
+}
+
+int orc_correct_rounds(int W, int H, int D, const double *f, double *g, double rel_eps, const int flags[7],
+                       int max_outer, long long max_rounds, int nthreads, int break_stalls, long long stats[9],
+                       int *cnt_out) {
     const int ps = flags[0], pv = flags[1], pg = flags[2], filt = flags[3], pc = flags[4], pt = flags[5],
               et = flags[6];
     for (int i = 0; i < 9; i++) stats[i] = 0;
@@ -1800,7 +1841,7 @@ int orc_correct_ex(int W, int H, int D, const double *f, double *g, double rel_e
     int *cmin = NULL, *cmax = NULL;
     int n_as = 1, n_ds = 1, n_wall = 1;
     long long total_ite = 0, cp_ite = 0, rounds = 0;
-    const long long round_cap = (long long)max_outer * 64;
+    const long long round_cap = max_rounds > 0 ? max_rounds : (long long)max_outer * 64;
     int converged = 1;
     ctx_t c;
     memset(&c, 0, sizeof(c));

@@ -92,11 +92,23 @@ void orc_edge_ids(int W, int H, int D, int n, const int *pairs, int *out);
 int orc_wall_detect(int W, int H, int D, const int *PV, const int *PE, const int *PF, const int *PT, const int *QV,
                     const int *QE, const int *QF, const int *QT, int *count, int *w_sad, int *w_edge,
                     long long *pops);
+/* 1: the descending separatrix checks of orc_path_detect and of the
+ * correction loops walk each 1-saddle endpoint's whole original descending
+ * path and record its first vertex whose decompressed pairing differs (the
+ * reference's get_false_ds_vpath compares the first vertex only); 0 (the
+ * default): the reference's check. */
+void orc_set_strict_ds(int on);
 /* orc_correct with stall breaking (break_stalls = 1: a round that changes no
  * value and no edit counter resets a box around the remaining mismatches to
  * the original values; stats[8] = such breaks). */
 int orc_correct_ex(int W, int H, int D, const double *f, double *g, double rel_eps, const int flags[7],
                    int max_outer, int nthreads, int break_stalls, long long stats[9], int *cnt_out);
+/* orc_correct_ex with an explicit cap on fix/apply rounds (max_rounds > 0;
+ * otherwise 64 x max_outer): the state after exactly max_rounds rounds of a
+ * loop that does not converge is the reference's after the same rounds. */
+int orc_correct_rounds(int W, int H, int D, const double *f, double *g, double rel_eps, const int flags[7],
+                       int max_outer, long long max_rounds, int nthreads, int break_stalls, long long stats[9],
+                       int *cnt_out);
 
 /* Manifold labels: desc[v] = minimum reached along the steepest-descent
  * pairing, asc[t] = maximum reached by the ascending tetrahedron walk, -1 if

@@ -48,12 +48,18 @@ def lib():
         L.orc_path_detect.restype = ctypes.c_int
         L.orc_path_detect_conn.argtypes = [ctypes.c_int] * 3 + [_i32p] * 8 + [_i32p] + [_i32p] * 4
         L.orc_path_detect_conn.restype = ctypes.c_int
+        L.orc_set_strict_ds.argtypes = [ctypes.c_int]
+        L.orc_set_strict_ds.restype = None
         L.orc_correct.argtypes = [ctypes.c_int] * 3 + [_f64p, _f64p, ctypes.c_double, _i32p, ctypes.c_int,
                                                         ctypes.c_int, _i64p, _i32p]
         L.orc_correct.restype = ctypes.c_int
         L.orc_correct_ex.argtypes = [ctypes.c_int] * 3 + [_f64p, _f64p, ctypes.c_double, _i32p, ctypes.c_int,
                                                            ctypes.c_int, ctypes.c_int, _i64p, _i32p]
         L.orc_correct_ex.restype = ctypes.c_int
+        L.orc_correct_rounds.argtypes = [ctypes.c_int] * 3 + [_f64p, _f64p, ctypes.c_double, _i32p, ctypes.c_int,
+                                                               ctypes.c_longlong, ctypes.c_int, ctypes.c_int, _i64p,
+                                                               _i32p]
+        L.orc_correct_rounds.restype = ctypes.c_int
         L.orc_tri_verts.argtypes = [ctypes.c_int] * 4 + [_i32p, _i32p]
         L.orc_edge_ids.argtypes = [ctypes.c_int] * 4 + [_i32p, _i32p]
         L.orc_wall_detect.argtypes = [ctypes.c_int] * 3 + [_i32p] * 8 + [_i32p, _i32p, _i32p, _i64p]
@@ -115,9 +121,10 @@ def fix_cp(f, g, cnt, bound, rng, edit_type, preserve_saddles, P, Q, lists, dims
     return buf, oob
 
 
-def path_detect(P, Q, dims, connectivity=False):
+def path_detect(P, Q, dims, connectivity=False, strict=False):
     """Separatrix records (as_tet, as_cur, ds_edge, ds_vert, oob) of geometry
-    mode, or of connectivity mode (ds_vert = trouble maker)."""
+    mode, or of connectivity mode (ds_vert = trouble maker).  strict: the
+    descending records come from whole-path walks (not the reference's check)."""
     W, H, D = dims
     V, E, F, T = counts(dims)
     c = np.zeros(2, np.int32)
@@ -126,16 +133,22 @@ def path_detect(P, Q, dims, connectivity=False):
     d_e = np.empty(E, np.int32)
     d_v = np.empty(E, np.int32)
     fn = lib().orc_path_detect_conn if connectivity else lib().orc_path_detect
-    oob = fn(W, H, D, *P, *Q, c, a_t, a_c, d_e, d_v)
+    lib().orc_set_strict_ds(int(bool(strict)))
+    try:
+        oob = fn(W, H, D, *P, *Q, c, a_t, a_c, d_e, d_v)
+    finally:
+        lib().orc_set_strict_ds(0)
     na, nd = int(c[0]), int(c[1])
     return a_t[:na].copy(), a_c[:na].copy(), d_e[:nd].copy(), d_v[:nd].copy(), oob
 
 
-def correct(f, g, dims, rel_eps, flags, max_outer=0, threads=1, break_stalls=False):
+def correct(f, g, dims, rel_eps, flags, max_outer=0, threads=1, break_stalls=False, max_rounds=0, strict=False):
     """Run the full correction loop.  Returns (corrected g, stats dict, cnt).
     break_stalls: reset a box around the remaining mismatches to the original
     values when a round changes nothing (not in the reference, whose loop
-    repeats such a round forever); stats["stall_breaks"] counts them."""
+    repeats such a round forever); stats["stall_breaks"] counts them.
+    max_rounds > 0 caps the fix/apply rounds exactly (else 64 x max_outer).
+    strict: whole-path descending separatrix checks (not the reference's)."""
     W, H, D = dims
     V = counts(dims)[0]
     ff = np.ascontiguousarray(f, np.float64).reshape(-1)
@@ -144,8 +157,12 @@ def correct(f, g, dims, rel_eps, flags, max_outer=0, threads=1, break_stalls=Fal
     fl = np.ascontiguousarray(flags, np.int32)
     st = np.zeros(9, np.int64)
     cnt = np.empty(V, np.int32)
-    rc = lib().orc_correct_ex(W, H, D, ff, gg, float(rel_eps), fl, int(max_outer), int(threads), int(bool(break_stalls)),
-                              st, cnt)
+    lib().orc_set_strict_ds(int(bool(strict)))
+    try:
+        rc = lib().orc_correct_rounds(W, H, D, ff, gg, float(rel_eps), fl, int(max_outer), int(max_rounds),
+                                      int(threads), int(bool(break_stalls)), st, cnt)
+    finally:
+        lib().orc_set_strict_ds(0)
     if rc != 0:
         raise ValueError(f"oracle correction failed ({rc})")
     stats = dict(outer_iterations=int(st[0]), cp_iterations=int(st[1]), oob=int(st[2]), converged=bool(st[3]),

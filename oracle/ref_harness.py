@@ -11,9 +11,13 @@ Three sub-commands:
        (relative to the working directory of a run);
     3. read-only instrumentation: after the initial pairings it writes the
        original and decompressed pairing arrays, and after every
-       applyDeltaBuffer1 launch it writes the delta buffer and the field, and
-       at the end the edit counters, to ./dumps/.  None of it changes what the
-       program computes.
+       applyDeltaBuffer1 launch it writes the delta buffer and the field (for
+       the first DMTZ_DUMP_ROUNDS rounds, default 400), and at the end the
+       edit counters, to ./dumps/.  None of it changes what the program
+       computes.  With DMTZ_STOP_AFTER_DUMPS set, the process exits after the
+       last dumped round: for inputs on which the reference's loop never ends
+       (its rules reach a fixed point with mismatches left), the dumped rounds
+       are the output.
 ``build`` (on the GPU host): nvcc for sm_103a into oracle/_ref/dmtz_ref.
 ``run`` (on the GPU host): generates every pinned case with dmtz_gb300.synth,
   lays out the reference's file contract (input .bin, decompressed file, dummy
@@ -34,6 +38,7 @@ import shutil
 import stat
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -41,7 +46,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
 REF_DIR = os.path.join(HERE, "_ref")
-REF_SRC = "/root/reference/main_3d.cu"
+# where the reference's main_3d.cu is read from (prepare) and where the runs
+# lay out their working directories; both can be overridden
+REF_SRC = os.environ.get("DMTZ_REFERENCE_SRC", "/root/reference/main_3d.cu")
+RUN_ROOT = os.environ.get("DMTZ_REF_WORKDIR", os.path.join(tempfile.gettempdir(), "dmtz_ref_run"))
 
 # name, field kind, dims (W,H,D), seed, rel_eps, decompression model, extra kwargs, flag sets
 CASES = [
@@ -56,6 +64,13 @@ CASES = [
     ("p64", "powerlaw", (64, 64, 64), 0, 1e-4, "sz", {}, [[1, 1, 1, 0, 0, 0, 0]]),
     ("g64", "gauss", (64, 64, 64), 0, 1e-3, "uniform", {}, [[1, 0, 0, 0, 0, 0, 0]]),
 ]
+# The 64^3 extrema-only workload (sum of 32 Gaussians + N(0, 1e-3) noise,
+# eps = 1e-3 x range, g = f + U[-eps, eps], flags 0000000) for seeds 0..9.
+# The reference's loop never ends on any of them (its rules reach a fixed
+# point with false maxima left), so these runs dump the initial pairings and
+# the first STALL_ROUNDS rounds and stop; only digests are kept.
+C0_CASES = [(f"g64s{s}", "gauss", (64, 64, 64), s, 1e-3, "uniform", {}, [[0, 0, 0, 0, 0, 0, 0]]) for s in range(10)]
+STALL_ROUNDS = 24
 # large cases: no dumps, only the corrected field's digest, iteration count and timings
 BIG_CASES = [
     ("p256", "powerlaw", (256, 256, 256), 0, 1e-4, "sz", {}, [[1, 1, 1, 0, 0, 0, 0]]),
@@ -99,9 +114,15 @@ static void dmtz_dump(const char* tag, int idx, const void* dptr, size_t bytes) 
     if (fp) { fwrite(h.data(), 1, bytes, fp); fclose(fp); }
 }
 static int dmtz_round = 0;
-#define DMTZ_DUMP_ROUND() do { if (dmtz_round < 400) { \
+static int dmtz_round_cap() {
+    static int cap = -1;
+    if (cap < 0) { const char* e = getenv("DMTZ_DUMP_ROUNDS"); cap = e ? atoi(e) : 400; }
+    return cap;
+}
+#define DMTZ_DUMP_ROUND() do { if (dmtz_round < dmtz_round_cap()) { \
     dmtz_dump("buf", dmtz_round, buffer_temp, size2 * sizeof(double)); \
-    dmtz_dump("decp", dmtz_round, decp_temp, size2 * sizeof(double)); } dmtz_round++; } while (0)
+    dmtz_dump("decp", dmtz_round, decp_temp, size2 * sizeof(double)); } dmtz_round++; \
+    if (getenv("DMTZ_STOP_AFTER_DUMPS") && dmtz_round >= dmtz_round_cap()) exit(0); } while (0)
 '''
 
 DUMP_INITIAL = r'''
@@ -182,7 +203,7 @@ def run(out_dir, only=None, timeout=240, big=False):
         f, g = case_fields(kind, dims, seed, rel, decomp, kw)
         for flags in flagsets:
             tag = f"{name}_{flag_tag(flags)}"
-            wd = os.path.join("/tmp", "dmtz_ref_run", tag)
+            wd = os.path.join(RUN_ROOT, tag)
             shutil.rmtree(wd, ignore_errors=True)
             cid = "none"
             rel_s = _prepare_workdir(wd, name, f, g, rel, cid)
@@ -280,18 +301,73 @@ def run(out_dir, only=None, timeout=240, big=False):
         json.dump(summary, fh, indent=1)
 
 
+def run_rounds(out_path, cases=C0_CASES, rounds=STALL_ROUNDS, timeout=120):
+    """Digests of reference runs whose loop does not end: per case the inputs'
+    and the eight initial pairing arrays' sha256, and per round r < rounds the
+    requested vertices (delta buffer entries other than the sentinel), their
+    buffer values and the whole field after the update, as sha256 and counts."""
+    exe = os.path.join(REF_DIR, "dmtz_ref")
+    out = []
+    for name, kind, dims, seed, rel, decomp, kw, flagsets in cases:
+        f, g = case_fields(kind, dims, seed, rel, decomp, kw)
+        for flags in flagsets:
+            tag = f"{name}_{flag_tag(flags)}"
+            wd = os.path.join(RUN_ROOT, tag)
+            shutil.rmtree(wd, ignore_errors=True)
+            rel_s = _prepare_workdir(wd, name, f, g, rel, "none")
+            W, H, D = dims
+            argv = [exe, f"{name},{W},{H},{D}", repr(rel), "none"] + [str(x) for x in flags]
+            env = dict(os.environ, PATH=os.path.join(wd, "bin") + ":" + os.environ.get("PATH", ""), DMTZ_DUMP="1",
+                       DMTZ_DUMP_ROUNDS=str(rounds), DMTZ_STOP_AFTER_DUMPS="1")
+            t = time.time()
+            try:
+                p = subprocess.run(argv, cwd=wd, env=env, capture_output=True, timeout=timeout)
+                rc = p.returncode
+            except subprocess.TimeoutExpired:
+                rc = -999
+            rec = {"name": name, "kind": kind, "dims": list(dims), "seed": seed, "rel": rel, "decomp": decomp,
+                   "kw": kw, "flags": flags, "rc": rc, "wall_s": time.time() - t,
+                   "f_sha": sha(f.reshape(-1)), "g_sha": sha(g.reshape(-1))}
+            dd = os.path.join(wd, "dumps")
+            for k in ("PV", "PE", "PF", "PT", "QV", "QE", "QF", "QT"):
+                p_ = os.path.join(dd, f"{k}_0.bin")
+                if os.path.exists(p_):
+                    arr = np.fromfile(p_, np.int32)
+                    rec[k + "_sha256"] = sha(arr)
+                    rec[k + "_ncrit"] = int((arr == -1).sum())
+            sentinel = -2000.0 * float(f.max() - f.min())
+            per = []
+            r = 0
+            while os.path.exists(os.path.join(dd, f"buf_{r}.bin")):
+                b = np.fromfile(os.path.join(dd, f"buf_{r}.bin"), np.float64)
+                d = np.fromfile(os.path.join(dd, f"decp_{r}.bin"), np.float64)
+                idx = np.nonzero(b != sentinel)[0].astype(np.int32)
+                per.append({"n_req": int(idx.size), "req_idx_sha": sha(idx), "req_buf_sha": sha(b[idx]),
+                            "field_sha": sha(d), "changed": int((d != g.reshape(-1)).sum())})
+                r += 1
+            rec["rounds"] = per
+            shutil.rmtree(wd, ignore_errors=True)
+            out.append(rec)
+            print(json.dumps({k: rec[k] for k in ("name", "rc", "wall_s")} | {"rounds": len(per)}), flush=True)
+    with open(out_path, "w") as fh:
+        json.dump(out, fh, indent=1)
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("cmd", choices=["prepare", "build", "run"])
+    ap.add_argument("cmd", choices=["prepare", "build", "run", "rounds"])
+    ap.add_argument("--src", default=REF_SRC, help="prepare: the reference's main_3d.cu")
     ap.add_argument("--out", default=os.path.join(REPO, "ref_runs"))
     ap.add_argument("--only", nargs="*")
     ap.add_argument("--timeout", type=float, default=240)
     ap.add_argument("--big", action="store_true", help="run the large timing cases (no dumps)")
     a = ap.parse_args()
     if a.cmd == "prepare":
-        prepare()
+        prepare(a.src)
     elif a.cmd == "build":
         build()
+    elif a.cmd == "rounds":
+        run_rounds(os.path.join(a.out, "rounds_c0.json"))
     else:
         run(a.out, a.only, a.timeout, a.big)
 
