@@ -31,6 +31,25 @@ def test_batch_equals_single(gpu_ctx):
         assert rep["outer_iterations"] == wrep["outer_iterations"]
 
 
+def test_batch_float32_matches_oracle(gpu_ctx):
+    """The batch path's float32 fields (widened to float64 on the way in)
+    against the oracle directly, not only against dmtz_correct: values and
+    round counts, bit for bit."""
+    from oracle import oracle as O
+
+    fields = _fields()
+    f32 = [x for x in fields if x[0].dtype == np.float32]
+    assert len(f32) >= 2
+    res = gpu_ctx.correct_batch(f32, workers=2, max_rounds=5000)
+    for (f, g, rel), (out, rep, st) in zip(f32, res):
+        D, H, W = f.shape
+        want, wst, _ = O.correct(f.astype(np.float64).reshape(-1), g.astype(np.float64).reshape(-1), (W, H, D), rel,
+                                 [1, 1, 1, 0, 0, 0, 0], max_outer=500, break_stalls=True)
+        assert st == 0 and rep["converged"] and wst["converged"] and wst["oob"] == 0
+        assert np.array_equal(out.reshape(-1), want)
+        assert rep["outer_iterations"] == wst["outer_iterations"] and rep["stall_breaks"] == wst["stall_breaks"]
+
+
 def test_tuning_does_not_change_results(gpu_ctx):
     from dmtz_gb300 import synth
 
