@@ -21,7 +21,8 @@ agree.
                     sample of the same workload (its first 96^3 corner block,
                     with the whole field's absolute bound).
 Multi-GPU: independent fields per rank (replicas, weak scaling), barrier +
-max over ranks of the timed region.
+max over ranks of the timed region.  `--gpus N` without a launcher starts the
+N ranks itself (torch.distributed.run on 127.0.0.1).
 """
 from __future__ import annotations
 
@@ -517,6 +518,36 @@ def sweep_only(size: int):
     ctx.close()
 
 
+def free_port() -> int:
+    import socket
+
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        return sk.getsockname()[1]
+
+
+def spawn_ranks(n: int, argv) -> int:
+    """`bench.py --gpus N` started without a launcher: start the N ranks
+    (one process per GPU, torch.distributed.run on 127.0.0.1) with the same
+    arguments and return their exit status.  Rank 0 prints the JSON line."""
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}",
+           "--master-addr=127.0.0.1", f"--master-port={free_port()}", os.path.abspath(__file__), *argv]
+    return subprocess.run(cmd).returncode
+
+
+def dist_check(args, rank, world):
+    """Launcher check without GPUs (gloo): every rank joins the group, the
+    max over ranks of a rank-dependent time is taken, rank 0 prints it."""
+    import torch.distributed as dist
+
+    dist.init_process_group("gloo")
+    t = max_over_ranks([0.5 + rank], dist, "cpu")[0]
+    dist.barrier()
+    if rank == 0:
+        print(json.dumps({"world": dist.get_world_size(), "max_t": t, "n_gpus": args.gpus}), flush=True)
+    dist.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -540,7 +571,13 @@ def main():
     ap.add_argument("--save-params", default="", help="learned workload: write the trained parameters (.npy)")
     ap.add_argument("--min-drop", type=float, nargs="+", default=[0.25, 0.5, 1.0],
                     help="learned workload: proposal thresholds (x bound) to evaluate")
+    ap.add_argument("--dist-check", action="store_true", help=argparse.SUPPRESS)
     args = ap.parse_args()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(spawn_ranks(args.gpus, sys.argv[1:]))
+    if args.dist_check:
+        dist_check(args, int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)))
+        return
     if args.workload == "batch":
         run_batch(args)
         return
@@ -559,7 +596,7 @@ def main():
         sweep_only(args.sweep_only)
         return
     rank = int(os.environ.get("RANK", 0))
-    world = int(os.environ.get("WORLD_SIZE", args.gpus if args.gpus == 1 else 1))
+    world = int(os.environ.get("WORLD_SIZE", 1))
     local_rank = int(os.environ.get("LOCAL_RANK", 0))
     if args.impl == "reference":
         run_reference(args, rank)
