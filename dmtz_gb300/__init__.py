@@ -37,7 +37,7 @@ class DmtzError(RuntimeError):
 class Opts(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int) for n in (
         "preserve_saddles", "preserve_vpath", "preserve_geometry", "filtration", "preserve_connectors",
-        "preserve_type", "edit_type", "max_rounds", "use_graph", "break_stalls")]
+        "preserve_type", "edit_type", "max_rounds", "use_graph", "break_stalls", "strict_separatrices")]
 
 
 class Report(ctypes.Structure):
@@ -87,6 +87,8 @@ def load_library(build_if_missing: bool = True):
     L.dmtz_mismatch.argtypes = [_vp, _int, _int, _int, _f64p, _f64p, _i64p, _i32p, _i32p, _i32p, _i32p]
     L.dmtz_fix_round.argtypes = [_vp, _int, _int, _int, _f64p, _f64p, _i32p, ctypes.c_double, _int, _int, _f64p]
     L.dmtz_path_detect.argtypes = [_vp, _int, _int, _int, _f64p, _f64p, _i64p, _i32p, _i32p, _i32p, _i32p]
+    L.dmtz_path_detect_strict.argtypes = [_vp, _int, _int, _int, _f64p, _f64p, _i64p, _i32p, _i32p, _i32p, _i32p]
+    L.dmtz_separatrix_agreement.argtypes = [_vp, _int, _int, _int, _vp, _vp, _int, _i64p]
     L.dmtz_path_detect_connectivity.argtypes = [_vp, _int, _int, _int, _f64p, _f64p, _i64p, _i32p, _i32p, _i32p,
                                                 _i32p]
     L.dmtz_path_detect_connectivity.restype = _int
@@ -244,28 +246,31 @@ class Context:
         n = int(c[0])
         return ws[:n].copy(), we[:n].copy()
 
-    def path_detect(self, f, g, dims=None, connectivity=False):
+    def path_detect(self, f, g, dims=None, connectivity=False, strict=False):
         """Separatrix records (as_tet, as_cur, ds_edge, ds_vert), sorted: geometry
-        mode, or connectivity mode (ds_vert = trouble maker)."""
+        mode, or connectivity mode (ds_vert = trouble maker); strict: whole-path
+        descending checks (dmtz_path_detect_strict)."""
         dims = _dims_of(np.asarray(f), dims)
         V, E, F, T = cell_counts(dims)
         c = np.zeros(2, np.int64)
         at, ac = np.empty(F, np.int32), np.empty(F, np.int32)
         de, dv = np.empty(E, np.int32), np.empty(E, np.int32)
-        fn = self._L.dmtz_path_detect_connectivity if connectivity else self._L.dmtz_path_detect
+        fn = self._L.dmtz_path_detect_connectivity if connectivity else (
+            self._L.dmtz_path_detect_strict if strict else self._L.dmtz_path_detect)
         self._check(fn(self._h, *dims, _flat(f), _flat(g), c, at, ac, de, dv))
         na, nd = int(c[0]), int(c[1])
         return at[:na].copy(), ac[:na].copy(), de[:nd].copy(), dv[:nd].copy()
 
     def correct(self, f, g, rel_eps, flags=(1, 1, 1, 0, 0, 0, 0), dims=None, max_rounds=0, use_graph=0,
-                return_counter=False, break_stalls=True):
-        """Full correction of g against f.  Returns (corrected g, report dict[, edit counter])."""
+                return_counter=False, break_stalls=True, strict=False):
+        """Full correction of g against f.  Returns (corrected g, report dict[, edit counter]).
+        strict: whole-path descending separatrix checks (dmtz_opts.strict_separatrices)."""
         dims = _dims_of(np.asarray(f), dims)
         ff = _flat(f)
         gg = np.array(_flat(g), copy=True)
         V = ff.size
         cnt = np.empty(V, np.int32)
-        o = Opts(*[int(x) for x in flags], int(max_rounds), int(use_graph), int(bool(break_stalls)))
+        o = Opts(*[int(x) for x in flags], int(max_rounds), int(use_graph), int(bool(break_stalls)), int(bool(strict)))
         r = Report()
         rc = self._L.dmtz_correct(self._h, *dims, ff.ctypes.data, gg.ctypes.data, 0, float(rel_eps),
                                   ctypes.byref(o), ctypes.byref(r), cnt.ctypes.data)
@@ -348,17 +353,33 @@ class Context:
         return best[0], best[1], ms.value
 
     def correct_ptr(self, f_ptr: int, g_ptr: int, dims, rel_eps, flags=(1, 1, 1, 0, 0, 0, 0), on_device=True,
-                    max_rounds=0, use_graph=0, allow_nonconverged=False, break_stalls=True):
+                    max_rounds=0, use_graph=0, allow_nonconverged=False, break_stalls=True, strict=False):
         """Correction on raw float64 buffers (device pointers when on_device, else host
         pointers, e.g. pinned memory); g is edited in place.  With
         allow_nonconverged, hitting max_rounds returns the report (converged
         False) instead of raising."""
-        o = Opts(*[int(x) for x in flags], int(max_rounds), int(use_graph), int(bool(break_stalls)))
+        o = Opts(*[int(x) for x in flags], int(max_rounds), int(use_graph), int(bool(break_stalls)), int(bool(strict)))
         r = Report()
         self._check(self._L.dmtz_correct(self._h, *dims, _vp(f_ptr), _vp(g_ptr), int(bool(on_device)),
                                          float(rel_eps), ctypes.byref(o), ctypes.byref(r), None),
                     allow=(4,) if allow_nonconverged else ())
         return r.as_dict()
+
+    def separatrix_agreement(self, f, g, dims=None, on_device=False):
+        """Labels of g's gradient against f's at the original saddles: dict with
+        the 1-saddle endpoints compared / with equal descending labels, the
+        2-saddle cofaces compared / with equal ascending labels, and the cells
+        whose criticality differs.  f, g: host arrays, or device pointers
+        (ints) with on_device and dims."""
+        out = np.zeros(5, np.int64)
+        if on_device:
+            self._check(self._L.dmtz_separatrix_agreement(self._h, *dims, _vp(f), _vp(g), 1, out))
+        else:
+            dims = _dims_of(np.asarray(f), dims)
+            ff, gg = _flat(f), _flat(g)
+            self._check(self._L.dmtz_separatrix_agreement(self._h, *dims, ff.ctypes.data, gg.ctypes.data, 0, out))
+        return {"desc_compared": int(out[0]), "desc_equal": int(out[1]), "asc_compared": int(out[2]),
+                "asc_equal": int(out[3]), "crit_differ": int(out[4])}
 
     def profile_sweep(self, f_ptr: int, g_ptr: int, dims, reps=10, on_device=True):
         """Mean per-launch ms of the six gradient-sweep kernels and of the whole sweep."""

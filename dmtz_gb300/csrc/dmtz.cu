@@ -979,6 +979,63 @@ __global__ void k_ds_back(PathRec R, const i64 *te, const i64 *tv, const unsigne
     }
 }
 
+// Strict descending check (dmtz_opts.strict_separatrices; no counterpart in
+// the reference).  get_false_ds_vpath compares each endpoint's pairing only
+// at the first vertex of its path (see above); this check walks the whole
+// original descending path of each endpoint of every original 1-saddle (v1,
+// the higher id, first; the walk follows the original steepest-descent
+// pairing to a minimum) and records the first vertex whose decompressed
+// pairing differs, in the same record format, so fix_ds_vpath's rule
+// (rule_ds_path) repairs it.  With no record left, every original descending
+// separatrix is a decompressed one vertex for vertex, so the descending
+// labels of all 1-saddle endpoints agree.
+__device__ __forceinline__ i64 dir_offset(const Grid &g, int d) {
+    i64 o = 0;
+#pragma unroll
+    for (int i = 0; i < 14; i++)
+        if (d == i) o = g.doff[i];
+    return o;
+}
+__global__ void k_ds_strict(RuleCtx c, PathRec R, i64 step_cap) {
+    const Grid &g = c.g;
+    for (i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x; v < g.V; v += (i64)gridDim.x * blockDim.x) {
+        const uint32_t m = (c.P.crit[v] >> 1) & 0x7Fu;
+        if (!m) continue;
+        int x, y, z;
+        decode_v(g, v, x, y, z);
+        DMTZ_FOR(7, K, {
+            constexpr int k = decltype(K)::value;
+            constexpr int c0 = cxt::TOPO_EDGE_V[k][0], c1 = cxt::TOPO_EDGE_V[k][1];
+            if ((m >> k) & 1u) {
+                const i64 ends[2] = {v + cxt::ccx(c0) + cxt::ccy(c0) * (i64)g.W + cxt::ccz(c0) * g.WH,
+                                     v + cxt::ccx(c1) + cxt::ccy(c1) * (i64)g.W + cxt::ccz(c1) * g.WH};
+                for (int j = 0; j < 2; j++) {
+                    i64 u = ends[j];
+                    bool found = false;
+                    for (i64 step = 0;; step++) {
+                        const int po = c.P.pv[u];
+                        if (po == 15) break;  // an original minimum: the path is clean
+                        if (po != c.Q.pv[u]) {
+                            const unsigned long long at = agg_slot(R.n + 1);
+                            if ((i64)at < R.cap_ds) {
+                                R.ds_edge[at] = edge_ref(g, x, y, z, k);
+                                R.ds_vert[at] = u;
+                            }
+                            found = true;
+                            break;
+                        }
+                        if (step >= step_cap) {  // a cycle: not a gradient
+                            atomicOr(c.err, ERR_WALK);
+                            break;
+                        }
+                        u += dir_offset(g, po);
+                    }
+                    if (found) break;
+                }
+            }
+        });
+    }
+}
 
 __global__ void k_fix_path(RuleCtx c, PathRec R) {
     const i64 na = min((i64)R.n[0], R.cap_as), nd = min((i64)R.n[1], R.cap_ds);
@@ -1406,6 +1463,7 @@ struct dmtz_ctx {
     uint32_t *brick_flags = nullptr;  // per brick (a byte each, four to a word): radius bits of the next sweep
     uint8_t *brick_fresh = nullptr;   // per brick: re-paired by the current round's criticality pass
     int inc_scan = 0;                 // repairs rebuild the mismatch lists incrementally (see k_list_keep)
+    int strict_ds = 0;                // descending separatrix checks walk whole paths (k_ds_strict)
     i64 *list_tmp[4] = {nullptr, nullptr, nullptr, nullptr};  // rebuilt mismatch lists, capL entries each
     uint32_t *brick_list = nullptr;   // compacted lists per radius, capB entries each
     unsigned long long *brick_n = nullptr;  // their lengths
@@ -1943,6 +2001,10 @@ void launch_detect(dmtz_ctx *ctx, const Grid &g, const RuleCtx &rc, const PathRe
         k_path_as_walk<<<grid, kBlock, 0, st>>>(g, ctx->sad2, ctx->counters + 10, ctx->P.tcode, ctx->Q.tcode,
                                                 ctx->succ, ctx->as_res, g.T + 16, ctx->errword, ctx->walk_box, T);
         k_path_as_pick<<<grid, kBlock, 0, st>>>(g, ctx->sad2, ctx->counters + 10, ctx->as_res, R);
+        if (ctx->strict_ds) {  // whole-path descending checks of every 1-saddle, into the records
+            k_ds_strict<<<grid, kBlock, 0, st>>>(rc, R, g.V + 16);
+            return;
+        }
         cudaMemsetAsync(ctx->counters + 26, 0, sizeof(unsigned long long), st);
         k_ds_keep<<<grid, kBlock, 0, st>>>(g, R, ctx->counters + 25, ctx->counters + 24, ctx->ds_tmp_edge,
                                            ctx->ds_tmp_vert, ctx->counters + 26, ctx->capDST, T);
@@ -1952,9 +2014,11 @@ void launch_detect(dmtz_ctx *ctx, const Grid &g, const RuleCtx &rc, const PathRe
                                            ctx->counters + 24);
     }
 }
+// kernels one detection launches
+int detect_kernels(const dmtz_ctx *ctx, int conn) { return conn ? 2 : (ctx->strict_ds ? 6 : 8); }
 void detect_paths(dmtz_ctx *ctx, const Grid &g, const RuleCtx &rc, const PathRec &R, unsigned grid, int conn = 0) {
     launch_detect(ctx, g, rc, R, grid, conn);
-    ctx->launches += conn ? 2 : 8;
+    ctx->launches += detect_kernels(ctx, conn);
 }
 
 // Wall records (preserve_connectors = 1) of the current decompressed gradient:
@@ -2080,6 +2144,56 @@ dmtz_status upload(dmtz_ctx *ctx, double *dst, const double *src, i64 n, int on_
 // =============================================================================
 // C ABI
 // =============================================================================
+// Separatrix agreement of two gradients (measurement and acceptance checks;
+// no counterpart in the reference): per original 1-saddle edge, the descending
+// labels of its two endpoints, and per original 2-saddle triangle, the
+// ascending labels of its cofaces, in the original field (dP, aP) and in the
+// decompressed one (dQ, aQ).  out: [0] endpoints compared, [1] equal, [2]
+// cofaces compared, [3] equal, [4] anchor cells whose criticality differs.
+__global__ void k_sep_agree(Grid g, const uint32_t *critP, const uint32_t *critQ, const i64 *dP, const i64 *dQ,
+                            const i64 *aP, const i64 *aQ, unsigned long long *out) {
+    unsigned long long c[5] = {0, 0, 0, 0, 0};
+    for (i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x; v < g.V; v += (i64)gridDim.x * blockDim.x) {
+        const uint32_t cp = critP[v];
+        c[4] += __popc(cp ^ critQ[v]);
+        const uint32_t m1 = (cp >> 1) & 0x7Fu, m2 = (cp >> 8) & 0xFFFu;
+        if (!(m1 | m2)) continue;
+        int x, y, z;
+        decode_v(g, v, x, y, z);
+        DMTZ_FOR(7, K, {
+            constexpr int k = decltype(K)::value;
+            constexpr int c0 = cxt::TOPO_EDGE_V[k][0], c1 = cxt::TOPO_EDGE_V[k][1];
+            if ((m1 >> k) & 1u) {
+                const i64 a = v + cxt::ccx(c0) + cxt::ccy(c0) * (i64)g.W + cxt::ccz(c0) * g.WH;
+                const i64 b = v + cxt::ccx(c1) + cxt::ccy(c1) * (i64)g.W + cxt::ccz(c1) * g.WH;
+                c[0] += 2;
+                c[1] += (dP[a] == dQ[a]) + (dP[b] == dQ[b]);
+            }
+        });
+        DMTZ_FOR(12, S, {
+            constexpr int sl = decltype(S)::value;
+            if ((m2 >> sl) & 1u) {
+                DMTZ_FOR(cxt::TOPO_FACE_NCOF[sl], J, {
+                    constexpr int j = decltype(J)::value;
+                    constexpr int tx = cxt::TOPO_FACE_COF[sl][j][0], ty = cxt::TOPO_FACE_COF[sl][j][1],
+                                  tz = cxt::TOPO_FACE_COF[sl][j][2], ts = cxt::TOPO_FACE_COF[sl][j][3];
+                    if (cell_ok(g, x + tx, y + ty, z + tz, 1, 1, 1)) {
+                        const i64 t = (v + tx + ty * (i64)g.W + tz * g.WH) * 6 + ts;
+                        c[2] += 1;
+                        c[3] += aP[t] == aQ[t];
+                    }
+                });
+            }
+        });
+    }
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        unsigned long long x = c[k];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if ((threadIdx.x & 31) == 0 && x) atomicAdd(out + k, x);
+    }
+}
+
 extern "C" {
 
 dmtz_status dmtz_ctx_create(dmtz_ctx **out, int device) {
@@ -2225,10 +2339,11 @@ dmtz_status dmtz_fix_round(dmtz_ctx *ctx, int W, int H, int D, const double *ori
 
 static dmtz_status path_detect_impl(dmtz_ctx *ctx, int W, int H, int D, const double *orig, const double *decp,
                                     int conn, int64_t counts[2], int32_t *as_tet, int32_t *as_cur, int32_t *ds_edge,
-                                    int32_t *ds_vert) {
+                                    int32_t *ds_vert, int strict = 0) {
     Grid g;
     dmtz_status s = check_dims(ctx, W, H, D, g);
     if (s != DMTZ_OK) return s;
+    ctx->strict_ds = strict && !conn;
     CK(cudaSetDevice(ctx->device));
     if ((s = setup_pair(ctx, g, orig, decp)) != DMTZ_OK) return s;
     CK(cudaMemsetAsync(ctx->errword, 0, sizeof(int), ctx->stream));
@@ -2293,6 +2408,12 @@ dmtz_status dmtz_path_detect(dmtz_ctx *ctx, int W, int H, int D, const double *o
                              int64_t counts[2], int32_t *as_tet, int32_t *as_cur, int32_t *ds_edge,
                              int32_t *ds_vert) {
     return path_detect_impl(ctx, W, H, D, orig, decp, 0, counts, as_tet, as_cur, ds_edge, ds_vert);
+}
+
+dmtz_status dmtz_path_detect_strict(dmtz_ctx *ctx, int W, int H, int D, const double *orig, const double *decp,
+                                    int64_t counts[2], int32_t *as_tet, int32_t *as_cur, int32_t *ds_edge,
+                                    int32_t *ds_vert) {
+    return path_detect_impl(ctx, W, H, D, orig, decp, 0, counts, as_tet, as_cur, ds_edge, ds_vert, 1);
 }
 
 dmtz_status dmtz_path_detect_connectivity(dmtz_ctx *ctx, int W, int H, int D, const double *orig,
@@ -2633,6 +2754,7 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
     if (!(rel_eps >= 0.0) || !std::isfinite(rel_eps)) return fail(ctx, DMTZ_ERR_ARG, "rel_eps must be finite and >= 0");
     const i64 max_rounds = opts->max_rounds > 0 ? opts->max_rounds : 100000;
     ctx->inc_scan = 0;  // full scans until the loop starts
+    ctx->strict_ds = (opts->strict_separatrices && !conn) ? 1 : 0;
     CK(cudaSetDevice(ctx->device));
     if ((s = ensure(ctx, g)) != DMTZ_OK) return s;
     cudaStream_t st = ctx->stream;
@@ -2759,7 +2881,7 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
             }
             pt_.end();
             // kernels per body run: switch + control, plus each state's own
-            const int64_t det = conn ? 2 : 8;  // separatrix detection kernels
+            const int64_t det = detect_kernels(ctx, conn);  // separatrix detection kernels
             // a fix round: fix + update, then the repair (dirty marks, compaction,
             // fresh and tile marks, six passes, the list rebuild)
             const int64_t rnd = 2 + 2 + (ctx->inc_scan ? 1 : 0) + (ctx->tile_dirty ? 1 : 0) + 6 + (ctx->inc_scan ? 3 : 1);
@@ -3022,6 +3144,56 @@ dmtz_status dmtz_labels(dmtz_ctx *ctx, int W, int H, int D, const double *data, 
     return s;
 }
 
+dmtz_status dmtz_separatrix_agreement(dmtz_ctx *ctx, int W, int H, int D, const double *orig, const double *decp,
+                                      int on_device, int64_t out[5]) {
+    Grid g;
+    dmtz_status s = check_dims(ctx, W, H, D, g);
+    if (s != DMTZ_OK) return s;
+    if (!out) return fail(ctx, DMTZ_ERR_ARG, "null output");
+    CK(cudaSetDevice(ctx->device));
+    if ((s = ensure(ctx, g)) != DMTZ_OK) return s;
+    if ((s = upload(ctx, ctx->f, orig, g.V, on_device)) != DMTZ_OK) return s;
+    if ((s = upload(ctx, ctx->g, decp, g.V, on_device)) != DMTZ_OK) return s;
+    cudaStream_t st = ctx->stream;
+    run_pairing(ctx, g, view(ctx->P, ctx->f), nullptr, 1);
+    run_pairing(ctx, g, view(ctx->Q, ctx->g), nullptr, 1);
+    i64 *dP = nullptr, *dQ = nullptr, *aP = nullptr, *aQ = nullptr;
+    uint8_t *succQ = nullptr;
+    unsigned long long *cnt = nullptr;
+    auto release = [&]() {
+        cudaFree(dP); cudaFree(dQ); cudaFree(aP); cudaFree(aQ); cudaFree(succQ); cudaFree(cnt);
+    };
+    if (dalloc(&dP, g.V) != cudaSuccess || dalloc(&dQ, g.V) != cudaSuccess || dalloc(&aP, 6 * g.V) != cudaSuccess ||
+        dalloc(&aQ, 6 * g.V) != cudaSuccess || dalloc(&succQ, 8 * g.V) != cudaSuccess || dalloc(&cnt, 5) != cudaSuccess) {
+        release();
+        return fail(ctx, DMTZ_ERR_CUDA, "cannot allocate label buffers");
+    }
+    const unsigned pg = persistent_grid();
+    k_path_succ<<<grid_for(g.V), kBlock, 0, st>>>(g, ctx->P.tcode, ctx->succ);
+    k_path_succ<<<grid_for(g.V), kBlock, 0, st>>>(g, ctx->Q.tcode, succQ);
+    k_desc_init<<<pg, kBlock, 0, st>>>(g, ctx->P.pv, dP);
+    k_desc_init<<<pg, kBlock, 0, st>>>(g, ctx->Q.pv, dQ);
+    k_asc_init<<<pg, kBlock, 0, st>>>(g, ctx->P.tcode, ctx->succ, aP);
+    k_asc_init<<<pg, kBlock, 0, st>>>(g, ctx->Q.tcode, succQ, aQ);
+    s = jump_to_roots(ctx, dP, g.V);
+    if (s == DMTZ_OK) s = jump_to_roots(ctx, dQ, g.V);
+    if (s == DMTZ_OK) s = jump_to_roots(ctx, aP, 6 * g.V);
+    if (s == DMTZ_OK) s = jump_to_roots(ctx, aQ, 6 * g.V);
+    if (s == DMTZ_OK) {
+        unsigned long long h[5];
+        if (cudaMemsetAsync(cnt, 0, 5 * sizeof(unsigned long long), st) != cudaSuccess) s = DMTZ_ERR_CUDA;
+        k_sep_agree<<<pg, kBlock, 0, st>>>(g, ctx->P.crit, ctx->Q.crit, dP, dQ, aP, aQ, cnt);
+        if (s == DMTZ_OK && (cudaMemcpyAsync(h, cnt, sizeof(h), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                             cudaStreamSynchronize(st) != cudaSuccess))
+            s = fail(ctx, DMTZ_ERR_CUDA, "label comparison failed");
+        if (s == DMTZ_OK)
+            for (int k = 0; k < 5; k++) out[k] = (int64_t)h[k];
+    }
+    release();
+    CK(cudaGetLastError());
+    return s;
+}
+
 dmtz_status dmtz_device_name(const dmtz_ctx *ctx, char *buf, int len) {
     if (!ctx || !buf || len < 1) return DMTZ_ERR_ARG;
     cudaDeviceProp p;
@@ -3270,8 +3442,8 @@ constexpr i64 kNaFp3 = kNaEa2 + na_round(kNaV * 4);
 constexpr i64 kNaFa3 = kNaFp3 + na_round(kNaV * 2);
 constexpr i64 kNaEup = kNaFa3 + na_round(kNaV * 4);
 constexpr i64 kNaFup = kNaEup + na_round(kNaV * 4);
-constexpr i64 kNaCrit = kNaFup + na_round(kNaV * 4);
-constexpr i64 kNaBytes = kNaCrit + na_round(kNaV * 4);
+// no criticality array: the export reads the pairing state alone
+constexpr i64 kNaBytes = kNaFup + na_round(kNaV * 4);
 
 }  // namespace
 
@@ -3284,7 +3456,9 @@ std::mutex g_noalloc_mu;
 constexpr int kNaMaxDevices = 64;
 void *g_noalloc_addr[kNaMaxDevices] = {};
 
-// device address of the scratch on the current device, looked up once per device
+// device address of the scratch on the current device, looked up once per
+// device.  The address belongs to the device's primary context: a
+// cudaDeviceReset between calls (which reloads the module) is not supported.
 cudaError_t noalloc_scratch(int dev, unsigned char **out) {
     if (dev < 0 || dev >= kNaMaxDevices) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
@@ -3304,6 +3478,9 @@ extern "C" dmtz_status dmtz_extract_noalloc(int W, int H, int D, const double *d
     if (W < 2 || H < 2 || D < 2 || !data || !PV || !PE || !PF || !PT) return DMTZ_ERR_ARG;
     const Grid g = make_grid(W, H, D);
     if (g.V > kNaV) return DMTZ_ERR_TOO_LARGE;
+    // an error left by the caller's own earlier work stays the caller's: it is
+    // reported, not cleared, and nothing is launched
+    if (cudaPeekAtLastError() != cudaSuccess) return DMTZ_ERR_CUDA;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return DMTZ_ERR_CUDA;
     unsigned char *base = nullptr;
@@ -3318,7 +3495,7 @@ extern "C" dmtz_status dmtz_extract_noalloc(int W, int H, int D, const double *d
     s.fa3 = (uint32_t *)(base + kNaFa3);
     s.eup = (uint32_t *)(base + kNaEup);
     s.fup = (uint32_t *)(base + kNaFup);
-    s.crit = (uint32_t *)(base + kNaCrit);
+    s.crit = nullptr;
     s.tcode = nullptr;
     cudaStream_t st = (cudaStream_t)stream;
     i64 nb;

@@ -24,6 +24,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <filesystem>
 #include <fstream>
 #include <iomanip>
@@ -281,6 +282,7 @@ int main(int argc, char **argv) {
         return 4;
     }
     dmtz_opts o;
+    memset(&o, 0, sizeof(o));
     o.preserve_saddles = r.flags[0];
     o.preserve_vpath = r.flags[1];
     o.preserve_geometry = r.flags[2];
@@ -294,6 +296,9 @@ int main(int argc, char **argv) {
     // until DMTZ_MAX_ROUNDS, as the reference does)
     const char *ref_stalls = std::getenv("DMTZ_REFERENCE_STALLS");
     o.break_stalls = (ref_stalls && std::atoi(ref_stalls) == 1) ? 0 : 1;
+    // DMTZ_STRICT_SEPARATRICES=1: whole-path descending separatrix checks (not the reference's output)
+    const char *strict = std::getenv("DMTZ_STRICT_SEPARATRICES");
+    o.strict_separatrices = (strict && std::atoi(strict) == 1) ? 1 : 0;
     const char *cap = std::getenv("DMTZ_MAX_ROUNDS");
     if (cap) o.max_rounds = std::atoi(cap);
     dmtz_report rep;

@@ -66,6 +66,15 @@ typedef struct {
                                  original ones (always within the bound) and go on;
                                  0: keep going until max_rounds, as the reference would.
                                  Rounds that make progress are the same either way. */
+    int strict_separatrices;  /* 0: the reference's descending separatrix check
+                                 (get_false_ds_vpath, main_3d.cu:4837-4959), which
+                                 compares each 1-saddle endpoint's pairing at the first
+                                 vertex of its path only; the output is the reference's.
+                                 1 (geometry mode): the whole original descending path
+                                 of every endpoint is compared, and its first differing
+                                 vertex fixed with the same rule (fix_ds_vpath), so that
+                                 every descending separatrix label agrees on exit; the
+                                 output then differs from the reference's. */
 } dmtz_opts;
 
 typedef struct {
@@ -135,6 +144,14 @@ dmtz_status dmtz_path_detect(dmtz_ctx *ctx, int W, int H, int D, const double *o
                              int64_t counts[2], int32_t *as_tet, int32_t *as_cur, int32_t *ds_edge,
                              int32_t *ds_vert);
 
+/* dmtz_path_detect with the descending half of strict_separatrices = 1: a
+ * record is the first vertex on a 1-saddle endpoint's whole original
+ * descending path whose decompressed pairing differs (no counterpart in the
+ * reference, whose walk stops after the first vertex).  Same arguments. */
+dmtz_status dmtz_path_detect_strict(dmtz_ctx *ctx, int W, int H, int D, const double *orig, const double *decp,
+                                    int64_t counts[2], int32_t *as_tet, int32_t *as_cur, int32_t *ds_edge,
+                                    int32_t *ds_vert);
+
 /* Connectivity-mode separatrix check (preserve_vpath=1, preserve_geometry=0):
  * a separatrix is false when its end differs, not its geometry.  Descending
  * half as get_false_ds_vpath_connectivity (main_3d.cu:4961-5062; ds_vert is
@@ -179,6 +196,17 @@ dmtz_status dmtz_correct(dmtz_ctx *ctx, int W, int H, int D, const double *orig,
  * jumping does not settle in 64 rounds. */
 dmtz_status dmtz_labels(dmtz_ctx *ctx, int W, int H, int D, const double *data, int on_device, int32_t *desc,
                         int32_t *asc);
+
+/* Separatrix agreement of `decp`'s gradient with `orig`'s (the acceptance
+ * check "the re-extracted MSC has the original's separatrix labels"; no
+ * reference counterpart): out[0] = endpoints of original 1-saddle edges
+ * compared, out[1] = of those, endpoints whose descending label (as
+ * dmtz_labels) is the same in both fields; out[2] = cofaces of original
+ * 2-saddle triangles compared, out[3] = of those, cofaces with the same
+ * ascending label; out[4] = cells whose criticality differs (all four
+ * dimensions).  Labels and counts are computed on the device. */
+dmtz_status dmtz_separatrix_agreement(dmtz_ctx *ctx, int W, int H, int D, const double *orig, const double *decp,
+                                      int on_device, int64_t out[5]);
 
 /* Decompression model on the GPU, for benchmarks and training data (the
  * reference runs an external compressor and reads the result back,
@@ -324,10 +352,13 @@ dmtz_status dmtz_correct_learned(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int
  *
  * Scratch: the per-vertex gradient state lives in one fixed device array
  * inside the library, sized for at most DMTZ_NOALLOC_MAX_VERTICES vertices
- * (64^3; about 8.7 MB that every GPU which loads the library keeps until the
+ * (64^3; about 7.6 MB that every GPU which loads the library keeps until the
  * process exits).  Larger grids return DMTZ_ERR_TOO_LARGE.  The first call on
  * a device looks up that array's device address (cudaGetSymbolAddress), so
- * make that first call before any stream capture.  All calls share the one
+ * make that first call before any stream capture.  The address is kept for
+ * the life of the process: a cudaDeviceReset between calls is not supported.
+ * A CUDA error already pending when the call starts is returned as
+ * DMTZ_ERR_CUDA and left pending; nothing is launched then.  All calls share the one
  * array: calls that can overlap on the GPU (different streams, or different
  * host threads) race and must be serialised by the caller. */
 #define DMTZ_NOALLOC_MAX_VERTICES (64 * 64 * 64)

@@ -50,6 +50,35 @@ def test_extract_noalloc_matches_extract():
     ctx.close()
 
 
+def test_extract_noalloc_side_stream_and_thin_grids():
+    """On a stream the caller created (synchronised on that stream alone),
+    including grids with an extent of 2, where every anchor lies on the
+    surface and takes the bounds-checked code."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import dmtz_gb300 as dm
+    from dmtz_gb300 import synth
+
+    fn = _noalloc_fn()
+    ctx = dm.Context(0)
+    torch.cuda.set_device(0)
+    side = torch.cuda.Stream()
+    for dims, seed in (((64, 2, 48), 41), ((2, 37, 5), 42), ((33, 31, 29), 43)):
+        f = synth.power_law(dims, seed).reshape(-1)
+        want = ctx.extract(f, dims)
+        V, E, F, T = dm.cell_counts(dims)
+        with torch.cuda.stream(side):
+            d = torch.from_numpy(f).pin_memory().to("cuda", non_blocking=True)
+            outs = [torch.full((n,), -7, dtype=torch.int32, device="cuda") for n in (V, E, F, T)]
+        rc = fn(*dims, d.data_ptr(), *[o.data_ptr() for o in outs], side.cuda_stream)
+        assert rc == 0
+        side.synchronize()
+        for got, ref, name in zip(outs, want, ("PV", "PE", "PF", "PT")):
+            assert np.array_equal(got.cpu().numpy(), ref), (dims, name)
+    ctx.close()
+
+
 def test_extract_noalloc_rejects_large_grids():
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
