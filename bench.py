@@ -158,6 +158,60 @@ def cpu_sample(f, g, threads: int):
     return SAMPLE ** 3 / dt / 1e6, dt, st
 
 
+def reference_cuda(f, g, ours_sha: str):
+    """The reference's own CUDA program on the same field and GPU: main_3d.cu,
+    built by oracle/ref_harness.py (one compile fix, the data prefix moved to
+    a working directory) into oracle/_ref/dmtz_ref, run once with its file
+    contract in a scratch directory.  Its time is its own additional_time
+    (main_3d.cu:7155, the correction after the files are read) and its phase
+    timers (:7187); its corrected field is compared with this build's.  A
+    baseline only, like cpu_baseline: run once, on rank 0."""
+    import hashlib
+    import shutil
+    import tempfile
+
+    from oracle import ref_harness as R
+
+    exe = os.path.join(R.REF_DIR, "dmtz_ref")
+    if not os.path.exists(exe):
+        return {"unavailable": "the reference program was not built on this host (oracle/_ref/dmtz_ref missing)"}
+    wd = tempfile.mkdtemp(prefix="dmtz_refcuda_")
+    name = f"bench{SIZE}"
+    try:
+        rel_s = R._prepare_workdir(wd, name, f, g, REL_EPS, "none")
+        argv = [exe, f"{name},{SIZE},{SIZE},{SIZE}", repr(REL_EPS), "none"] + [str(x) for x in FLAGS]
+        env = dict(os.environ, PATH=os.path.join(wd, "bin") + ":" + os.environ.get("PATH", ""))
+        t0 = time.perf_counter()
+        try:
+            p = subprocess.run(argv, cwd=wd, env=env, capture_output=True, timeout=900)
+            rc, out = p.returncode, p.stdout.decode(errors="replace")
+        except subprocess.TimeoutExpired:
+            return {"unavailable": "the reference program did not finish within 900 s"}
+        wall = time.perf_counter() - t0
+        rec = {"rc": rc, "wall_s": wall}
+        fx = os.path.join(wd, f"mscz/fixed_decp_data/fixed_decp_{name}_{rel_s}.bin")
+        if os.path.exists(fx):
+            raw = open(fx, "rb").read()
+            n = int(np.frombuffer(raw[:8], np.uint64)[0])
+            fixed = np.frombuffer(raw[8:], np.float64)[:n]
+            rec["output_bit_identical"] = hashlib.sha256(fixed.tobytes()).hexdigest() == ours_sha
+        sdir = os.path.join(wd, "stat_result")
+        for fn in sorted(os.listdir(sdir)):
+            for line in open(os.path.join(sdir, fn)):
+                if line.startswith("additional_time:") and "seconds" not in rec:
+                    rec["seconds"] = float(line.split(":")[1])
+                if line.startswith("iteration number:"):
+                    rec["iteration_number"] = int(line.split(":")[1])
+        for line in out.splitlines():
+            if line.startswith("build_cells:"):
+                rec["phase_timers_s"] = line.strip()
+        if "seconds" in rec:
+            rec["mvox_s"] = SIZE ** 3 / rec["seconds"] / 1e6
+        return rec
+    finally:
+        shutil.rmtree(wd, ignore_errors=True)
+
+
 def max_over_ranks(values, dist=None, device="cpu"):
     """Element-wise maximum of per-rank floats over the process group (the
     slowest rank sets the job time); the values themselves without one."""
@@ -268,6 +322,37 @@ def run_ours(args, rank, world, local_rank):
         e2e_t.append(time.perf_counter() - t1)
     e2e_step = max_over_ranks([float(np.mean(e2e_t))], dist, "cuda")[0]
 
+    # separatrix labels of the corrected field (g_dev holds the last timed
+    # step's output): the reference's descending check looks at the first
+    # vertex of each path only, so some descending labels may differ
+    out_sha = None
+    if rank == 0:
+        import hashlib
+
+        out_sha = hashlib.sha256(g_dev.cpu().numpy().tobytes()).hexdigest()
+    agree = ctx.separatrix_agreement(f_dev.data_ptr(), g_dev.data_ptr(), dims, on_device=True)
+    # the opt-in strict separatrix mode on the same field (not the reference's output)
+    g_dev.copy_(g0_dev)
+    torch.cuda.synchronize()
+    srep = ctx.correct_ptr(f_dev.data_ptr(), g_dev.data_ptr(), dims, REL_EPS, FLAGS, on_device=True,
+                           use_graph=args.graph, strict=True)
+    sagree = ctx.separatrix_agreement(f_dev.data_ptr(), g_dev.data_ptr(), dims, on_device=True)
+
+    # the reference arm's problem (the first SAMPLE^3 corner block, with the
+    # whole field's bound) on the GPU, inputs resident in HBM
+    fs, gs = octant(f, SIZE, SAMPLE), octant(g, SIZE, SAMPLE)
+    rel_s = REL_EPS * float(f.max() - f.min()) / float(fs.max() - fs.min())
+    fsd, gsd0 = torch.from_numpy(fs).cuda(), torch.from_numpy(gs).cuda()
+    gsd = gsd0.clone()
+    sdims = (SAMPLE, SAMPLE, SAMPLE)
+    s_t = []
+    for i in range(4):
+        gsd.copy_(gsd0)
+        torch.cuda.synchronize()
+        r = ctx.correct_ptr(fsd.data_ptr(), gsd.data_ptr(), sdims, rel_s, FLAGS, on_device=True, use_graph=args.graph)
+        if i:
+            s_t.append(r["seconds"])
+
     # roofline of the dominant kernel group: the gradient sweep run every round
     ms = ctx.profile_sweep(f_dev.data_ptr(), g0_dev.data_ptr(), dims, reps=20, on_device=True)
     alg_bytes = V * (2 * 8 + 1 / 8)  # read g and f, write a 1-bit mismatch flag per vertex
@@ -297,12 +382,28 @@ def run_ours(args, rank, world, local_rank):
                              "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                              "kernel": "gradient sweep (5 pairing passes + criticality)",
                              "sweep_ms": ms[6], "per_kernel_ms": [round(x, 4) for x in ms[:6]]},
-                "clocks": clk, "gpu_launches": launches}
+                "clocks": clk, "gpu_launches": launches,
+                "separatrix_agreement": {
+                    "descending": agree["desc_equal"] / max(agree["desc_compared"], 1),
+                    "ascending": agree["asc_equal"] / max(agree["asc_compared"], 1),
+                    "critical_cells_differing": agree["crit_differ"], "counts": agree,
+                    "note": "default (reference) loop: its descending check compares the first vertex of each path"},
+                "strict_separatrices": {"seconds": srep["seconds"], "mvox_s": V / srep["seconds"] / 1e6,
+                                        "outer_iterations": srep["outer_iterations"],
+                                        "converged": srep["converged"],
+                                        "descending": sagree["desc_equal"] / max(sagree["desc_compared"], 1),
+                                        "ascending": sagree["asc_equal"] / max(sagree["asc_compared"], 1),
+                                        "critical_cells_differing": sagree["crit_differ"]},
+                "same_sample": {"workload": f"first {SAMPLE}^3 corner block, the field's bound (the reference arm's "
+                                            f"problem)", "value": SAMPLE ** 3 / float(np.mean(s_t)) / 1e6,
+                                "unit": "Mvox/s", "seconds": float(np.mean(s_t))}}
         if rank == 0 and world == 1 and not args.no_cpu:
             v, dt, st = cpu_sample(f, g, os.cpu_count() or 1)
             line["cpu_baseline"] = {"value": v, "unit": "Mvox/s", "cores": os.cpu_count() or 1, "kind": "port",
                                     "sample": f"oracle full correction of the first {SAMPLE}^3 corner block (field's bound), "
                                               f"{dt:.1f} s, {st['outer_iterations']} outer iterations"}
+            if not args.no_ref_cuda:
+                line["reference_cuda"] = reference_cuda(f, g, out_sha)
         print(json.dumps(line), flush=True)
     ctx.close()
     if dist:
@@ -555,6 +656,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-ref-cuda", action="store_true", help="skip the run of the reference's CUDA program")
     ap.add_argument("--graph", type=int, default=1, help="1: loop as a CUDA graph with a device-side flag")
     ap.add_argument("--sweep-only", type=int, default=0, metavar="SIZE",
                     help="profiling aid: only time the gradient sweep on a SIZE^3 field of the same kind")

@@ -31,6 +31,44 @@ __host__ __device__ constexpr int ccy(int c) { return (c >> 1) & 1; }
 __host__ __device__ constexpr int ccz(int c) { return (c >> 2) & 1; }
 // direction from corner c to offset (x, y, z), all relative to the same anchor
 __host__ __device__ constexpr int cdir_to(int c, int x, int y, int z) { return cdir(x - ccx(c), y - ccy(c), z - ccz(c)); }
+// Candidates in increasing vertex id order.  Every candidate of a selection
+// is the anchor plus a compile-time offset (-1..2 per axis), and ids grow with
+// (dz, dy, dx) lexicographically, so visiting candidates in that order and
+// keeping the first of equal keys (a strict key comparison) takes the
+// smallest id among equal values: the (value, id) tie-break of
+// compare_vertices (main_3d.cu:1043-1049) without comparing ids.
+__host__ __device__ constexpr int lex3(int x, int y, int z) { return (z + 4) * 64 + (y + 4) * 8 + (x + 4); }
+__host__ __device__ constexpr int dir_by_id(int r) {
+    for (int i = 0; i < 14; i++) {
+        int rank = 0;
+        for (int j = 0; j < 14; j++)
+            rank += lex3(TOPO_DIRS[j][0], TOPO_DIRS[j][1], TOPO_DIRS[j][2]) <
+                    lex3(TOPO_DIRS[i][0], TOPO_DIRS[i][1], TOPO_DIRS[i][2]);
+        if (rank == r) return i;
+    }
+    return -1;
+}
+__host__ __device__ constexpr bool dir_up(int i) { return lex3(TOPO_DIRS[i][0], TOPO_DIRS[i][1], TOPO_DIRS[i][2]) > lex3(0, 0, 0); }
+__host__ __device__ constexpr int edge_cand_by_id(int k, int r) {
+    for (int i = 0; i < TOPO_EDGE_NCOF[k]; i++) {
+        int rank = 0;
+        for (int j = 0; j < TOPO_EDGE_NCOF[k]; j++)
+            rank += lex3(TOPO_EDGE_THIRD[k][j][0], TOPO_EDGE_THIRD[k][j][1], TOPO_EDGE_THIRD[k][j][2]) <
+                    lex3(TOPO_EDGE_THIRD[k][i][0], TOPO_EDGE_THIRD[k][i][1], TOPO_EDGE_THIRD[k][i][2]);
+        if (rank == r) return i;
+    }
+    return -1;
+}
+__host__ __device__ constexpr int face_cand_by_id(int s, int r) {
+    for (int i = 0; i < TOPO_FACE_NCOF[s]; i++) {
+        int rank = 0;
+        for (int j = 0; j < TOPO_FACE_NCOF[s]; j++)
+            rank += lex3(TOPO_FACE_FOURTH[s][j][0], TOPO_FACE_FOURTH[s][j][1], TOPO_FACE_FOURTH[s][j][2]) <
+                    lex3(TOPO_FACE_FOURTH[s][i][0], TOPO_FACE_FOURTH[s][i][1], TOPO_FACE_FOURTH[s][i][2]);
+        if (rank == r) return i;
+    }
+    return -1;
+}
 // index of the corner with offset (x,y,z) among a tet's four corners (-1 if none)
 __host__ __device__ constexpr int tet_corner_index(int ts, int x, int y, int z) {
     return (TOPO_TET_V[ts][0] == x + 2 * y + 4 * z)   ? 0
@@ -67,29 +105,33 @@ __device__ __forceinline__ void static_for(std::integer_sequence<int, Is...>, F 
 __device__ __forceinline__ bool bit(uint32_t m, int d) { return (m >> d) & 1u; }
 
 // ---------------------------------------------------------------- pass 1
+// s.key holds the order keys of the anchor and its neighbours (the staged
+// sweep computes them while staging).  The reference's search starts from
+// DBL_MAX with id -1, so a neighbour whose value is DBL_MAX is never taken:
+// a strict comparison against that key does the same.
 __device__ __forceinline__ void fast_vertex(const Grid &g, const FieldState &s, int v) {
-    const uint64_t kv = okey(s.val[v]);
+    const uint64_t kv = s.key[v];
     uint64_t bk = DMTZ_KEY_DBL_MAX;
-    int bid = -1;
     int bdir = 15;
     uint32_t lm = 0;
-#pragma unroll
-    for (int i = 0; i < 14; i++) {
-        const int nb = v + g.doff32[i];
-        const uint64_t kn = okey(s.val[nb]);
-        if (key_less32(kn, nb, kv, v)) {
-            lm |= 1u << i;
-            if (key_less32(kn, nb, bk, bid)) {
-                bk = kn;
-                bid = nb;
-                bdir = i;
-            }
-        }
-    }
-    s.key[v] = kv;
+    DMTZ_FOR(14, R, {
+        constexpr int i = cxt::dir_by_id(decltype(R)::value);
+        const uint64_t kn = s.key[v + off<cxt::TOPO_DIRS[i][0], cxt::TOPO_DIRS[i][1], cxt::TOPO_DIRS[i][2]>(g)];
+        // below v in (value, id) order; the neighbour's id is above v's iff dir_up
+        const bool below = cxt::dir_up(i) ? (kn < kv) : (kn <= kv);
+        lm |= below ? (1u << i) : 0u;
+        const bool better = below & (kn < bk);
+        bk = better ? kn : bk;
+        bdir = better ? i : bdir;
+    });
     s.low[v] = (uint16_t)lm;
     s.pv[v] = (uint8_t)bdir;
 }
+
+// start of the edge and triangle passes' searches: the reference starts from
+// DBL_MAX with the largest id, so a candidate whose value is DBL_MAX is taken
+// over the start; one above DBL_MAX's key, a strict comparison does the same
+#define DMTZ_KEY_ABOVE_DBL_MAX (DMTZ_KEY_DBL_MAX + 1ull)
 
 // ---------------------------------------------------------------- pass 2 / 4 (edges)
 // A2 = true: candidates below both endpoints (pass 2); false: between them (pass 4)
@@ -102,22 +144,20 @@ __device__ __forceinline__ int fast_edge_choice(const Grid &g, const FieldState 
     const bool qb = bit(lp, dpq);  // q below p: p is the higher endpoint
     claimed = qb ? (s.pv[p] == dpq) : (s.pv[q] == dqp);
     if (claimed) return -1;
-    const uint32_t lhi = qb ? lp : lq, llo = qb ? lq : lp;
-    uint64_t bk = DMTZ_KEY_DBL_MAX;
-    int bid = INT_MAX;
+    // candidates: below both endpoints (pass 2), i.e. below the lower one;
+    // or below exactly one of them (pass 4), i.e. below the higher and not
+    // below the lower one (the order is total)
+    uint64_t bk = DMTZ_KEY_ABOVE_DBL_MAX;
     int bj = -1;
-    DMTZ_FOR(cxt::TOPO_EDGE_NCOF[K], J, {
-        constexpr int j = decltype(J)::value;
+    DMTZ_FOR(cxt::TOPO_EDGE_NCOF[K], R, {
+        constexpr int j = cxt::edge_cand_by_id(K, decltype(R)::value);
         constexpr int tx = cxt::TOPO_EDGE_THIRD[K][j][0], ty = cxt::TOPO_EDGE_THIRD[K][j][1],
                       tz = cxt::TOPO_EDGE_THIRD[K][j][2];
         constexpr int dp = cxt::cdir_to(cp, tx, ty, tz), dq = cxt::cdir_to(cq, tx, ty, tz);
-        const int dlo = qb ? dq : dp, dhi = qb ? dp : dq;
-        const bool ok = A2 ? bit(llo, dlo) : (bit(lhi, dhi) & !bit(llo, dlo));
-        const int nb = v + off<tx, ty, tz>(g);
-        const uint64_t kn = s.key[nb];
-        const bool better = ok & key_less32_nb(kn, nb, bk, bid);
+        const bool ok = A2 ? (bit(lp, dp) & bit(lq, dq)) : (bit(lp, dp) ^ bit(lq, dq));
+        const uint64_t kn = s.key[v + off<tx, ty, tz>(g)];
+        const bool better = ok & (kn < bk);
         bk = better ? kn : bk;
-        bid = better ? nb : bid;
         bj = better ? j : bj;
     });
     return bj;
@@ -197,25 +237,22 @@ template <int S, bool A3>
 __device__ __forceinline__ int fast_face_choice(const Grid &g, const FieldState &s, int v, const uint32_t l[3], int jlo,
                                                 int jmid) {
     constexpr int c0 = cxt::TOPO_FACE_V[S][0], c1 = cxt::TOPO_FACE_V[S][1], c2 = cxt::TOPO_FACE_V[S][2];
-    const uint32_t llo = jlo == 0 ? l[0] : (jlo == 1 ? l[1] : l[2]);
-    const uint32_t lmid = jmid == 0 ? l[0] : (jmid == 1 ? l[1] : l[2]);
-    uint64_t bk = DMTZ_KEY_DBL_MAX;
-    int bid = INT_MAX;
+    // candidates: below the lowest corner (pass 3), i.e. below all three; or
+    // below the middle and not below the lowest one (pass 5), i.e. below
+    // exactly two of the three (the order is total)
+    uint64_t bk = DMTZ_KEY_ABOVE_DBL_MAX;
     int bj = -1;
-    DMTZ_FOR(cxt::TOPO_FACE_NCOF[S], J, {
-        constexpr int j = decltype(J)::value;
+    DMTZ_FOR(cxt::TOPO_FACE_NCOF[S], R, {
+        constexpr int j = cxt::face_cand_by_id(S, decltype(R)::value);
         constexpr int nx = cxt::TOPO_FACE_FOURTH[S][j][0], ny = cxt::TOPO_FACE_FOURTH[S][j][1],
                       nz = cxt::TOPO_FACE_FOURTH[S][j][2];
         constexpr int d0 = cxt::cdir_to(c0, nx, ny, nz), d1 = cxt::cdir_to(c1, nx, ny, nz),
                       d2 = cxt::cdir_to(c2, nx, ny, nz);
-        const int dlo = jlo == 0 ? d0 : (jlo == 1 ? d1 : d2);
-        const int dmid = jmid == 0 ? d0 : (jmid == 1 ? d1 : d2);
-        const bool ok = A3 ? bit(llo, dlo) : (bit(lmid, dmid) & !bit(llo, dlo));
-        const int nb = v + off<nx, ny, nz>(g);
-        const uint64_t kn = s.key[nb];
-        const bool better = ok & key_less32_nb(kn, nb, bk, bid);
+        const bool b0 = bit(l[0], d0), b1 = bit(l[1], d1), b2 = bit(l[2], d2);
+        const bool ok = A3 ? (b0 & b1 & b2) : (((b0 & b1) | (b0 & b2) | (b1 & b2)) & !(b0 & b1 & b2));
+        const uint64_t kn = s.key[v + off<nx, ny, nz>(g)];
+        const bool better = ok & (kn < bk);
         bk = better ? kn : bk;
-        bid = better ? nb : bid;
         bj = better ? j : bj;
     });
     return bj;
@@ -414,7 +451,7 @@ __global__ void __launch_bounds__(DMTZ_BRICK, DMTZ_SWEEP_MINB) k_sweep_sm(Grid g
     constexpr bool K = PASS <= 4, L = PASS <= 4, PV = PASS != 2 && PASS != 4, A = PASS >= 1, B = PASS >= 2,
                    C = PASS >= 2 && PASS <= 4, DD = PASS >= 4, E = PASS == 5, VAL = PASS == 0;
     __shared__ uint64_t sh_key[K ? NB : 1];
-    __shared__ double sh_val[VAL ? NB : 1];
+
     __shared__ uint16_t sh_low[L ? NB : 1];
     __shared__ uint8_t sh_pv[PV ? NB : 1];
     __shared__ uint32_t sh_a[A ? NB : 1];
@@ -424,7 +461,7 @@ __global__ void __launch_bounds__(DMTZ_BRICK, DMTZ_SWEEP_MINB) k_sweep_sm(Grid g
     __shared__ uint32_t sh_e[E ? NB : 1];
     const Grid gb = box_grid<BX, BY>();
     FieldState t;  // box views of the pass's inputs and outputs
-    t.val = sh_val;
+    t.val = nullptr;
     t.key = sh_key;
     t.low = sh_low;
     t.pv = sh_pv;
@@ -447,7 +484,7 @@ __global__ void __launch_bounds__(DMTZ_BRICK, DMTZ_SWEEP_MINB) k_sweep_sm(Grid g
             const int ux = x0 - 1 + e % BX, uy = y0 - 1 + (e / BX) % BY, uz = z0 - 1 + e / (BX * BY);
             const bool in = ux >= 0 && uy >= 0 && uz >= 0 && ux < g.W && uy < g.H && uz < g.D;
             const i64 u = in ? ux + (i64)uy * g.W + (i64)uz * g.WH : 0;
-            if (VAL) sh_val[e] = in ? s.val[u] : 0.0;
+            if (VAL) sh_key[e] = in ? okey(s.val[u]) : 0ull;  // pass 0 stages order keys
             if (PASS >= 1 && PASS <= 4) {
                 sh_low[e] = in ? s.low[u] : (uint16_t)0;
                 sh_key[e] = in ? s.key[u] : 0ull;
