@@ -89,6 +89,7 @@ def load_library(build_if_missing: bool = True):
     L.dmtz_path_detect.argtypes = [_vp, _int, _int, _int, _f64p, _f64p, _i64p, _i32p, _i32p, _i32p, _i32p]
     L.dmtz_path_detect_strict.argtypes = [_vp, _int, _int, _int, _f64p, _f64p, _i64p, _i32p, _i32p, _i32p, _i32p]
     L.dmtz_separatrix_agreement.argtypes = [_vp, _int, _int, _int, _vp, _vp, _int, _i64p]
+    L.dmtz_link_classes.argtypes = [_vp, _int, _int, _int, _vp, _int, _vp, _i64p]
     L.dmtz_path_detect_connectivity.argtypes = [_vp, _int, _int, _int, _f64p, _f64p, _i64p, _i32p, _i32p, _i32p,
                                                 _i32p]
     L.dmtz_path_detect_connectivity.restype = _int
@@ -380,6 +381,24 @@ class Context:
             self._check(self._L.dmtz_separatrix_agreement(self._h, *dims, ff.ctypes.data, gg.ctypes.data, 0, out))
         return {"desc_compared": int(out[0]), "desc_equal": int(out[1]), "asc_compared": int(out[2]),
                 "asc_equal": int(out[3]), "crit_differ": int(out[4])}
+
+    def link_classes(self, data, dims=None, per_vertex=True):
+        """Link components per vertex (uint8: lower | upper << 4, or None) and
+        the counts [minima, maxima, regular, join-saddle multiplicity,
+        split-saddle multiplicity, sum(1 - chi(lower link))]."""
+        dims = _dims_of(np.asarray(data), dims)
+        d = _flat(data)
+        out = np.zeros(d.size, np.uint8) if per_vertex else None
+        c = np.zeros(6, np.int64)
+        self._check(self._L.dmtz_link_classes(self._h, *dims, d.ctypes.data, 0,
+                                              out.ctypes.data if per_vertex else None, c))
+        return out, [int(x) for x in c]
+
+    def link_counts_ptr(self, data_ptr: int, dims):
+        """The counts of link_classes for a device buffer."""
+        c = np.zeros(6, np.int64)
+        self._check(self._L.dmtz_link_classes(self._h, *dims, _vp(data_ptr), 1, None, c))
+        return [int(x) for x in c]
 
     def profile_sweep(self, f_ptr: int, g_ptr: int, dims, reps=10, on_device=True):
         """Mean per-launch ms of the six gradient-sweep kernels and of the whole sweep."""

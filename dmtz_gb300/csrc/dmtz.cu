@@ -2144,6 +2144,107 @@ dmtz_status upload(dmtz_ctx *ctx, double *dst, const double *src, i64 n, int on_
 // =============================================================================
 // C ABI
 // =============================================================================
+// Link components of every vertex (no counterpart in the reference, which
+// classifies cells by the discrete gradient; this is the piecewise-linear
+// reading of "min / max / saddle from the lower and upper link").  The
+// Freudenthal triangulation is a flag complex, so the link of v has an edge
+// between two stencil neighbours exactly when they are adjacent, and a
+// triangle for every adjacent triple.  Lower (upper) link: the neighbours
+// below (above) v in compare_vertices order (main_3d.cu:1043-1049).
+namespace lnk {
+__host__ __device__ constexpr uint32_t adj(int i) {
+    uint32_t m = 0;
+    for (int j = 0; j < 14; j++)
+        if (j != i && cxt::cdir(cxt::TOPO_DIRS[i][0] - cxt::TOPO_DIRS[j][0], cxt::TOPO_DIRS[i][1] - cxt::TOPO_DIRS[j][1],
+                                cxt::TOPO_DIRS[i][2] - cxt::TOPO_DIRS[j][2]) >= 0)
+            m |= 1u << j;
+    return m;
+}
+// the n-th adjacent triple i < j < k (packed i | j << 4 | k << 8), -1 past the end
+__host__ __device__ constexpr int tri(int n) {
+    for (int i = 0; i < 14; i++)
+        for (int j = i + 1; j < 14; j++)
+            for (int k = j + 1; k < 14; k++)
+                if (((adj(i) >> j) & 1u) && ((adj(i) >> k) & 1u) && ((adj(j) >> k) & 1u) && n-- == 0)
+                    return i | (j << 4) | (k << 8);
+    return -1;
+}
+__host__ __device__ constexpr int ntri() {
+    int n = 0;
+    while (tri(n) >= 0) n++;
+    return n;
+}
+// the neighbours reachable from `seed` inside m
+__device__ __forceinline__ uint32_t grow(uint32_t seed, uint32_t m) {
+    uint32_t comp = seed, prev = 0;
+    while (comp != prev) {
+        prev = comp;
+        uint32_t nb = comp;
+        DMTZ_FOR(14, I, {
+            constexpr int i = decltype(I)::value;
+            nb |= ((comp >> i) & 1u) ? adj(i) : 0u;
+        });
+        comp = nb & m;
+    }
+    return comp;
+}
+__device__ __forceinline__ int components(uint32_t m) {
+    int c = 0;
+    while (m) {
+        m &= ~grow(m & (0u - m), m);
+        c++;
+    }
+    return c;
+}
+// Euler characteristic of the link's full subcomplex on m
+__device__ __forceinline__ int chi(uint32_t m) {
+    int e2 = 0, t = 0;
+    DMTZ_FOR(14, I, {
+        constexpr int i = decltype(I)::value;
+        e2 += ((m >> i) & 1u) ? __popc(adj(i) & m) : 0;
+    });
+    DMTZ_FOR(ntri(), N, {
+        constexpr int p = tri(decltype(N)::value);
+        t += (int)((m >> (p & 15)) & (m >> ((p >> 4) & 15)) & (m >> (p >> 8)) & 1u);
+    });
+    return __popc(m) - e2 / 2 + t;
+}
+}  // namespace lnk
+
+__global__ void k_link_classes(Grid g, const double *data, uint8_t *out, unsigned long long *counts) {
+    long long c[6] = {0, 0, 0, 0, 0, 0};
+    for (i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x; v < g.V; v += (i64)gridDim.x * blockDim.x) {
+        int x, y, z;
+        decode_v(g, v, x, y, z);
+        const uint64_t kv = okey(data[v]);
+        uint32_t lo = 0, up = 0;
+        DMTZ_FOR(14, I, {
+            constexpr int i = decltype(I)::value;
+            constexpr int dx = cxt::TOPO_DIRS[i][0], dy = cxt::TOPO_DIRS[i][1], dz = cxt::TOPO_DIRS[i][2];
+            if (inb(g, x + dx, y + dy, z + dz)) {
+                const uint64_t kn = okey(data[v + dx + dy * (i64)g.W + dz * g.WH]);
+                const bool below = cxt::dir_up(i) ? (kn < kv) : (kn <= kv);
+                lo |= below ? (1u << i) : 0u;
+                up |= below ? 0u : (1u << i);
+            }
+        });
+        const int cl = lnk::components(lo), cu = lnk::components(up);
+        if (out) out[v] = (uint8_t)(cl | (cu << 4));
+        c[0] += cl == 0;
+        c[1] += cu == 0;
+        c[2] += cl == 1 && cu == 1;
+        c[3] += cl >= 2 ? cl - 1 : 0;
+        c[4] += cu >= 2 ? cu - 1 : 0;
+        c[5] += 1 - lnk::chi(lo);
+    }
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        long long x = c[k];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if ((threadIdx.x & 31) == 0 && x) atomicAdd(counts + k, (unsigned long long)x);
+    }
+}
+
 // Separatrix agreement of two gradients (measurement and acceptance checks;
 // no counterpart in the reference): per original 1-saddle edge, the descending
 // labels of its two endpoints, and per original 2-saddle triangle, the
@@ -3192,6 +3293,36 @@ dmtz_status dmtz_separatrix_agreement(dmtz_ctx *ctx, int W, int H, int D, const 
     release();
     CK(cudaGetLastError());
     return s;
+}
+
+dmtz_status dmtz_link_classes(dmtz_ctx *ctx, int W, int H, int D, const double *data, int on_device, uint8_t *out,
+                              int64_t counts[6]) {
+    Grid g;
+    dmtz_status s = check_dims(ctx, W, H, D, g);
+    if (s != DMTZ_OK) return s;
+    if (!counts) return fail(ctx, DMTZ_ERR_ARG, "null counts");
+    CK(cudaSetDevice(ctx->device));
+    if ((s = ensure(ctx, g)) != DMTZ_OK) return s;
+    if ((s = upload(ctx, ctx->f, data, g.V, on_device)) != DMTZ_OK) return s;
+    cudaStream_t st = ctx->stream;
+    uint8_t *dout = nullptr;
+    unsigned long long *cnt = nullptr;
+    if ((out && dalloc(&dout, g.V) != cudaSuccess) || dalloc(&cnt, 6) != cudaSuccess) {
+        cudaFree(dout);
+        return fail(ctx, DMTZ_ERR_CUDA, "cannot allocate link buffers");
+    }
+    unsigned long long h[6];
+    cudaError_t e = cudaMemsetAsync(cnt, 0, sizeof(h), st);
+    k_link_classes<<<persistent_grid(), kBlock, 0, st>>>(g, ctx->f, dout, cnt);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, cnt, sizeof(h), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && out) e = cudaMemcpyAsync(out, dout, (size_t)g.V, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(dout);
+    cudaFree(cnt);
+    if (e != cudaSuccess) return fail(ctx, DMTZ_ERR_CUDA, cudaGetErrorString(e));
+    for (int k = 0; k < 6; k++) counts[k] = (int64_t)h[k];
+    CK(cudaGetLastError());
+    return DMTZ_OK;
 }
 
 dmtz_status dmtz_device_name(const dmtz_ctx *ctx, char *buf, int len) {

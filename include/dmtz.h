@@ -208,6 +208,22 @@ dmtz_status dmtz_labels(dmtz_ctx *ctx, int W, int H, int D, const double *data, 
 dmtz_status dmtz_separatrix_agreement(dmtz_ctx *ctx, int W, int H, int D, const double *orig, const double *decp,
                                       int on_device, int64_t out[5]);
 
+/* Piecewise-linear classification of every vertex by its link (no
+ * counterpart in the reference, whose critical cells are the unpaired cells
+ * of the discrete gradient; a diagnostic).  The link of v is spanned by its
+ * 14 stencil neighbours (two are joined when they are adjacent: the
+ * triangulation is a flag complex); its lower (upper) part holds the
+ * neighbours below (above) v in the reference's (value, id) order.
+ * out (host, V bytes, may be NULL): lower components | upper components << 4.
+ * counts: [0] minima (empty lower link; the same vertices the reference
+ * leaves unpaired), [1] maxima (empty upper link), [2] regular (one lower and
+ * one upper component), [3] join-saddle multiplicity (sum of lower
+ * components - 1 where there are two or more), [4] split-saddle multiplicity
+ * (the same for upper components), [5] sum over vertices of 1 - chi(lower
+ * link), the Euler characteristic of the grid's box: always 1. */
+dmtz_status dmtz_link_classes(dmtz_ctx *ctx, int W, int H, int D, const double *data, int on_device, uint8_t *out,
+                              int64_t counts[6]);
+
 /* Decompression model on the GPU, for benchmarks and training data (the
  * reference runs an external compressor and reads the result back,
  * main_3d.cu:6331-6356): decp = SZ-style error-bounded quantisation of orig,

@@ -2104,3 +2104,83 @@ void orc_mismatch_anchors(int W, int H, int D, const int *PV, const int *PE, con
             mask[anchor_of(&G, vs, 4)] = 1;
         }
 }
+
+/* ---------------------------------------------------------------------------
+ * Link components (no counterpart in the reference, which classifies cells by
+ * the discrete gradient; this is the piecewise-linear reading of "min / max /
+ * saddle from the lower and upper link").  The link of vertex v is the
+ * subcomplex of its 14 stencil neighbours whose simplices span a simplex with
+ * v.  The Freudenthal triangulation is a flag complex: any neighbours that are
+ * pairwise adjacent span a simplex with v, so the link's edges are the
+ * adjacent neighbour pairs and its triangles the adjacent triples.  Lower
+ * (upper) link: the neighbours below (above) v in compare_vertices order
+ * (main_3d.cu:1043-1049).  Per vertex: out[v] = (lower components) |
+ * (upper components) << 4.  counts: [0] vertices with an empty lower link
+ * (minima), [1] with an empty upper link (maxima), [2] with one lower and one
+ * upper component (regular), [3] sum of (lower components - 1) over vertices
+ * with at least two (join saddles, by multiplicity), [4] the same for upper
+ * components (split saddles), [5] sum over vertices of 1 - chi(lower link),
+ * which equals the Euler characteristic of the grid's solid box, 1 (every
+ * edge, triangle and tetrahedron is counted once, at its highest vertex).
+ * ------------------------------------------------------------------------- */
+static int link_adj(int i, int j) {
+    return i != j && is_dir(DIRS[i][0] - DIRS[j][0], DIRS[i][1] - DIRS[j][1], DIRS[i][2] - DIRS[j][2]);
+}
+
+void orc_link_classes(int W, int H, int D, const double *data, unsigned char *out, long long counts[6]) {
+    grid_t G;
+    grid_init(&G, W, H, D);
+    for (int k = 0; k < 6; k++) counts[k] = 0;
+    for (int v = 0; v < G.V; v++) {
+        const int x = v % W, y = (v / W) % H, z = v / (W * H);
+        int side[14]; /* -1 below, 1 above, 0 outside the grid */
+        for (int i = 0; i < 14; i++) {
+            const int nx = x + DIRS[i][0], ny = y + DIRS[i][1], nz = z + DIRS[i][2];
+            if (nx < 0 || ny < 0 || nz < 0 || nx >= W || ny >= H || nz >= D) {
+                side[i] = 0;
+                continue;
+            }
+            const int n = nx + ny * W + nz * W * H;
+            const int below = data[n] < data[v] || (data[n] == data[v] && n < v);
+            side[i] = below ? -1 : 1;
+        }
+        int comps[2] = {0, 0};
+        for (int h = 0; h < 2; h++) {
+            const int want = h == 0 ? -1 : 1;
+            int seen[14] = {0};
+            for (int i = 0; i < 14; i++) {
+                if (side[i] != want || seen[i]) continue;
+                comps[h]++;
+                int stack[14], sp = 0;
+                stack[sp++] = i;
+                seen[i] = 1;
+                while (sp) {
+                    const int a = stack[--sp];
+                    for (int b = 0; b < 14; b++)
+                        if (side[b] == want && !seen[b] && link_adj(a, b)) {
+                            seen[b] = 1;
+                            stack[sp++] = b;
+                        }
+                }
+            }
+        }
+        long long nv = 0, ne = 0, nt = 0; /* the lower link's simplices */
+        for (int i = 0; i < 14; i++) {
+            if (side[i] != -1) continue;
+            nv++;
+            for (int j = i + 1; j < 14; j++) {
+                if (side[j] != -1 || !link_adj(i, j)) continue;
+                ne++;
+                for (int k = j + 1; k < 14; k++)
+                    if (side[k] == -1 && link_adj(i, k) && link_adj(j, k)) nt++;
+            }
+        }
+        out[v] = (unsigned char)(comps[0] | (comps[1] << 4));
+        if (comps[0] == 0) counts[0]++;
+        if (comps[1] == 0) counts[1]++;
+        if (comps[0] == 1 && comps[1] == 1) counts[2]++;
+        if (comps[0] >= 2) counts[3] += comps[0] - 1;
+        if (comps[1] >= 2) counts[4] += comps[1] - 1;
+        counts[5] += 1 - (nv - ne + nt);
+    }
+}

@@ -136,6 +136,11 @@ void orc_mismatch_anchors(int W, int H, int D,
                           const int *PV, const int *PE, const int *PF, const int *PT,
                           const int *QV, const int *QE, const int *QF, const int *QT, unsigned char *mask);
 
+/* Link components of every vertex (lower | upper << 4) and their summary
+ * counts: minima, maxima, regular, join-saddle and split-saddle
+ * multiplicities, and sum(1 - chi(lower link)) (= 1). */
+void orc_link_classes(int W, int H, int D, const double *data, unsigned char *out, long long counts[6]);
+
 #ifdef __cplusplus
 }
 #endif

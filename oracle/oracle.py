@@ -48,6 +48,9 @@ def lib():
         L.orc_path_detect.restype = ctypes.c_int
         L.orc_path_detect_conn.argtypes = [ctypes.c_int] * 3 + [_i32p] * 8 + [_i32p] + [_i32p] * 4
         L.orc_path_detect_conn.restype = ctypes.c_int
+        L.orc_link_classes.argtypes = [ctypes.c_int] * 3 + [_f64p, np.ctypeslib.ndpointer(dtype=np.uint8,
+                                                                                         flags="C_CONTIGUOUS"), _i64p]
+        L.orc_link_classes.restype = None
         L.orc_set_strict_ds.argtypes = [ctypes.c_int]
         L.orc_set_strict_ds.restype = None
         L.orc_correct.argtypes = [ctypes.c_int] * 3 + [_f64p, _f64p, ctypes.c_double, _i32p, ctypes.c_int,
@@ -233,3 +236,14 @@ def mismatch_anchors(P, Q, dims):
     out = np.zeros(W * H * D, np.uint8)
     lib().orc_mismatch_anchors(W, H, D, *P, *Q, out)
     return out
+
+
+def link_classes(data, dims):
+    """Link components per vertex (lower | upper << 4, uint8) and the counts
+    [minima, maxima, regular, join-saddle multiplicity, split-saddle
+    multiplicity, sum(1 - chi(lower link))]."""
+    W, H, D = dims
+    out = np.zeros(W * H * D, np.uint8)
+    c = np.zeros(6, np.int64)
+    lib().orc_link_classes(W, H, D, np.ascontiguousarray(data, np.float64).reshape(-1), out, c)
+    return out, [int(x) for x in c]
