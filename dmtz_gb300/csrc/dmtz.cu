@@ -287,19 +287,31 @@ struct CpLists {
     i64 cap[4];
 };
 
-// fix_minimum, [fix_saddle, fix_2saddle], fix_maximum over the current lists
-// (the host never runs this on an overflowed list; the clamp only keeps
-// every read inside the allocation)
-__global__ void k_fix_cp(RuleCtx c, CpLists L, int preserve_saddles) {
-    const i64 n0 = min((i64)L.n[0], L.cap[0]), n1 = preserve_saddles ? min((i64)L.n[1], L.cap[1]) : 0,
-              n2 = preserve_saddles ? min((i64)L.n[2], L.cap[2]) : 0, n3 = min((i64)L.n[3], L.cap[3]);
-    const i64 total = n0 + n1 + n2 + n3;
-    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (i64)gridDim.x * blockDim.x) {
-        if (i < n0) rule_min(c, L.l[0][i]);
-        else if (i < n0 + n1) rule_saddle(c, L.l[1][i - n0]);
-        else if (i < n0 + n1 + n2) rule_2saddle(c, L.l[2][i - n0 - n1]);
-        else rule_max(c, L.l[3][i - n0 - n1 - n2]);
+// One list's rules: fix_minimum (T = 0), fix_saddle (1), fix_2saddle (2) or
+// fix_maximum (3).  One kernel per cell type: with all four rule trees in one
+// kernel, warps of different types shared the instruction cache and stalled
+// on instruction fetch (lists of millions of cells, a few active lanes per
+// warp on the divergent case trees).  The rules only set request bits, so
+// the order of the four launches does not change the result.
+template <int T>
+__global__ void __launch_bounds__(kBlock) k_fix_cp_t(RuleCtx c, CpLists L) {
+    const i64 n = min((i64)L.n[T], L.cap[T]);
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+        if (T == 0) rule_min(c, L.l[0][i]);
+        else if (T == 1) rule_saddle(c, L.l[1][i]);
+        else if (T == 2) rule_2saddle(c, L.l[2][i]);
+        else rule_max(c, L.l[3][i]);
     }
+}
+// the critical-point fix round's kernels; returns how many were launched
+inline int launch_fix_cp(const RuleCtx &rc, const CpLists &L, int preserve_saddles, unsigned grid, cudaStream_t st) {
+    k_fix_cp_t<0><<<grid, kBlock, 0, st>>>(rc, L);
+    if (preserve_saddles) {
+        k_fix_cp_t<1><<<grid, kBlock, 0, st>>>(rc, L);
+        k_fix_cp_t<2><<<grid, kBlock, 0, st>>>(rc, L);
+    }
+    k_fix_cp_t<3><<<grid, kBlock, 0, st>>>(rc, L);
+    return preserve_saddles ? 4 : 2;
 }
 
 // separatrix records
@@ -2420,7 +2432,7 @@ dmtz_status dmtz_fix_round(dmtz_ctx *ctx, int W, int H, int D, const double *ori
     CK(cudaMemsetAsync(ctx->counters + 4, 0, sizeof(unsigned long long), ctx->stream));
     CK(cudaMemsetAsync(ctx->errword, 0, sizeof(int), ctx->stream));
     RuleCtx rc = rule_ctx(ctx, g, bound, edit_type);
-    k_fix_cp<<<persistent_grid(), kBlock, 0, ctx->stream>>>(rc, cp_lists(ctx), preserve_saddles);
+    launch_fix_cp(rc, cp_lists(ctx), preserve_saddles, persistent_grid(), ctx->stream);
     double *dd = nullptr;
     CK(dalloc(&dd, g.V));
     const double sentinel = -2000.0 * range;
@@ -2731,7 +2743,7 @@ static dmtz_status run_graph_loop(dmtz_ctx *ctx, const Grid &g, const RuleCtx &r
             if (state != LS_PCHECK) {
                 cudaMemsetAsync(ctx->counters + 4, 0, sizeof(unsigned long long), st);
                 cudaMemsetAsync(ctx->counters + 7, 0, sizeof(unsigned long long), st);
-                if (state == LS_CP) k_fix_cp<<<pgrid, kBlock, 0, st>>>(rc, L, ps);
+                if (state == LS_CP) launch_fix_cp(rc, L, ps, pgrid, st);
                 else k_fix_path<<<pgrid, kBlock, 0, st>>>(rc, PR);
                 k_apply<<<pgrid, kBlock, 0, st>>>(rc, range, pt, 1, ctx->changed, nullptr);
                 repair_dirty(ctx, g, Qs, ctx->P.crit, state == LS_CP ? (ps == 1) : 1);
@@ -2986,7 +2998,8 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
             // a fix round: fix + update, then the repair (dirty marks, compaction,
             // fresh and tile marks, six passes, the list rebuild)
             const int64_t rnd = 2 + 2 + (ctx->inc_scan ? 1 : 0) + (ctx->tile_dirty ? 1 : 0) + 6 + (ctx->inc_scan ? 3 : 1);
-            ctx->launches += 2 * (fin.runs[0] + fin.runs[1] + fin.runs[2] + fin.runs[3]) + rnd * fin.runs[LS_CP] +
+            const int64_t rnd_cp = rnd - 1 + (ps == 1 ? 4 : 2);  // the fix round runs one kernel per cell type
+            ctx->launches += 2 * (fin.runs[0] + fin.runs[1] + fin.runs[2] + fin.runs[3]) + rnd_cp * fin.runs[LS_CP] +
                              (rnd + det) * fin.runs[LS_PDF] + det * fin.runs[LS_PCHECK] + rnd * fin.runs[LS_PFIX];
         }
         R.outer_iterations = fin.outer;
@@ -3014,12 +3027,12 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
             CK(cudaMemsetAsync(ctx->counters + 4, 0, sizeof(unsigned long long), st));
             CK(cudaMemsetAsync(ctx->counters + 7, 0, sizeof(unsigned long long), st));
             pt_.begin(PH_FIXCP);
-            k_fix_cp<<<pgrid, kBlock, 0, st>>>(rc, cp_lists(ctx), ps);
+            const int nfix = launch_fix_cp(rc, cp_lists(ctx), ps, pgrid, st);
             pt_.end();
             pt_.begin(PH_APPLY);
             k_apply<<<pgrid, kBlock, 0, st>>>(rc, range, pt, 1, ctx->changed, nullptr);
             pt_.end();
-            ctx->launches += 2;
+            ctx->launches += nfix + 1;
             pt_.begin(PH_PAIR);
             repair_dirty(ctx, g, Qs, ctx->P.crit, ps == 1);
             pt_.end();
