@@ -287,31 +287,59 @@ struct CpLists {
     i64 cap[4];
 };
 
-// One list's rules: fix_minimum (T = 0), fix_saddle (1), fix_2saddle (2) or
-// fix_maximum (3).  One kernel per cell type: with all four rule trees in one
-// kernel, warps of different types shared the instruction cache and stalled
-// on instruction fetch (lists of millions of cells, a few active lanes per
-// warp on the divergent case trees).  The rules only set request bits, so
-// the order of the four launches does not change the result.
+// fix_minimum, [fix_saddle, fix_2saddle], fix_maximum over the current lists
+// (the host never runs this on an overflowed list; the clamp only keeps
+// every read inside the allocation).  Two forms, chosen on the device from
+// the list lengths, so that a graph can hold both: when every listed cell
+// fits one pass of the grid (`pass` threads), k_fix_cp gives each thread one
+// cell of the concatenated lists and the four rules' latency chains overlap;
+// longer lists (the first rounds of noisy fields: millions of cells) go to
+// one kernel per cell type, k_fix_cp_t, whose code holds one rule tree: in one
+// kernel the four case trees thrashed the instruction cache (a few active
+// lanes per warp, warps stalled on instruction fetch).  The rules only set
+// request bits, so neither form changes the result.
+__device__ __forceinline__ void cp_counts(const CpLists &L, int preserve_saddles, i64 n[4]) {
+    n[0] = min((i64)L.n[0], L.cap[0]);
+    n[1] = preserve_saddles ? min((i64)L.n[1], L.cap[1]) : 0;
+    n[2] = preserve_saddles ? min((i64)L.n[2], L.cap[2]) : 0;
+    n[3] = min((i64)L.n[3], L.cap[3]);
+}
+__global__ void k_fix_cp(RuleCtx c, CpLists L, int preserve_saddles, i64 pass) {
+    i64 n[4];
+    cp_counts(L, preserve_saddles, n);
+    if (n[0] + n[1] + n[2] + n[3] > pass) return;  // the per-type kernels take it
+    i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n[0]) { rule_min(c, L.l[0][i]); return; }
+    i -= n[0];
+    if (i < n[1]) { rule_saddle(c, L.l[1][i]); return; }
+    i -= n[1];
+    if (i < n[2]) { rule_2saddle(c, L.l[2][i]); return; }
+    i -= n[2];
+    if (i < n[3]) rule_max(c, L.l[3][i]);
+}
 template <int T>
-__global__ void __launch_bounds__(kBlock) k_fix_cp_t(RuleCtx c, CpLists L) {
-    const i64 n = min((i64)L.n[T], L.cap[T]);
-    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (i64)gridDim.x * blockDim.x) {
+__global__ void k_fix_cp_t(RuleCtx c, CpLists L, int preserve_saddles, i64 pass) {
+    i64 n[4];
+    cp_counts(L, preserve_saddles, n);
+    if (n[0] + n[1] + n[2] + n[3] <= pass) return;  // k_fix_cp took it
+    for (i64 i = (i64)blockIdx.x * blockDim.x + threadIdx.x; i < n[T]; i += (i64)gridDim.x * blockDim.x) {
         if (T == 0) rule_min(c, L.l[0][i]);
         else if (T == 1) rule_saddle(c, L.l[1][i]);
         else if (T == 2) rule_2saddle(c, L.l[2][i]);
         else rule_max(c, L.l[3][i]);
     }
 }
-// the critical-point fix round's kernels; returns how many were launched
-inline int launch_fix_cp(const RuleCtx &rc, const CpLists &L, int preserve_saddles, unsigned grid, cudaStream_t st) {
-    k_fix_cp_t<0><<<grid, kBlock, 0, st>>>(rc, L);
-    if (preserve_saddles) {
-        k_fix_cp_t<1><<<grid, kBlock, 0, st>>>(rc, L);
-        k_fix_cp_t<2><<<grid, kBlock, 0, st>>>(rc, L);
+// the critical-point fix round; returns the number of kernels launched
+inline int launch_fix_cp(const RuleCtx &rc, const CpLists &L, int ps, unsigned grid, cudaStream_t st) {
+    const i64 pass = (i64)grid * kBlock;
+    k_fix_cp<<<grid, kBlock, 0, st>>>(rc, L, ps, pass);
+    k_fix_cp_t<0><<<grid, kBlock, 0, st>>>(rc, L, ps, pass);
+    if (ps) {
+        k_fix_cp_t<1><<<grid, kBlock, 0, st>>>(rc, L, ps, pass);
+        k_fix_cp_t<2><<<grid, kBlock, 0, st>>>(rc, L, ps, pass);
     }
-    k_fix_cp_t<3><<<grid, kBlock, 0, st>>>(rc, L);
-    return preserve_saddles ? 4 : 2;
+    k_fix_cp_t<3><<<grid, kBlock, 0, st>>>(rc, L, ps, pass);
+    return ps ? 5 : 3;
 }
 
 // separatrix records
@@ -1416,8 +1444,10 @@ __global__ void k_dilate(Grid g, int axis, const uint8_t *src, uint8_t *dst) {
 // at least min_drop (absolute; the network's min_drop x bound); a value that
 // the reference's own bound test |f - g| <= bound would reject becomes
 // f - bound, the value the reference falls back to (main_3d.cu:1133-1141).
+// the proposal's edits also go to the request list, so that only the bricks
+// around them are re-paired afterwards
 __global__ void k_propose(i64 V, const double *f, double *gv, const float *o, const uint8_t *active, double bound,
-                          double min_drop, uint8_t *changed) {
+                          double min_drop, uint8_t *changed, i64 *reqlist, unsigned long long *reqn) {
     for (i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x; v < V; v += (i64)gridDim.x * blockDim.x) {
         if (!active[v]) continue;
         const double fv = f[v], old = gv[v];
@@ -1428,6 +1458,7 @@ __global__ void k_propose(i64 V, const double *f, double *gv, const float *o, co
         if (nv != old) {
             gv[v] = nv;
             changed[v] = 1;
+            reqlist[agg_slot(reqn)] = v;
         }
     }
 }
@@ -2799,7 +2830,7 @@ static dmtz_status features_into(dmtz_ctx *ctx, const Grid &g, double bound, __n
 }
 
 // Learned warm start: features, network, proposal, then the gradient of the
-// edited field and its mismatch lists again.
+// edited field (around the edits) and its mismatch lists again.
 static dmtz_status learned_start(dmtz_ctx *ctx, dmtz_cnn *net, const Grid &g, double bound) {
     using namespace dmtz_cnn_impl;
     if (device_of(net) != ctx->device) return fail(ctx, DMTZ_ERR_ARG, "network and context on different devices");
@@ -2811,10 +2842,15 @@ static dmtz_status learned_start(dmtz_ctx *ctx, dmtz_cnn *net, const Grid &g, do
     if ((s = features_into(ctx, g, bound, feat, active)) != DMTZ_OK) return s;
     s = forward_on(net, g.W, g.H, g.D, feat, out, 0, ctx->stream);
     if (s != DMTZ_OK) return fail(ctx, s, "network: " + error_of(net));
+    CK(cudaMemsetAsync(ctx->counters + 4, 0, sizeof(unsigned long long), ctx->stream));
     k_propose<<<persistent_grid(), kBlock, 0, ctx->stream>>>(g.V, ctx->f, ctx->g, out, active, bound,
-                                                              (double)min_drop_of(net) * bound, ctx->changed);
+                                                              (double)min_drop_of(net) * bound, ctx->changed,
+                                                              ctx->reqlist, ctx->counters + 4);
     ctx->launches += 5;
-    run_pairing(ctx, g, view(ctx->Q, ctx->g), ctx->P.crit, 1);
+    // re-pair only the bricks within the passes' radii of the edited vertices
+    // (the mismatch lists are rebuilt by a full scan: the loop has not started)
+    repair_dirty(ctx, g, view(ctx->Q, ctx->g), ctx->P.crit, 1);
+    CK(cudaMemsetAsync(ctx->counters + 4, 0, sizeof(unsigned long long), ctx->stream));
     CK(cudaGetLastError());
     return DMTZ_OK;
 }
@@ -2998,7 +3034,7 @@ static dmtz_status correct_impl(dmtz_ctx *ctx, dmtz_cnn *net, int W, int H, int 
             // a fix round: fix + update, then the repair (dirty marks, compaction,
             // fresh and tile marks, six passes, the list rebuild)
             const int64_t rnd = 2 + 2 + (ctx->inc_scan ? 1 : 0) + (ctx->tile_dirty ? 1 : 0) + 6 + (ctx->inc_scan ? 3 : 1);
-            const int64_t rnd_cp = rnd - 1 + (ps == 1 ? 4 : 2);  // the fix round runs one kernel per cell type
+            const int64_t rnd_cp = rnd - 1 + (ps == 1 ? 5 : 3);  // the fix round's two forms (launch_fix_cp)
             ctx->launches += 2 * (fin.runs[0] + fin.runs[1] + fin.runs[2] + fin.runs[3]) + rnd_cp * fin.runs[LS_CP] +
                              (rnd + det) * fin.runs[LS_PDF] + det * fin.runs[LS_PCHECK] + rnd * fin.runs[LS_PFIX];
         }
