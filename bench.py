@@ -254,6 +254,52 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
+def learned_vs_plain(ctx, f_dev, g0_dev, g_dev, dims, args):
+    """Train the proposal network on args.traces traces of 128^3 power-law
+    fields (seeds 1000.., eps = 1e-4 x range, 10 epochs, deterministic), then
+    time the plain loop and the learned warm start on the benchmark field
+    (device seconds, median of 3 each) and report the rounds of each."""
+    import torch
+
+    import dmtz_gb300 as dm
+    from dmtz_gb300 import learned
+
+    t0 = time.perf_counter()
+    traces, skipped = learned.make_traces(ctx, args.traces, (128, 128, 128), 1000, REL_EPS)
+    gen_s = time.perf_counter() - t0
+    net = dm.Network(0, seed=0)
+    t1 = time.perf_counter()
+    hist = learned.train(net, traces, epochs=10, lr=1e-3)
+    train_s = time.perf_counter() - t1
+    del traces
+    torch.cuda.empty_cache()
+    net.set_min_drop(args.min_drop[-1])
+    res = {}
+    for name in ("plain", "learned"):
+        secs, rep = [], None
+        for _ in range(3):
+            g_dev.copy_(g0_dev)
+            torch.cuda.synchronize()
+            if name == "plain":
+                rep = ctx.correct_ptr(f_dev.data_ptr(), g_dev.data_ptr(), dims, REL_EPS, FLAGS, on_device=True,
+                                      use_graph=args.graph)
+            else:
+                rep = ctx.correct_learned_ptr(net, f_dev.data_ptr(), g_dev.data_ptr(), dims, REL_EPS, FLAGS,
+                                              on_device=True, use_graph=args.graph)
+            secs.append(rep["seconds"])
+        res[name] = {"seconds": float(np.median(secs)), "cp_rounds": rep["cp_rounds"],
+                     "path_rounds": rep["path_rounds"], "converged": rep["converged"],
+                     "edited_vertices": rep["edited_vertices"]}
+    net.close()
+    k = max(1, len(hist) // 10)
+    return {"plain": res["plain"], "learned": res["learned"],
+            "speedup_plain_over_learned": res["plain"]["seconds"] / res["learned"]["seconds"],
+            "training": {"traces": args.traces - len(skipped), "epochs": 10, "trace_generation_s": gen_s,
+                         "train_s": train_s, "loss_first_epoch": float(np.mean(hist[:k])),
+                         "loss_last_epoch": float(np.mean(hist[-k:])), "min_drop": args.min_drop[-1]},
+            "note": "the network's edits are a warm start; the exact loop finishes, so values and labels stay exact"}
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
 
@@ -353,6 +399,12 @@ def run_ours(args, rank, world, local_rank):
         if i:
             s_t.append(r["seconds"])
 
+    # learned warm start against the plain loop on the same field (the
+    # network trained here on 128^3 power-law traces; not timed above)
+    learned_ab = None
+    if rank == 0 and world == 1 and not args.no_learned:
+        learned_ab = learned_vs_plain(ctx, f_dev, g0_dev, g_dev, dims, args)
+
     # roofline of the dominant kernel group: the gradient sweep run every round
     ms = ctx.profile_sweep(f_dev.data_ptr(), g0_dev.data_ptr(), dims, reps=20, on_device=True)
     alg_bytes = V * (2 * 8 + 1 / 8)  # read g and f, write a 1-bit mismatch flag per vertex
@@ -394,6 +446,7 @@ def run_ours(args, rank, world, local_rank):
                                         "descending": sagree["desc_equal"] / max(sagree["desc_compared"], 1),
                                         "ascending": sagree["asc_equal"] / max(sagree["asc_compared"], 1),
                                         "critical_cells_differing": sagree["crit_differ"]},
+                "learned": learned_ab,
                 "same_sample": {"workload": f"first {SAMPLE}^3 corner block, the field's bound (the reference arm's "
                                             f"problem)", "value": SAMPLE ** 3 / float(np.mean(s_t)) / 1e6,
                                 "unit": "Mvox/s", "seconds": float(np.mean(s_t))}}
@@ -666,7 +719,8 @@ def main():
     ap.add_argument("--big-kind", choices=["powerlaw", "gauss"], default="powerlaw", help="big workload: field kind")
     ap.add_argument("--max-rounds", type=int, default=2000)
     ap.add_argument("--cnn-size", type=int, default=256, help="cnn workload: grid size")
-    ap.add_argument("--traces", type=int, default=64, help="learned workload: training traces")
+    ap.add_argument("--traces", type=int, default=200, help="learned workload and line: training traces")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned warm start's A/B in the default line")
     ap.add_argument("--epochs", type=int, default=10, help="learned workload: epochs")
     ap.add_argument("--lr", type=float, default=1e-3, help="learned workload: Adam learning rate")
     ap.add_argument("--eval-size", type=int, default=512, help="learned workload: held-out field size")

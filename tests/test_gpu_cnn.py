@@ -259,3 +259,57 @@ def test_training_reduces_loss(gpu_ctx):
     assert np.isfinite(hist).all()
     assert last < 0.8 * first, (first, last)
     n.close()
+
+
+def _proposal(gpu_ctx, net, f, g, dims, rel, min_drop=0.5):
+    """The vertices the network's warm start would edit (the rule of
+    dmtz_correct_learned: active, and f + bound tanh(o) lowers g by at least
+    min_drop x bound), and the active mask."""
+    V = f.size
+    fd, gd = torch.from_numpy(f).cuda(), torch.from_numpy(g).cuda()
+    feat = torch.empty((V, 16), dtype=torch.bfloat16, device="cuda")
+    active = torch.empty(V, dtype=torch.uint8, device="cuda")
+    out = torch.empty(V, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    gpu_ctx.features(fd.data_ptr(), gd.data_ptr(), dims, rel, feat.data_ptr(), active.data_ptr())
+    net.forward(feat.data_ptr(), out.data_ptr(), dims)
+    torch.cuda.synchronize()
+    bound = rel * float(f.max() - f.min())
+    p = fd + bound * torch.tanh(out.double())
+    prop = (active > 0) & (gd - p >= min_drop * bound)
+    return prop.cpu().numpy(), (active > 0).cpu().numpy()
+
+
+def test_trained_network_finds_the_loops_edits(gpu_ctx):
+    """What training gains: on a held-out field, the vertices the trained
+    network proposes to lower are much more often ones the exact loop lowers
+    than those of the untrained network, or than active vertices at random.
+    (It does not make the loop faster on the benchmark fields: the loop needs
+    as many rounds from the proposal, and the network pass costs more than it
+    saves; bench.py reports that A/B.)"""
+    import dmtz_gb300 as dm
+    from dmtz_gb300 import learned
+
+    rel = 1e-4
+    traces = [learned.make_trace(gpu_ctx, *learned.trace_fields((64, 64, 64), 3000 + i, rel), rel) for i in range(24)]
+    traces = [t for t in traces if t is not None]
+    trained = dm.Network(0, seed=0)
+    learned.train(trained, traces, epochs=10, lr=1e-3)
+    del traces
+    untrained = dm.Network(0, seed=0)
+    dims = (96, 96, 96)
+    f, g = learned.trace_fields(dims, 77, rel)
+    f, g = f.reshape(-1), g.reshape(-1)
+    fixed, rep = gpu_ctx.correct(f, g, rel, dims=dims, use_graph=1)
+    assert rep["converged"]
+    edited = fixed < g
+    res = {}
+    for name, n in (("trained", trained), ("untrained", untrained)):
+        prop, active = _proposal(gpu_ctx, n, f, g, dims, rel)
+        res[name] = (int(prop.sum()), float((prop & edited).sum() / max(prop.sum(), 1)))
+    base = float((edited & active).sum() / active.sum())
+    trained.close()
+    untrained.close()
+    n_tr, prec_tr = res["trained"]
+    assert n_tr > 0
+    assert prec_tr > 2 * base and prec_tr > res["untrained"][1], (res, base)
