@@ -126,6 +126,7 @@ def load_library(build_if_missing: bool = True):
     L.dmtz_cnn_backward.argtypes = [_vp, _int, _int, _int, _vp, _vp, ctypes.POINTER(ctypes.c_double)]
     L.dmtz_cnn_step.argtypes = [_vp, ctypes.c_float]
     L.dmtz_cnn_set_min_drop.argtypes = [_vp, ctypes.c_float]
+    L.dmtz_cnn_set_tensor_path.argtypes = [_vp, _int]
     L.dmtz_cnn_set_min_drop.restype = _int
     L.dmtz_cnn_profile.argtypes = [_vp, _int, _int, _int, _vp, _vp, _vp, _vp, _int, _f64p]
     L.dmtz_cnn_profile.restype = _int
@@ -492,6 +493,10 @@ class Network:
         loss = ctypes.c_double()
         self._check(self._L.dmtz_cnn_backward(self._h, *dims, _vp(target_ptr), _vp(active_ptr), ctypes.byref(loss)))
         return loss.value
+
+    def set_tensor_path(self, path: int):
+        """1: convolutions on tcgen05 (default); 0: on mma.sync."""
+        self._check(self._L.dmtz_cnn_set_tensor_path(self._h, int(path)))
 
     def set_min_drop(self, min_drop: float):
         """Apply the proposal only where it lowers g by at least min_drop x bound."""

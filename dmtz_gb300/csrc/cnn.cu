@@ -11,7 +11,10 @@
 // tap = (dz+1)*9 + (dy+1)*3 + (dx+1).
 //
 // Kernels (all persistent: one or two blocks per SM loop over tiles):
-//   k_conv   implicit-GEMM convolution on mma.sync.m16n8k16 (bf16 in, f32
+//   k_conv_tc  the convolutions (forward and data gradient) on tcgen05: a
+//            tile of 128 vertices per MMA chain, accumulator in tensor
+//            memory (the default path; see its comment).
+//   k_conv   the same convolution on mma.sync.m16n8k16 (bf16 in, f32
 //            accumulate).  A block keeps all 27 x out x in weights in shared
 //            memory and streams 8x8x4-vertex tiles (+1 halo) through a
 //            cp.async double buffer; operands reach registers by ldmatrix.
@@ -24,6 +27,8 @@
 //            (deterministic).
 //   k_loss, k_loss_final, k_reduce, k_adam, k_pack: loss, gradient scaling,
 //            Adam, bf16 weight refresh.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -234,6 +239,280 @@ __global__ void __launch_bounds__(256, 1) k_conv(Dims d, const bf16 *__restrict_
         __syncthreads();  // buffer `buf` is refilled two iterations on
     }
     cp_wait<0>();
+}
+
+// ------------------------------------------------- convolution on tcgen05
+// The same convolution (same modes, FLIP, epilogues) on the 5th-generation
+// tensor cores: tcgen05.mma with the accumulator in tensor memory.
+//
+// GEMM per tile: D[128 vertices][COUT] = sum over 27 taps of A_tap[128][CIN] x
+// W_tap[CIN][COUT], K = 16 per instruction.  The tile is 8 x 16 x 1 vertices
+// (x, y, z), so its 128 rows are 16 lines of 8 x-neighbours.  Its halo box
+// (10 x 18 x 3 vertices) sits in shared memory as CIN/8 planes, one per
+// 16-byte group of 8 channels, each plane vertex-major (16 bytes per vertex).
+// In that layout the 8 rows of one x-line and one channel group are 128
+// contiguous bytes: one "core matrix" of the no-swizzle K-major operand
+// layout.  A tap's A operand is the box shifted by the tap's offset: its
+// descriptor starts at the shifted vertex, steps 10 x 16 bytes from one line
+// to the next (stride byte offset) and one plane from one channel group to
+// the next (leading byte offset).  Weights are stored per tap as [group][out
+// channel][8 channels], the same layout for B.  One thread issues the MMAs;
+// completion is signalled by tcgen05.commit on an mbarrier (a bounded wait:
+// on timeout the block reports in *err and leaves); each warp then reads its
+// 32 rows of the accumulator (tcgen05.ld, lane = tile row) for the epilogue.
+// The next tile's box streams in by cp.async while the MMAs run.
+constexpr int QX = 8, QY = 16, QZ = 1;                                  // tile (128 vertices)
+constexpr int GX = QX + 2, GY = QY + 2, GZ = QZ + 2, GVOX = GX * GY * GZ;  // halo box
+inline Dims make_tc_dims(int W, int H, int D) {
+    Dims d{W, H, D, (W + QX - 1) / QX, (H + QY - 1) / QY, (D + QZ - 1) / QZ, 0};
+    d.ntiles = (i64)d.ntx * d.nty * d.ntz;
+    return d;
+}
+__device__ __forceinline__ void tc_tile_origin(const Dims &d, i64 tile, int &x0, int &y0, int &z0) {
+    x0 = (int)(tile % d.ntx) * QX;
+    y0 = (int)((tile / d.ntx) % d.nty) * QY;
+    z0 = (int)(tile / ((i64)d.ntx * d.nty)) * QZ;
+}
+// shared-memory matrix descriptor: no swizzle, start / leading / stride byte
+// offsets in 16-byte units, descriptor version 1 (bit 46)
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+// instruction descriptor of kind::f16: f32 accumulator, bf16 A and B, both
+// K-major, N = COUT, M = 128
+template <int COUT>
+__device__ __forceinline__ uint32_t tc_idesc() {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(COUT >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+}
+__device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.u32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int limit) {
+    uint32_t done = 0;
+    for (int it = 0; it < limit && !done; it++)
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(bar), "r"(parity));
+    return done != 0;
+}
+// this warp's 32 accumulator rows, columns 0..N-1 (N = 16 or 32)
+template <int N>
+__device__ __forceinline__ void tmem_rows(uint32_t taddr, float (&v)[N]) {
+    uint32_t r[N];
+    if constexpr (N == 32) {
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+            "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+              "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]),
+              "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),
+              "=r"(r[30]), "=r"(r[31])
+            : "r"(taddr));
+    } else {
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+            "[%16];\n"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+            : "r"(taddr));
+    }
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n");
+#pragma unroll
+    for (int i = 0; i < N; i++) v[i] = __uint_as_float(r[i]);
+}
+// The halo box arrives by TMA: the activations are a 4-d tensor (channel,
+// x, y, z) with a box of (8 channels, GX, GY, GZ), so one bulk copy per
+// 8-channel group writes exactly one plane (vertex-major, 16 bytes per
+// vertex), zeros outside the grid.  The box starts at channel 8c (16-byte
+// aligned, as a tiled copy's innermost coordinate must be) and at the halo's
+// corner (x0-1, y0-1, z0-1), which may be -1.  Planes are padded to a
+// multiple of 128 bytes (bulk-copy destinations).
+constexpr uint32_t TC_PLANE = ((GVOX * 16 + 127) / 128) * 128;
+template <int CIN>
+__device__ __forceinline__ void tc_issue_box(const CUtensorMap *tm, uint32_t dst, uint32_t bar, int x0, int y0,
+                                             int z0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar),
+                 "r"((uint32_t)(CIN / 8 * GVOX * 16)));
+#pragma unroll
+    for (int c = 0; c < CIN / 8; c++)
+        asm volatile(
+            "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+            "%5}], [%6];\n" ::"r"(dst + c * TC_PLANE),
+            "l"(reinterpret_cast<uint64_t>(tm)), "r"(c * 8), "r"(x0 - 1), "r"(y0 - 1), "r"(z0 - 1), "r"(bar)
+            : "memory");
+}
+
+template <int CIN, int COUT>
+constexpr size_t tc_smem() {
+    return 128 + (size_t)27 * (CIN / 8) * COUT * 16 + 2 * (size_t)(CIN / 8) * TC_PLANE;
+}
+
+template <int CIN, int COUT, int MODE, bool FLIP>
+__global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUtensorMap tmap, Dims d,
+                                                 const bf16 *__restrict__ wt, const float *__restrict__ bias,
+                                                 void *out, const bf16 *__restrict__ aux, int *err) {
+    constexpr int KCH = CIN / 8;
+    constexpr uint32_t PLANE = TC_PLANE, WTAP = KCH * COUT * 16, WBYTES = 27 * WTAP, XBYTES = KCH * PLANE;
+    static_assert(CIN % 16 == 0 && (COUT == 16 || COUT == 32), "tile shapes");
+    static_assert(WTAP % 128 == 0, "planes stay 128-byte aligned");
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ uint32_t tmem_slot;
+    __shared__ __align__(8) uint64_t mbar_mma[2], mbar_box[2];
+    unsigned char *ws = smem_raw + ((128 - (smem_addr(smem_raw) & 127)) & 127);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    for (int i = tid; i < 27 * COUT * KCH; i += blockDim.x) {
+        const int tap = i / (COUT * KCH), rem = i - tap * (COUT * KCH), n = rem / KCH, c = rem - n * KCH;
+        cp16(ws + tap * WTAP + c * COUT * 16 + n * 16, wt + ((i64)tap * COUT + n) * CIN + c * 8, 16);
+    }
+    cp_commit();
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;\n" ::"r"(
+            smem_addr(&tmem_slot)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    const uint32_t mbars[2] = {smem_addr(&mbar_mma[0]), smem_addr(&mbar_mma[1])},
+                   bbar[2] = {smem_addr(&mbar_box[0]), smem_addr(&mbar_box[1])};
+    const uint32_t wbase = smem_addr(ws), xbase0 = wbase + WBYTES;
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mbars[0]));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mbars[1]));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bbar[0]));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bbar[1]));
+        asm volatile("fence.mbarrier_init.release.cluster;\n");
+    }
+    cp_wait<0>();
+    asm volatile("fence.proxy.async.shared::cta;\n");  // the weights, for the tensor core
+    asm volatile("tcgen05.fence::before_thread_sync;\n");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n");
+    const uint32_t tmem = tmem_slot, taddr = tmem + ((uint32_t)(warp * 32) << 16);
+    const uint32_t idesc = tc_idesc<COUT>();
+    const uint32_t bar = mbars[0];
+
+    i64 tile = blockIdx.x;
+    int it = 0;
+    bool box_pending = false, mma_pending = false, failed = false;
+    uint32_t pending_bar = 0, pending_par = 0, cur_bar = 0, cur_par = 0;
+    if (tid == 0 && tile < d.ntiles) {
+        int x0, y0, z0;
+        tc_tile_origin(d, tile, x0, y0, z0);
+        tc_issue_box<CIN>(&tmap, xbase0, bbar[0], x0, y0, z0);
+    }
+    for (; tile < d.ntiles; tile += gridDim.x, it++) {
+        const int buf = it & 1;
+        const uint32_t bpar = (uint32_t)(it >> 1) & 1u, mpar = (uint32_t)it & 1u;
+        bool ok = true;
+        if (tid == 0) {
+            const i64 next = tile + gridDim.x;
+            if (next < d.ntiles) {  // the other buffer's MMAs finished last iteration
+                int x0, y0, z0;
+                tc_tile_origin(d, next, x0, y0, z0);
+                tc_issue_box<CIN>(&tmap, xbase0 + (buf ^ 1) * XBYTES, bbar[buf ^ 1], x0, y0, z0);
+                box_pending = true;
+                pending_bar = bbar[buf ^ 1];
+                pending_par = (uint32_t)((it + 1) >> 1) & 1u;
+            } else {
+                box_pending = false;
+            }
+            ok = mbar_wait(bbar[buf], bpar, 1 << 24);
+            if (!ok) {  // this box too is still in flight
+                cur_bar = bbar[buf];
+                cur_par = bpar;
+            }
+            if (ok) {
+                // descriptors of every (tap, channel group) differ from the
+                // buffer's and the weights' base descriptors only in the
+                // start-address field (shared addresses stay below 2^18, so
+                // adding the offset in 16-byte units never carries out of it):
+                // the unrolled chain adds immediates
+                const uint64_t a0 = smem_desc(xbase0 + buf * XBYTES, PLANE, GX * 16);
+                const uint64_t b0 = smem_desc(wbase, COUT * 16, 128);
+#pragma unroll
+                for (int tap = 0; tap < 27; tap++) {
+                    // offset + 1 along each axis (FLIP mirrors the tap: -d + 1 = 2 - (d + 1))
+                    const int sx = FLIP ? 2 - tap % 3 : tap % 3, sy = FLIP ? 2 - (tap / 3) % 3 : (tap / 3) % 3,
+                              sz = FLIP ? 2 - tap / 9 : tap / 9;
+                    const uint32_t shift = (uint32_t)((sz * GY + sy) * GX + sx) * 16u;
+#pragma unroll
+                    for (int kk = 0; kk < KCH / 2; kk++)
+                        tc_mma(tmem, a0 + ((shift + kk * 2 * PLANE) >> 4), b0 + ((tap * WTAP + kk * 2 * COUT * 16) >> 4),
+                               idesc, (tap | kk) != 0);
+                }
+                asm volatile(
+                    "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar));
+            }
+        }
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            break;
+        }
+        mma_pending = true;
+        ok = mbar_wait(bar, mpar, 1 << 24);
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            break;
+        }
+        mma_pending = false;
+        asm volatile("tcgen05.fence::after_thread_sync;\n");
+        float acc[COUT];
+        tmem_rows<COUT>(taddr, acc);
+        int x0, y0, z0;
+        tc_tile_origin(d, tile, x0, y0, z0);
+        const int r = warp * 32 + lane, gx = x0 + (r & 7), gy = y0 + (r >> 3), gz = z0;
+        if (gx < d.W && gy < d.H && gz < d.D) {
+            const i64 v = gx + (i64)gy * d.W + (i64)gz * d.W * d.H;
+            if constexpr (MODE == 1) {
+                reinterpret_cast<float *>(out)[v] = acc[0] + bias[0];
+            } else {
+                uint4 *o = reinterpret_cast<uint4 *>(reinterpret_cast<bf16 *>(out) + v * COUT);
+                const uint4 *ax = MODE == 2 ? reinterpret_cast<const uint4 *>(aux + v * COUT) : nullptr;
+#pragma unroll
+                for (int q = 0; q < COUT / 8; q++) {
+                    uint4 mk = make_uint4(0, 0, 0, 0);
+                    if constexpr (MODE == 2) mk = ax[q];
+                    const bf16 *mb = reinterpret_cast<const bf16 *>(&mk);
+                    uint4 pk;
+                    __nv_bfloat162 *p2 = reinterpret_cast<__nv_bfloat162 *>(&pk);
+#pragma unroll
+                    for (int h = 0; h < 4; h++) {
+                        const int ch = q * 8 + 2 * h;
+                        float v0 = acc[ch], v1 = acc[ch + 1];
+                        if constexpr (MODE == 0) {
+                            v0 = fmaxf(v0 + bias[ch], 0.f);
+                            v1 = fmaxf(v1 + bias[ch + 1], 0.f);
+                        } else {
+                            if (!(__bfloat162float(mb[2 * h]) > 0.f)) v0 = 0.f;
+                            if (!(__bfloat162float(mb[2 * h + 1]) > 0.f)) v1 = 0.f;
+                        }
+                        p2[h] = __floats2bfloat162_rn(v0, v1);
+                    }
+                    o[q] = pk;
+                }
+            }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;\n");
+        __syncthreads();  // accumulator read before the next tile's MMAs overwrite it
+        asm volatile("tcgen05.fence::after_thread_sync;\n");
+    }
+    if (failed) {
+        // report, then give the copies and MMAs in flight one more bounded
+        // wait before the accumulator is released
+        if (tid == 0) {
+            atomicOr(err, 1);
+            if (box_pending) mbar_wait(pending_bar, pending_par, 1 << 24);
+            if (cur_bar) mbar_wait(cur_bar, cur_par, 1 << 24);
+        }
+        if (mma_pending) mbar_wait(bar, (uint32_t)it & 1u, 1 << 24);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;\n" ::"r"(tmem));
 }
 
 // ------------------------------------------------------------ weight gradient
@@ -461,6 +740,9 @@ struct dmtz_cnn {
     int lastW = 0, lastH = 0, lastD = 0, last_train = 0;
     const bf16 *last_feat = nullptr;
     const float *last_out = nullptr;
+    // convolutions on tcgen05 (1, the default) or on mma.sync (0)
+    int tensor_path = 1;
+    int *tc_err = nullptr;  // set by a tcgen05 convolution whose wait timed out
     // warm-start scratch
     i64 capS = 0;
     bf16 *feat = nullptr;
@@ -526,9 +808,42 @@ dmtz_status launch_persistent(dmtz_cnn *net, K kernel, int threads, size_t smem,
     return DMTZ_OK;
 }
 
+// tensor map of a channels-last bf16 activation tensor for the TMA box of
+// k_conv_tc (the driver's encoder, looked up once through the runtime)
+dmtz_status box_map(dmtz_cnn *net, CUtensorMap *tm, const bf16 *act, int C, int W, int H, int D) {
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        cudaDriverEntryPointQueryResult q;
+        void *fn = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !fn)
+            return nfail(net, DMTZ_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+        encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+    const cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)D};
+    const cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)C * 2 * W, (cuuint64_t)C * 2 * W * H};
+    const cuuint32_t box[4] = {8, GX, GY, GZ}, estr[4] = {1, 1, 1, 1};
+    const CUresult r = encode(tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16 *>(act), dims, strides, box,
+                              estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return nfail(net, DMTZ_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+    return DMTZ_OK;
+}
+
 template <int CIN, int COUT, int MODE, bool FLIP>
 dmtz_status conv(dmtz_cnn *net, const Dims &d, const bf16 *in, const bf16 *w, const float *bias, void *out,
                  const bf16 *aux, cudaStream_t st) {
+    if (net->tensor_path) {
+        Dims dt = make_tc_dims(d.W, d.H, d.D);
+        CUtensorMap tm;
+        dmtz_status s = box_map(net, &tm, in, CIN, d.W, d.H, d.D);
+        if (s != DMTZ_OK) return s;
+        int *err = net->tc_err;
+        void *args[] = {&tm, &dt, &w, &bias, &out, &aux, &err};
+        return launch_persistent(net, k_conv_tc<CIN, COUT, MODE, FLIP>, 128, tc_smem<CIN, COUT>(), dt.ntiles, 0,
+                                 nullptr, st, args);
+    }
     Dims dd = d;
     void *args[] = {&dd, &in, &w, &bias, &out, &aux};
     return launch_persistent(net, k_conv<CIN, COUT, MODE, FLIP>, 256, conv_smem<CIN, COUT, MODE, FLIP>(), d.ntiles, 0,
@@ -679,8 +994,9 @@ dmtz_status dmtz_cnn_create(dmtz_cnn **out, int device, uint64_t seed) {
     if (nalloc(&net->w, kParams) || nalloc(&net->grad, kParams) || nalloc(&net->m1, kParams) ||
         nalloc(&net->m2, kParams) || nalloc(&net->wf, kWeights) || nalloc(&net->wt, kWeights) ||
         nalloc(&net->part, (i64)net->part_blocks * largest) || nalloc(&net->lpart, 2 * kLossBlocks) ||
-        nalloc(&net->lres, 2) || nalloc(&net->scale, 1))
+        nalloc(&net->lres, 2) || nalloc(&net->scale, 1) || nalloc(&net->tc_err, 1))
         return bail(DMTZ_ERR_CUDA);
+    if (cudaMemset(net->tc_err, 0, sizeof(int)) != cudaSuccess) return bail(DMTZ_ERR_CUDA);
     // He-uniform weights (bound sqrt(6 / fan_in)); the output layer 0.1x and
     // only its channel 0 nonzero; zero biases
     std::vector<float> h((size_t)kParams, 0.f);
@@ -708,7 +1024,7 @@ void dmtz_cnn_destroy(dmtz_cnn *net) {
     for (void *p : {(void *)net->w, (void *)net->grad, (void *)net->m1, (void *)net->m2, (void *)net->wf,
                     (void *)net->wt, (void *)net->part, (void *)net->lpart, (void *)net->lres, (void *)net->scale,
                     (void *)net->a[0], (void *)net->a[1], (void *)net->dz4, (void *)net->gA, (void *)net->gB,
-                    (void *)net->feat, (void *)net->active, (void *)net->out})
+                    (void *)net->feat, (void *)net->active, (void *)net->out, (void *)net->tc_err})
         cudaFree(p);
     if (net->cap_train) cudaFree(net->a[2]);
     if (net->stream) cudaStreamDestroy(net->stream);
@@ -754,12 +1070,30 @@ dmtz_status dmtz_cnn_get_grads(dmtz_cnn *net, float *host) {
     return DMTZ_OK;
 }
 
+// a tcgen05 convolution whose completion wait timed out leaves a flag (the
+// kernel itself returns); the synchronous calls report it
+static dmtz_status check_tc(dmtz_cnn *net) {
+    int e = 0;
+    NCK(cudaMemcpy(&e, net->tc_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) {
+        NCK(cudaMemset(net->tc_err, 0, sizeof(int)));
+        return nfail(net, DMTZ_ERR_CUDA, "a tensor-core convolution timed out waiting for its MMAs");
+    }
+    return DMTZ_OK;
+}
+
+dmtz_status dmtz_cnn_set_tensor_path(dmtz_cnn *net, int path) {
+    if (!net || (path != 0 && path != 1)) return DMTZ_ERR_ARG;
+    net->tensor_path = path;
+    return DMTZ_OK;
+}
+
 dmtz_status dmtz_cnn_forward(dmtz_cnn *net, int W, int H, int D, const void *feat, float *out, int train) {
     if (!net) return DMTZ_ERR_ARG;
     dmtz_status s = forward_on(net, W, H, D, static_cast<const bf16 *>(feat), out, train, net->stream);
     if (s != DMTZ_OK) return s;
     NCK(cudaStreamSynchronize(net->stream));
-    return DMTZ_OK;
+    return check_tc(net);
 }
 
 dmtz_status dmtz_cnn_backward(dmtz_cnn *net, int W, int H, int D, const float *target, const uint8_t *active,
@@ -793,7 +1127,7 @@ dmtz_status dmtz_cnn_backward(dmtz_cnn *net, int W, int H, int D, const float *t
     NCK(cudaMemcpyAsync(res, net->lres, sizeof(res), cudaMemcpyDeviceToHost, st));
     NCK(cudaStreamSynchronize(st));
     if (loss) *loss = res[0];
-    return DMTZ_OK;
+    return check_tc(net);
 }
 
 dmtz_status dmtz_cnn_step(dmtz_cnn *net, float lr) {

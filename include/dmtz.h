@@ -327,6 +327,11 @@ dmtz_status dmtz_cnn_forward(dmtz_cnn *net, int W, int H, int D, const void *fea
  * buffer */
 dmtz_status dmtz_cnn_backward(dmtz_cnn *net, int W, int H, int D, const float *target, const uint8_t *active,
                               double *loss);
+/* Tensor-core path of the convolutions (no counterpart in the reference):
+ * 1 (the default) = tcgen05.mma with the accumulators in tensor memory,
+ * 0 = the warp-level mma.sync kernels.  Same arithmetic (bf16 products, f32
+ * sums); results differ only in the order of the f32 sums. */
+dmtz_status dmtz_cnn_set_tensor_path(dmtz_cnn *net, int path);
 /* proposal threshold in units of the bound, 0..2 */
 dmtz_status dmtz_cnn_set_min_drop(dmtz_cnn *net, float min_drop);
 /* one Adam step (beta 0.9 / 0.999, eps 1e-8) with learning rate lr */

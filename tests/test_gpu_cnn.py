@@ -55,8 +55,19 @@ def _rel(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
 
 
-@pytest.mark.parametrize("dims", [(8, 8, 4), (13, 11, 9), (21, 6, 5)])
-def test_forward_matches_reference(net, dims):
+PATHS = pytest.mark.parametrize("path", [1, 0], ids=["tcgen05", "mma_sync"])
+
+
+@pytest.fixture
+def tensor_path(net, path):
+    net.set_tensor_path(path)
+    yield path
+    net.set_tensor_path(1)
+
+
+@PATHS
+@pytest.mark.parametrize("dims", [(8, 8, 4), (13, 11, 9), (21, 6, 5), (40, 35, 3)])
+def test_forward_matches_reference(net, tensor_path, dims):
     W, H, D = dims
     p = _params(1)
     net.set_params(p)
@@ -73,8 +84,9 @@ def test_forward_matches_reference(net, dims):
     assert _rel(got, ref64) < 3e-2
 
 
+@PATHS
 @pytest.mark.parametrize("dims,weighted", [((13, 11, 9), False), ((16, 16, 8), False), ((13, 11, 9), True)])
-def test_backward_matches_reference(net, dims, weighted):
+def test_backward_matches_reference(net, tensor_path, dims, weighted):
     W, H, D = dims
     V = W * H * D
     p = _params(3)
@@ -313,3 +325,21 @@ def test_trained_network_finds_the_loops_edits(gpu_ctx):
     n_tr, prec_tr = res["trained"]
     assert n_tr > 0
     assert prec_tr > 2 * base and prec_tr > res["untrained"][1], (res, base)
+
+
+def test_tensor_paths_agree(net):
+    """tcgen05 and mma.sync convolutions: the same bf16 products and f32 sums,
+    only in another order, on a grid of many tiles (128^2 x 24)."""
+    dims = (128, 128, 24)
+    W, H, D = dims
+    net.set_params(_params(9))
+    _, feat_d = _feat(10, dims)
+    outs = []
+    for path in (1, 0):
+        net.set_tensor_path(path)
+        out = torch.empty(W * H * D, dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        net.forward(feat_d.data_ptr(), out.data_ptr(), dims)
+        outs.append(out.cpu().numpy().astype(np.float64))
+    net.set_tensor_path(1)
+    assert _rel(outs[0], outs[1]) < 1e-2
