@@ -658,6 +658,23 @@ def run_big(args):
     ctx.close()
 
 
+def run_batch_field(args):
+    """One field of the uneven batch (host-driven loop, so that every kernel
+    is its own launch for profilers): device time, rounds and phase times."""
+    import dmtz_gb300 as dm
+    from dmtz_gb300 import synth
+
+    f, g, rel = synth.batch_workload(64)[args.batch_field]
+    D, H, W = f.shape
+    ctx = dm.Context(0)
+    out, rep = ctx.correct(f.astype(np.float64), g.astype(np.float64), rel, dims=(W, H, D), max_rounds=args.max_rounds,
+                           use_graph=0)
+    print(json.dumps({"workload": f"batch field {args.batch_field}: {W}x{H}x{D} {f.dtype}, eps {rel} x range",
+                      **{k: rep[k] for k in ("seconds", "cp_rounds", "path_rounds", "stall_breaks", "kernel_launches",
+                                             "phase_ms", "converged")}}), flush=True)
+    ctx.close()
+
+
 def sweep_only(size: int):
     """Gradient sweep kernels alone (for kernel profilers): 3 timed sweeps."""
     import torch
@@ -727,12 +744,17 @@ def main():
     ap.add_argument("--save-params", default="", help="learned workload: write the trained parameters (.npy)")
     ap.add_argument("--min-drop", type=float, nargs="+", default=[0.25, 0.5, 1.0],
                     help="learned workload: proposal thresholds (x bound) to evaluate")
+    ap.add_argument("--batch-field", type=int, default=-1, metavar="I",
+                    help="profiling aid: correct field I of the uneven batch alone (host-driven loop)")
     ap.add_argument("--dist-check", action="store_true", help=argparse.SUPPRESS)
     args = ap.parse_args()
     if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
         sys.exit(spawn_ranks(args.gpus, sys.argv[1:]))
     if args.dist_check:
         dist_check(args, int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)))
+        return
+    if args.batch_field >= 0:
+        run_batch_field(args)
         return
     if args.workload == "batch":
         run_batch(args)
