@@ -261,7 +261,7 @@ __global__ void __launch_bounds__(256, 1) k_conv(Dims d, const bf16 *__restrict_
 // on timeout the block reports in *err and leaves); each warp then reads its
 // 32 rows of the accumulator (tcgen05.ld, lane = tile row) for the epilogue.
 // The next tile's box streams in by cp.async while the MMAs run.
-constexpr int QX = 8, QY = 16, QZ = 1;                                  // tile (128 vertices)
+constexpr int QX = 8, QY = 16, QZ = 4;  // tile: QZ slices of 128 vertices (one MMA chain each)
 constexpr int GX = QX + 2, GY = QY + 2, GZ = QZ + 2, GVOX = GX * GY * GZ;  // halo box
 inline Dims make_tc_dims(int W, int H, int D) {
     Dims d{W, H, D, (W + QX - 1) / QX, (H + QY - 1) / QY, (D + QZ - 1) / QZ, 0};
@@ -372,7 +372,7 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUte
     }
     cp_commit();
     if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;\n" ::"r"(
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;\n" ::"r"(
             smem_addr(&tmem_slot)));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
     }
@@ -433,6 +433,10 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUte
                 // the unrolled chain adds immediates
                 const uint64_t a0 = smem_desc(xbase0 + buf * XBYTES, PLANE, GX * 16);
                 const uint64_t b0 = smem_desc(wbase, COUT * 16, 128);
+                // the QZ slices' chains are interleaved: consecutive MMAs go
+                // to different accumulators, so one MMA's accumulation does
+                // not wait for the previous one (a single chain of these
+                // small N = COUT products kept the tensor pipe 15 % busy)
 #pragma unroll
                 for (int tap = 0; tap < 27; tap++) {
                     // offset + 1 along each axis (FLIP mirrors the tap: -d + 1 = 2 - (d + 1))
@@ -441,8 +445,10 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUte
                     const uint32_t shift = (uint32_t)((sz * GY + sy) * GX + sx) * 16u;
 #pragma unroll
                     for (int kk = 0; kk < KCH / 2; kk++)
-                        tc_mma(tmem, a0 + ((shift + kk * 2 * PLANE) >> 4), b0 + ((tap * WTAP + kk * 2 * COUT * 16) >> 4),
-                               idesc, (tap | kk) != 0);
+#pragma unroll
+                        for (int q = 0; q < QZ; q++)
+                            tc_mma(tmem + (uint32_t)(q * 32), a0 + ((shift + q * GY * GX * 16 + kk * 2 * PLANE) >> 4),
+                                   b0 + ((tap * WTAP + kk * 2 * COUT * 16) >> 4), idesc, (tap | kk) != 0);
                 }
                 asm volatile(
                     "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar));
@@ -460,11 +466,13 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUte
         }
         mma_pending = false;
         asm volatile("tcgen05.fence::after_thread_sync;\n");
-        float acc[COUT];
-        tmem_rows<COUT>(taddr, acc);
         int x0, y0, z0;
         tc_tile_origin(d, tile, x0, y0, z0);
-        const int r = warp * 32 + lane, gx = x0 + (r & 7), gy = y0 + (r >> 3), gz = z0;
+#pragma unroll 1
+        for (int zq = 0; zq < QZ; zq++) {  // slice zq of the tile: accumulator columns 32 zq ..
+        float acc[COUT];
+        tmem_rows<COUT>(taddr + (uint32_t)(zq * 32), acc);
+        const int r = warp * 32 + lane, gx = x0 + (r & 7), gy = y0 + (r >> 3), gz = z0 + zq;
         if (gx < d.W && gy < d.H && gz < d.D) {
             const i64 v = gx + (i64)gy * d.W + (i64)gz * d.W * d.H;
             if constexpr (MODE == 1) {
@@ -496,6 +504,7 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUte
                 }
             }
         }
+        }
         asm volatile("tcgen05.fence::before_thread_sync;\n");
         __syncthreads();  // accumulator read before the next tile's MMAs overwrite it
         asm volatile("tcgen05.fence::after_thread_sync;\n");
@@ -512,7 +521,7 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUte
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n");
     __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;\n" ::"r"(tmem));
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;\n" ::"r"(tmem));
 }
 
 // ------------------------------------------------------------ weight gradient
