@@ -433,7 +433,11 @@ def run_ours(args, rank, world, local_rank):
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                              "kernel": "gradient sweep (5 pairing passes + criticality)",
-                             "sweep_ms": ms[6], "per_kernel_ms": [round(x, 4) for x in ms[:6]]},
+                             "sweep_ms": ms[6], "per_kernel_ms": [round(x, 4) for x in ms[:6]],
+                             "step": {"definition": "the whole correction's least traffic: read f and g, "
+                                                    "write the corrected g, 24 B/vertex, per step time",
+                                      "achieved": 24.0 * V / t_step / 1e9,
+                                      "frac": 24.0 * V / t_step / 1e9 / peak}},
                 "clocks": clk, "gpu_launches": launches,
                 "separatrix_agreement": {
                     "descending": agree["desc_equal"] / max(agree["desc_compared"], 1),
