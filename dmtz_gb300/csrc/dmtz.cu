@@ -1774,6 +1774,8 @@ BrickList all_bricks(const Grid &g, int shape, i64 &nb) {
     bl.n = nullptr;
     bl.shape = shape;
     nb = bricks_of(g, shape, bl.nbx, bl.nby, bl.nbz);
+    bl.dbx = make_fdiv((unsigned long long)bl.nbx);
+    bl.dby = make_fdiv((unsigned long long)bl.nby);
     return bl;
 }
 
@@ -1831,6 +1833,8 @@ void repair_dirty(dmtz_ctx *ctx, const Grid &g, const FieldState &s, const uint3
         bl[p].list = ctx->brick_list + (i64)(radius[p] - 1) * ctx->capB;
         bl[p].n = ctx->brick_n + (radius[p] - 1);
         bl[p].nbx = nbx; bl[p].nby = nby; bl[p].nbz = nbz;
+        bl[p].dbx = make_fdiv((unsigned long long)nbx);
+        bl[p].dby = make_fdiv((unsigned long long)nby);
         bl[p].shape = shape;
     }
     sweep_passes(ctx, g, s, bl, nb);

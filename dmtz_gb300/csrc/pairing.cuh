@@ -344,6 +344,7 @@ struct BrickList {
     const unsigned long long *n;    // number of listed bricks (device), when list != nullptr
     int nbx, nby, nbz;              // bricks per axis
     int shape;                      // brick shape index (DMTZ_SHAPES)
+    FDiv dbx, dby;                  // division by nbx and nby (brick index -> coordinates)
 };
 // brick shapes (anchors per brick along x, y, z); each is one 128-thread block
 #define DMTZ_NSHAPES 3
@@ -358,11 +359,11 @@ __device__ __forceinline__ void brick_coords(const BrickList &bl, i64 b, int &bx
         bx = e & 0x7FF;
         by = (e >> 11) & 0x7FF;
         bz = e >> 22;
-    } else {
-        const int bi = (int)b;
-        bx = bi % bl.nbx;
-        by = (bi / bl.nbx) % bl.nby;
-        bz = bi / (bl.nbx * bl.nby);
+    } else {  // every thread of the block decodes the same index: multiply-high, not division
+        const unsigned long long u = (unsigned long long)b, q = fdiv(bl.dbx, u), r = fdiv(bl.dby, q);
+        bx = (int)(u - q * (unsigned long long)bl.nbx);
+        by = (int)(q - r * (unsigned long long)bl.nby);
+        bz = (int)r;
     }
 }
 
