@@ -475,11 +475,45 @@ __global__ void __launch_bounds__(DMTZ_BRICK, DMTZ_SWEEP_MINB) k_sweep_sm(Grid g
     const int lx = threadIdx.x % SX, ly = (threadIdx.x / SX) % SY, lz = threadIdx.x / (SX * SY);
     const int li = (lx + 1) + BX * ((ly + 1) + BY * (lz + 1));  // this thread's anchor in the box
     const i64 nbr = brick_count(bl);
+    // The box entries a thread stages are the same for every brick: their
+    // offsets from the box corner (32-bit grids) are computed once.  A brick
+    // whose box lies inside the grid (almost all of them) stages without
+    // bounds tests, by 32-bit offsets from its corner, and all its anchors
+    // take the fast path.
+    constexpr int NE = (NB + DMTZ_BRICK - 1) / DMTZ_BRICK;
+    int eoff[NE];
+#pragma unroll
+    for (int k = 0; k < NE; k++) {
+        const int e = threadIdx.x + k * DMTZ_BRICK;
+        eoff[k] = e % BX + ((e / BX) % BY) * g.W + (e / (BX * BY)) * g.WHi;
+    }
     for (i64 b = blockIdx.x; b < nbr; b += gridDim.x) {
         int bx, by, bz;
         brick_coords(bl, b, bx, by, bz);
         const int x0 = bx * SX, y0 = by * SY, z0 = bz * SZ;
+        const bool boxin = g.small && x0 >= 1 && y0 >= 1 && z0 >= 1 && x0 + SX < g.W && y0 + SY < g.H && z0 + SZ < g.D;
+        const int corner = boxin ? (x0 - 1) + (y0 - 1) * g.W + (z0 - 1) * g.WHi : 0;
         __syncthreads();  // the previous brick's readers are done
+        if (boxin) {
+#pragma unroll
+            for (int k = 0; k < NE; k++) {
+                const int e = threadIdx.x + k * DMTZ_BRICK;
+                if (k + 1 < NE || e < NB) {
+                    const unsigned u = (unsigned)(corner + eoff[k]);
+                    if (VAL) sh_key[e] = okey(s.val[u]);
+                    if (PASS >= 1 && PASS <= 4) {
+                        sh_low[e] = s.low[u];
+                        sh_key[e] = s.key[u];
+                    }
+                    if (PASS == 1 || PASS == 3 || PASS == 5) sh_pv[e] = s.pv[u];
+                    if (PASS == 2 || PASS == 3) sh_a[e] = s.ea2[u];
+                    if (PASS == 4 || PASS == 5) sh_a[e] = s.eup[u];
+                    if (PASS == 3 || PASS == 4) sh_c[e] = s.fp3[u];
+                    if (PASS == 4) sh_b[e] = s.fa3[u];
+                    if (PASS == 5) sh_b[e] = s.fup[u];
+                }
+            }
+        } else
         for (int e = threadIdx.x; e < NB; e += DMTZ_BRICK) {
             const int ux = x0 - 1 + e % BX, uy = y0 - 1 + (e / BX) % BY, uz = z0 - 1 + e / (BX * BY);
             const bool in = ux >= 0 && uy >= 0 && uz >= 0 && ux < g.W && uy < g.H && uz < g.D;
@@ -498,9 +532,11 @@ __global__ void __launch_bounds__(DMTZ_BRICK, DMTZ_SWEEP_MINB) k_sweep_sm(Grid g
         }
         __syncthreads();
         const int x = x0 + lx, y = y0 + ly, z = z0 + lz;
-        const bool ingrid = x < g.W && y < g.H && z < g.D;
-        const bool inner = ingrid && x >= 1 && y >= 1 && z >= 1 && x <= g.W - 2 && y <= g.H - 2 && z <= g.D - 2;
-        const i64 v = x + (i64)y * g.W + (i64)z * g.WH;
+        const bool ingrid = boxin || (x < g.W && y < g.H && z < g.D);
+        const bool inner =
+            boxin || (ingrid && x >= 1 && y >= 1 && z >= 1 && x <= g.W - 2 && y <= g.H - 2 && z <= g.D - 2);
+        const i64 v = boxin ? (i64)(unsigned)(corner + (lx + 1) + (ly + 1) * g.W + (lz + 1) * g.WHi)
+                            : x + (i64)y * g.W + (i64)z * g.WH;
         if (inner) {
             if (PASS == 0) {
                 fast_vertex(gb, t, li);
