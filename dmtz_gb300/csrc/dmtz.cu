@@ -826,16 +826,17 @@ static_assert(cxt::TOPO_FACE_NCOF[0] == 2 && cxt::TOPO_FACE_NCOF[5] == 2 && cxt:
 // those sit at anchors inside the box of tiles the walk recorded.  A walk
 // whose box holds no tile re-paired since the last detection keeps its
 // result and is not walked again.
+// Walks are handed out in chunks of kWalkChunk by a ticket (*ticket, zero at
+// launch): a warp's idle lanes take the next walks of its chunk, then of the
+// next free chunk of the whole list, so warps that meet long walks do not hold
+// the kernel's end while others sit idle (one atomic per chunk, not per refill).
 __global__ void k_path_as_walk(Grid g, const i64 *sad2, const unsigned long long *nsad, const uint32_t *tcP,
                                const uint32_t *tcQ, const uint8_t *succ, i64 *res, i64 cap, int *err,
-                               unsigned long long *wbox, TileSat T) {
+                               unsigned long long *wbox, TileSat T, unsigned long long *ticket) {
+    constexpr i64 kWalkChunk = 64;
     const i64 n = 2 * (i64)*nsad;
     const unsigned full = 0xffffffffu, lane = threadIdx.x & 31u;
-    const i64 nwarps = ((i64)gridDim.x * blockDim.x) >> 5;
-    const i64 warp = ((i64)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const i64 chunk = (n + nwarps - 1) / nwarps;
-    i64 pos = warp * chunk;                      // next walk of this warp's range (same in every lane)
-    const i64 end = min(n, pos + chunk);
+    i64 pos = 0, end = 0;  // the warp's current chunk (the same in every lane)
     i64 item = -1, steps = 0;
     int x = 0, y = 0, z = 0, s = 0;
     int bx0 = 0, bx1 = 0, by0 = 0, by1 = 0, bz0 = 0, bz1 = 0;  // tile box of the current walk
@@ -843,9 +844,17 @@ __global__ void k_path_as_walk(Grid g, const i64 *sad2, const unsigned long long
     while (true) {
         const unsigned want = __ballot_sync(full, item < 0 && !drained);
         if (want) {
+            if (pos >= end) {  // the warp's chunk is used up: take the next one
+                unsigned long long b0 = 0;
+                if (lane == 0) b0 = atomicAdd(ticket, (unsigned long long)kWalkChunk);
+                pos = (i64)__shfl_sync(full, b0, 0);
+                end = min(n, pos + kWalkChunk);
+            }
+            const i64 my = pos + __popc(want & ((1u << lane) - 1u));
             if (item < 0 && !drained) {
-                const i64 my = pos + __popc(want & ((1u << lane) - 1u));
-                if (my < end) {
+                if (pos >= n) {
+                    drained = true;  // no walk is left anywhere
+                } else if (my < end) {
                     const unsigned long long b = wbox[my];
                     if (!(b & kBoxKnown) || box_dirty(T, b) != 0u) {
                         item = my;
@@ -868,11 +877,9 @@ __global__ void k_path_as_walk(Grid g, const i64 *sad2, const unsigned long long
                             item = -1;
                         }
                     }
-                } else {
-                    drained = true;
-                }
+                }  // else: past this chunk's end, the next refill takes a new chunk
             }
-            pos += __popc(want);
+            pos = min(pos + (i64)__popc(want), end);
         }
         if (__all_sync(full, item < 0 && drained)) break;
         if (item >= 0) {  // one step of the walk
@@ -2045,8 +2052,10 @@ void launch_detect(dmtz_ctx *ctx, const Grid &g, const RuleCtx &rc, const PathRe
         T.ntx = ntx;
         T.nty = nty;
         T.ntz = ntz;
+        cudaMemsetAsync(ctx->counters + 27, 0, sizeof(unsigned long long), st);  // the walks' ticket
         k_path_as_walk<<<grid, kBlock, 0, st>>>(g, ctx->sad2, ctx->counters + 10, ctx->P.tcode, ctx->Q.tcode,
-                                                ctx->succ, ctx->as_res, g.T + 16, ctx->errword, ctx->walk_box, T);
+                                                ctx->succ, ctx->as_res, g.T + 16, ctx->errword, ctx->walk_box, T,
+                                                ctx->counters + 27);
         k_path_as_pick<<<grid, kBlock, 0, st>>>(g, ctx->sad2, ctx->counters + 10, ctx->as_res, R);
         if (ctx->strict_ds) {  // whole-path descending checks of every 1-saddle, into the records
             k_ds_strict<<<grid, kBlock, 0, st>>>(rc, R, g.V + 16);
