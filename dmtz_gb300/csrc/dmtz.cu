@@ -407,8 +407,12 @@ __global__ void k_path_succ(Grid g, const uint32_t *tcodeP, uint8_t *succ) {
     reinterpret_cast<uint64_t *>(succ)[v] = packed;
 }
 
-// compact list of the original 2-saddle triangles (anchor * 12 + slot)
-__global__ void k_sad2_list(Grid g, const uint32_t *critP, i64 *list, i64 cap, unsigned long long *n) {
+// compact list of original critical cells of one dimension: criticality
+// bits FIRST .. FIRST+SLOTS-1 of an anchor (SLOTS cells per anchor), entry =
+// anchor * SLOTS + slot.  The 2-saddle triangles: <8, 12>; the 1-saddle
+// edges: <1, 7>.
+template <int FIRST, int SLOTS>
+__global__ void k_crit_list(Grid g, const uint32_t *critP, i64 *list, i64 cap, unsigned long long *n) {
     // a block takes kBlock x 8 consecutive anchors per step: each thread
     // counts its 8 anchors' 2-saddles, a block scan places them in anchor
     // order, and one atomic per block step reserves the block's range (one
@@ -424,7 +428,7 @@ __global__ void k_sad2_list(Grid g, const uint32_t *critP, i64 *list, i64 cap, u
         unsigned mine = 0;
 #pragma unroll
         for (int j = 0; j < 8; j++) {
-            m[j] = v0 + j < g.V ? (critP[v0 + j] >> 8) & 0xFFFu : 0u;
+            m[j] = v0 + j < g.V ? (critP[v0 + j] >> FIRST) & ((1u << SLOTS) - 1u) : 0u;
             mine += __popc(m[j]);
         }
         unsigned incl = mine;
@@ -451,7 +455,7 @@ __global__ void k_sad2_list(Grid g, const uint32_t *critP, i64 *list, i64 cap, u
             while (mm) {
                 const int sl = __ffs(mm) - 1;
                 mm &= mm - 1;
-                if ((i64)at < cap) list[at] = (v0 + j) * 12 + sl;
+                if ((i64)at < cap) list[at] = (v0 + j) * SLOTS + sl;
                 at++;
             }
         }
@@ -1043,44 +1047,80 @@ __device__ __forceinline__ i64 dir_offset(const Grid &g, int d) {
         if (d == i) o = g.doff[i];
     return o;
 }
-__global__ void k_ds_strict(RuleCtx c, PathRec R, i64 step_cap) {
+// Items are the original 1-saddles (the list of k_crit_list<1, 7>); one lane
+// walks one item's first endpoint's path, then, if that is clean, the
+// second's, and idle lanes take new items from chunks of 64 handed out by a
+// ticket (*ticket, zero at launch): walks are long and uneven, and a lane that
+// finished does not wait for the warp's longest walk.
+__global__ void k_ds_strict(RuleCtx c, PathRec R, const i64 *sad1, const unsigned long long *nsad1, i64 step_cap,
+                            unsigned long long *ticket) {
     const Grid &g = c.g;
-    for (i64 v = (i64)blockIdx.x * blockDim.x + threadIdx.x; v < g.V; v += (i64)gridDim.x * blockDim.x) {
-        const uint32_t m = (c.P.crit[v] >> 1) & 0x7Fu;
-        if (!m) continue;
-        int x, y, z;
-        decode_v(g, v, x, y, z);
-        DMTZ_FOR(7, K, {
-            constexpr int k = decltype(K)::value;
-            constexpr int c0 = cxt::TOPO_EDGE_V[k][0], c1 = cxt::TOPO_EDGE_V[k][1];
-            if ((m >> k) & 1u) {
-                const i64 ends[2] = {v + cxt::ccx(c0) + cxt::ccy(c0) * (i64)g.W + cxt::ccz(c0) * g.WH,
-                                     v + cxt::ccx(c1) + cxt::ccy(c1) * (i64)g.W + cxt::ccz(c1) * g.WH};
-                for (int j = 0; j < 2; j++) {
-                    i64 u = ends[j];
-                    bool found = false;
-                    for (i64 step = 0;; step++) {
-                        const int po = c.P.pv[u];
-                        if (po == 15) break;  // an original minimum: the path is clean
-                        if (po != c.Q.pv[u]) {
-                            const unsigned long long at = agg_slot(R.n + 1);
-                            if ((i64)at < R.cap_ds) {
-                                R.ds_edge[at] = edge_ref(g, x, y, z, k);
-                                R.ds_vert[at] = u;
-                            }
-                            found = true;
-                            break;
-                        }
-                        if (step >= step_cap) {  // a cycle: not a gradient
-                            atomicOr(c.err, ERR_WALK);
-                            break;
-                        }
-                        u += dir_offset(g, po);
-                    }
-                    if (found) break;
+    constexpr i64 kChunk = 64;
+    // corners (dx + 2 dy + 4 dz) of edge family k, higher id first: bits 6k .. 6k+5
+    constexpr uint64_t kEnds = []() {
+        uint64_t e = 0;
+        for (int k = 0; k < 7; k++)
+            e |= (uint64_t)(cxt::TOPO_EDGE_V[k][0] | (cxt::TOPO_EDGE_V[k][1] << 3)) << (6 * k);
+        return e;
+    }();
+    const i64 n = min((i64)*nsad1, R.cap_ds);
+    const unsigned full = 0xffffffffu, lane = threadIdx.x & 31u;
+    i64 pos = 0, end = 0, item = -1, steps = 0, u = 0, second = 0, edge = 0;
+    bool first = true, drained = false;
+    while (true) {
+        const unsigned want = __ballot_sync(full, item < 0 && !drained);
+        if (want) {
+            if (pos >= end) {  // the warp's chunk is used up: take the next one
+                unsigned long long b0 = 0;
+                if (lane == 0) b0 = atomicAdd(ticket, (unsigned long long)kChunk);
+                pos = (i64)__shfl_sync(full, b0, 0);
+                end = min(n, pos + kChunk);
+            }
+            const i64 my = pos + __popc(want & ((1u << lane) - 1u));
+            if (item < 0 && !drained) {
+                if (pos >= n) {
+                    drained = true;
+                } else if (my < end) {
+                    const i64 code = sad1[my], a = code / 7;
+                    const int k = (int)(code - 7 * a);
+                    int x, y, z;
+                    decode_v(g, a, x, y, z);
+                    const int ends = (int)((kEnds >> (6 * k)) & 63u), c0 = ends & 7, c1 = ends >> 3;
+                    u = a + (c0 & 1) + ((c0 >> 1) & 1) * (i64)g.W + (c0 >> 2) * g.WH;
+                    second = a + (c1 & 1) + ((c1 >> 1) & 1) * (i64)g.W + (c1 >> 2) * g.WH;
+                    edge = edge_ref(g, x, y, z, k);
+                    item = my;
+                    first = true;
+                    steps = 0;
                 }
             }
-        });
+            pos = min(pos + (i64)__popc(want), end);
+        }
+        if (__all_sync(full, item < 0 && drained)) break;
+        if (item >= 0) {  // one step of the current endpoint's walk
+            const int po = c.P.pv[u];
+            if (po == 15) {  // an original minimum: this endpoint's path is clean
+                if (first) {
+                    first = false;
+                    u = second;
+                    steps = 0;
+                } else {
+                    item = -1;
+                }
+            } else if (po != c.Q.pv[u]) {
+                const unsigned long long at = agg_slot(R.n + 1);
+                if ((i64)at < R.cap_ds) {
+                    R.ds_edge[at] = edge;
+                    R.ds_vert[at] = u;
+                }
+                item = -1;
+            } else if (++steps > step_cap) {  // a cycle: not a gradient
+                atomicOr(c.err, ERR_WALK);
+                item = -1;
+            } else {
+                u += dir_offset(g, po);
+            }
+        }
     }
 }
 
@@ -1518,6 +1558,8 @@ struct dmtz_ctx {
     uint32_t *brick_list = nullptr;   // compacted lists per radius, capB entries each
     unsigned long long *brick_n = nullptr;  // their lengths
     i64 *sad2 = nullptr;      // original 2-saddle triangles
+    i64 *sad1 = nullptr;      // original 1-saddle edges (strict descending checks only)
+    i64 capSad1 = 0;
     i64 *as_res = nullptr;    // per (2-saddle, coface) walk results, 2 x capSad2
     // walk cache: per walk, the box of 16^3-anchor tiles its last walk visited
     // (walk_box); per tile, whether the decompressed gradient was recomputed
@@ -1599,6 +1641,9 @@ void free_all(dmtz_ctx *c) {
     c->capWall = c->capWS = 0;
     cudaFree(c->brick_n);
     c->brick_n = nullptr;
+    cudaFree(c->sad1);
+    c->sad1 = nullptr;
+    c->capSad1 = 0;
     c->succ = nullptr; c->sad2 = nullptr; c->brick_flags = nullptr; c->brick_list = nullptr;
     c->f = c->g = nullptr; c->cnt = nullptr; c->reqbits = nullptr; c->reqlist = nullptr;
     c->as_tet = c->as_cur = c->ds_edge = c->ds_vert = nullptr; c->counters = nullptr;
@@ -2024,7 +2069,22 @@ dmtz_status prep_paths(dmtz_ctx *ctx, const Grid &g) {
     CK(cudaMemsetAsync(ctx->tile_dirty, 0, (size_t)nt, st));
     CK(cudaMemsetAsync(ctx->counters + 10, 0, sizeof(unsigned long long), st));
     k_path_succ<<<grid_for(g.V), kBlock, 0, st>>>(g, ctx->P.tcode, ctx->succ);
-    k_sad2_list<<<persistent_grid(), kBlock, 0, st>>>(g, ctx->P.crit, ctx->sad2, ctx->capSad2, ctx->counters + 10);
+    k_crit_list<8, 12><<<persistent_grid(), kBlock, 0, st>>>(g, ctx->P.crit, ctx->sad2, ctx->capSad2,
+                                                             ctx->counters + 10);
+    if (ctx->strict_ds) {  // the whole-path descending checks walk from the 1-saddle list
+        const i64 need = std::max<i64>((i64)n[0], 1);
+        if (need > ctx->capSad1) {
+            cudaFree(ctx->sad1);
+            ctx->sad1 = nullptr;
+            ctx->capSad1 = 0;
+            CK(dalloc(&ctx->sad1, need));
+            ctx->capSad1 = need;
+        }
+        CK(cudaMemsetAsync(ctx->counters + 28, 0, sizeof(unsigned long long), st));
+        k_crit_list<1, 7><<<persistent_grid(), kBlock, 0, st>>>(g, ctx->P.crit, ctx->sad1, ctx->capSad1,
+                                                                ctx->counters + 28);
+        ctx->launches++;
+    }
     ctx->launches += 3;
     CK(cudaGetLastError());
     return DMTZ_OK;
@@ -2058,7 +2118,9 @@ void launch_detect(dmtz_ctx *ctx, const Grid &g, const RuleCtx &rc, const PathRe
                                                 ctx->counters + 27);
         k_path_as_pick<<<grid, kBlock, 0, st>>>(g, ctx->sad2, ctx->counters + 10, ctx->as_res, R);
         if (ctx->strict_ds) {  // whole-path descending checks of every 1-saddle, into the records
-            k_ds_strict<<<grid, kBlock, 0, st>>>(rc, R, g.V + 16);
+            cudaMemsetAsync(ctx->counters + 29, 0, sizeof(unsigned long long), st);  // the walks' ticket
+            k_ds_strict<<<grid, kBlock, 0, st>>>(rc, R, ctx->sad1, ctx->counters + 28, g.V + 16,
+                                                 ctx->counters + 29);
             return;
         }
         cudaMemsetAsync(ctx->counters + 26, 0, sizeof(unsigned long long), st);
