@@ -182,25 +182,19 @@ __device__ __forceinline__ bool cof_face_paired3(const Grid &g, const FieldState
     return bit(s.fp3[v + off<fx, fy, fz>(g)], fs);
 }
 
-__device__ __forceinline__ void fast_edge_a4(const Grid &g, const FieldState &s, int v) {
-    const uint32_t a2 = s.ea2[v];
-    uint32_t out = a2;
-    DMTZ_FOR(7, K, {
-        constexpr int k = decltype(K)::value;
-        if (!eup_get(a2, k)) {
-            bool claimed;
-            const int bj = fast_edge_choice<k, false>(g, s, v, claimed);
-            if (bj >= 0) {
-                bool taken = false;
-                DMTZ_FOR(cxt::TOPO_EDGE_NCOF[k], J, {
-                    constexpr int j = decltype(J)::value;
-                    if (bj == j) taken = cof_face_paired3<k, j>(g, s, v);
-                });
-                if (!taken) out |= (uint32_t)(bj + 1) << (3 * k);
-            }
-        }
+// pass 4 for one edge slot K of anchor v (an edge pass 2 left unpaired): its
+// choice if that triangle is still free, as the slot's bits of eup (0 if none)
+template <int K>
+__device__ __forceinline__ uint32_t edge_a4_slot(const Grid &g, const FieldState &s, int v) {
+    bool claimed;
+    const int bj = fast_edge_choice<K, false>(g, s, v, claimed);
+    if (bj < 0) return 0u;
+    bool taken = false;
+    DMTZ_FOR(cxt::TOPO_EDGE_NCOF[K], J, {
+        constexpr int j = decltype(J)::value;
+        if (bj == j) taken = cof_face_paired3<K, j>(g, s, v);
     });
-    s.eup[v] = out;
+    return taken ? 0u : (uint32_t)(bj + 1) << (3 * K);
 }
 
 // ---------------------------------------------------------------- triangles
@@ -308,33 +302,26 @@ __device__ __forceinline__ bool cof_tet_claimed3(const Grid &g, const FieldState
     return r;
 }
 
-__device__ __forceinline__ void fast_face_a5(const Grid &g, const FieldState &s, int v) {
-    const uint32_t a3 = s.fa3[v];
-    const uint32_t p3 = s.fp3[v];
-    uint32_t out = a3;
-    DMTZ_FOR(12, S, {
-        constexpr int sl = decltype(S)::value;
-        if (!bit(p3, sl)) {
-            const bool ep = edge_points_to_face<sl>(g, s.eup, v, 0) || edge_points_to_face<sl>(g, s.eup, v, 1) ||
-                            edge_points_to_face<sl>(g, s.eup, v, 2);
-            if (!ep) {
-                uint32_t l[3];
-                load_corner_lows<sl>(g, s, v, l);
-                int jlo, jmid;
-                fast_tri_order<sl>(s, l, jlo, jmid);
-                const int bj = fast_face_choice<sl, false>(g, s, v, l, jlo, jmid);
-                if (bj >= 0) {
-                    bool claimed = false;
-                    DMTZ_FOR(cxt::TOPO_FACE_NCOF[sl], J, {
-                        constexpr int j = decltype(J)::value;
-                        if (bj == j) claimed = cof_tet_claimed3<sl, j>(g, s, v, jlo);
-                    });
-                    if (!claimed) out |= (uint32_t)(bj + 1) << (2 * sl);
-                }
-            }
-        }
+// pass 5 for one triangle slot S of anchor v (a triangle pass 3 left
+// unpaired): unless pass 4 paired it with an edge, its choice if that
+// tetrahedron is still free, as the slot's bits of fup (0 if none)
+template <int S>
+__device__ __forceinline__ uint32_t face_a5_slot(const Grid &g, const FieldState &s, int v) {
+    const bool ep = edge_points_to_face<S>(g, s.eup, v, 0) || edge_points_to_face<S>(g, s.eup, v, 1) ||
+                    edge_points_to_face<S>(g, s.eup, v, 2);
+    if (ep) return 0u;
+    uint32_t l[3];
+    load_corner_lows<S>(g, s, v, l);
+    int jlo, jmid;
+    fast_tri_order<S>(s, l, jlo, jmid);
+    const int bj = fast_face_choice<S, false>(g, s, v, l, jlo, jmid);
+    if (bj < 0) return 0u;
+    bool claimed = false;
+    DMTZ_FOR(cxt::TOPO_FACE_NCOF[S], J, {
+        constexpr int j = decltype(J)::value;
+        if (bj == j) claimed = cof_tet_claimed3<S, j>(g, s, v, jlo);
     });
-    s.fup[v] = out;
+    return claimed ? 0u : (uint32_t)(bj + 1) << (2 * S);
 }
 
 // ---------------------------------------------------------------- criticality
@@ -459,6 +446,13 @@ __global__ void __launch_bounds__(DMTZ_BRICK, DMTZ_SWEEP_MINB) k_sweep_sm(Grid g
     __shared__ uint16_t sh_c[C ? NB : 1];
     __shared__ uint32_t sh_d[DD ? NB : 1];
     __shared__ uint32_t sh_e[E ? NB : 1];
+    // passes 3 and 4: per slot, the box indices of the anchors whose cell of
+    // that slot is still unpaired, and their count
+    constexpr bool CMP = PASS == 3 || PASS == 4;
+    constexpr int NS = PASS == 3 ? 7 : 12;
+    __shared__ uint16_t sh_item[CMP ? NS : 1][CMP ? DMTZ_BRICK : 1];
+    __shared__ unsigned sh_cnt[CMP ? NS : 1];
+    if (CMP && threadIdx.x < NS) sh_cnt[threadIdx.x] = 0;
     const Grid gb = box_grid<BX, BY>();
     FieldState t;  // box views of the pass's inputs and outputs
     t.val = nullptr;
@@ -537,7 +531,67 @@ __global__ void __launch_bounds__(DMTZ_BRICK, DMTZ_SWEEP_MINB) k_sweep_sm(Grid g
             boxin || (ingrid && x >= 1 && y >= 1 && z >= 1 && x <= g.W - 2 && y <= g.H - 2 && z <= g.D - 2);
         const i64 v = boxin ? (i64)(unsigned)(corner + (lx + 1) + (ly + 1) * g.W + (lz + 1) * g.WHi)
                             : x + (i64)y * g.W + (i64)z * g.WH;
-        if (inner) {
+        if constexpr (CMP) {
+            // The second edge and triangle passes act on the cells the first
+            // ones left unpaired (about one in ten), so a warp running slot by
+            // slot over its anchors would run every slot's body with a few
+            // lanes each.  Instead each slot's pending anchors are listed and
+            // its body runs on consecutive threads; a slot's result bits go
+            // into the anchor's output word by a shared-memory OR.  Slot s's
+            // list starts at warp s mod 4, so the bodies spread over the warps.
+            uint32_t need = 0;
+            if (inner) {
+                if (PASS == 3) {
+                    const uint32_t a2 = sh_a[li];
+                    sh_b[li] = a2;
+                    DMTZ_FOR(7, K, {
+                        constexpr int k = decltype(K)::value;
+                        need |= eup_get(a2, k) ? 0u : 1u << k;
+                    });
+                } else {
+                    sh_d[li] = sh_b[li];
+                    need = ~(uint32_t)sh_c[li] & 0xFFFu;
+                }
+            }
+            const unsigned lane = threadIdx.x & 31u;
+            DMTZ_FOR(NS, S, {
+                constexpr int sl = decltype(S)::value;
+                const bool nd = bit(need, sl);
+                const unsigned m = __ballot_sync(0xffffffffu, nd);
+                if (m) {
+                    unsigned base = 0;
+                    if (lane == 0) base = atomicAdd(&sh_cnt[sl], (unsigned)__popc(m));
+                    base = __shfl_sync(0xffffffffu, base, 0);
+                    if (nd) sh_item[sl][base + (unsigned)__popc(m & ((1u << lane) - 1u))] = (uint16_t)li;
+                }
+            });
+            __syncthreads();
+            DMTZ_FOR(NS, S, {
+                constexpr int sl = decltype(S)::value;
+                const unsigned r = (threadIdx.x + DMTZ_BRICK - 32 * (sl % 4)) % DMTZ_BRICK;
+                const bool mine = r < sh_cnt[sl];
+                // a vote is warp-uniform: warps without items branch around
+                // the body instead of running it under a false predicate
+                if (__any_sync(0xffffffffu, mine) && mine) {
+                    const int a = sh_item[sl][r];
+                    if constexpr (PASS == 3) {
+                        const uint32_t bits = edge_a4_slot<sl>(gb, t, a);
+                        if (bits) atomicOr(&sh_b[a], bits);
+                    } else {
+                        const uint32_t bits = face_a5_slot<sl>(gb, t, a);
+                        if (bits) atomicOr(&sh_d[a], bits);
+                    }
+                }
+            });
+            __syncthreads();
+            if (threadIdx.x < NS) sh_cnt[threadIdx.x] = 0;  // read by no thread before the next brick's barriers
+            if (inner) {
+                if (PASS == 3) s.eup[v] = sh_b[li];
+                else s.fup[v] = sh_d[li];
+            } else if (ingrid && !skip_bnd) {
+                pass_at<PASS>(g, s, v, x, y, z);
+            }
+        } else if (inner) {
             if (PASS == 0) {
                 fast_vertex(gb, t, li);
                 s.key[v] = sh_key[li];
@@ -550,12 +604,6 @@ __global__ void __launch_bounds__(DMTZ_BRICK, DMTZ_SWEEP_MINB) k_sweep_sm(Grid g
                 fast_face_a3(gb, t, li);
                 s.fa3[v] = sh_b[li];
                 s.fp3[v] = sh_c[li];
-            } else if (PASS == 3) {
-                fast_edge_a4(gb, t, li);
-                s.eup[v] = sh_b[li];
-            } else if (PASS == 4) {
-                fast_face_a5(gb, t, li);
-                s.fup[v] = sh_d[li];
             } else {
                 fast_crit(gb, t, li);
                 s.crit[v] = sh_d[li];
