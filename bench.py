@@ -535,6 +535,9 @@ def run_cnn(args):
     pk, pk_src = bf16_peak()
     conv_flop = 2 * 27 * 32 * 32 * V
     tf_conv = conv_flop / (ms[2] * 1e-3) / 1e12
+    # the tensor pipe's own rate for the instruction shape the convolutions
+    # use (128 x 32 x 16) and for wider ones, measured here
+    ceil = {n: net.mma_ceiling(n) for n in (32, 64, 128, 256)}
     line = {"metric": "learned-proposal network, forward TFLOP/s (bf16 tensor cores)",
             "value": CNN_FLOP_PER_VOX * V / (ms[0] * 1e-3) / 1e12, "unit": "TFLOP/s", "n_gpus": 1,
             "steps": args.steps, "warmup": 1, "ms_per_step": ms[0], "higher_is_better": True, "dtype": "bf16",
@@ -543,9 +546,11 @@ def run_cnn(args):
                        "flop_per_voxel_forward": CNN_FLOP_PER_VOX, "train_step_ms": ms[1],
                        "train_step_tflops": 3 * CNN_FLOP_PER_VOX * V / (ms[1] * 1e-3) / 1e12,
                        "wgrad32_ms": ms[3], "wgrad32_tflops": conv_flop / (ms[3] * 1e-3) / 1e12},
-            "roofline": {"bound": "tensor", "kernel": "k_conv<32,32> (one 32->32 layer)", "achieved": tf_conv,
+            "roofline": {"bound": "tensor", "kernel": "k_conv_tc<32,32> (one 32->32 layer)", "achieved": tf_conv,
                          "peak": pk, "unit": "TFLOP/s", "frac": tf_conv / pk, "peak_source": pk_src,
-                         "traffic": None}}
+                         "traffic": None,
+                         "mma_shape_tflops": {f"128x{n}x16": ceil[n] for n in ceil},
+                         "frac_of_shape": tf_conv / ceil[32]}}
     print(json.dumps(line), flush=True)
     net.close()
     ctx.close()

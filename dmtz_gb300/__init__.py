@@ -127,6 +127,7 @@ def load_library(build_if_missing: bool = True):
     L.dmtz_cnn_step.argtypes = [_vp, ctypes.c_float]
     L.dmtz_cnn_set_min_drop.argtypes = [_vp, ctypes.c_float]
     L.dmtz_cnn_set_tensor_path.argtypes = [_vp, _int]
+    L.dmtz_cnn_mma_ceiling.argtypes = [_vp, _int, _int, ctypes.POINTER(ctypes.c_double)]
     L.dmtz_cnn_set_min_drop.restype = _int
     L.dmtz_cnn_profile.argtypes = [_vp, _int, _int, _int, _vp, _vp, _vp, _vp, _int, _f64p]
     L.dmtz_cnn_profile.restype = _int
@@ -497,6 +498,13 @@ class Network:
     def set_tensor_path(self, path: int):
         """1: convolutions on tcgen05 (default); 0: on mma.sync."""
         self._check(self._L.dmtz_cnn_set_tensor_path(self._h, int(path)))
+
+    def mma_ceiling(self, n: int = 32, reps: int = 512) -> float:
+        """TFLOP/s of back-to-back tcgen05.mma of shape 128 x n x 16 (bf16) on
+        every SM: the tensor pipe's ceiling for the convolutions' n = 32."""
+        t = ctypes.c_double()
+        self._check(self._L.dmtz_cnn_mma_ceiling(self._h, int(n), int(reps), ctypes.byref(t)))
+        return t.value
 
     def set_min_drop(self, min_drop: float):
         """Apply the proposal only where it lowers g by at least min_drop x bound."""

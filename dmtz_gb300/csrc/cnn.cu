@@ -300,10 +300,10 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int lim
             : "r"(bar), "r"(parity));
     return done != 0;
 }
-// this warp's 32 accumulator rows, columns 0..N-1 (N = 16 or 32)
+// this warp's 32 accumulator rows, columns 0..N-1 (N = 16 or 32), into r;
+// the registers are valid after tmem_wait()
 template <int N>
-__device__ __forceinline__ void tmem_rows(uint32_t taddr, float (&v)[N]) {
-    uint32_t r[N];
+__device__ __forceinline__ void tmem_ld(uint32_t taddr, uint32_t (&r)[N]) {
     if constexpr (N == 32) {
         asm volatile(
             "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
@@ -322,10 +322,8 @@ __device__ __forceinline__ void tmem_rows(uint32_t taddr, float (&v)[N]) {
               "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
             : "r"(taddr));
     }
-    asm volatile("tcgen05.wait::ld.sync.aligned;\n");
-#pragma unroll
-    for (int i = 0; i < N; i++) v[i] = __uint_as_float(r[i]);
 }
+__device__ __forceinline__ void tmem_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory"); }
 // The halo box arrives by TMA: the activations are a 4-d tensor (channel,
 // x, y, z) with a box of (8 channels, GX, GY, GZ), so one bulk copy per
 // 8-channel group writes exactly one plane (vertex-major, 16 bytes per
@@ -353,17 +351,34 @@ constexpr size_t tc_smem() {
     return 128 + (size_t)27 * (CIN / 8) * COUT * 16 + 2 * (size_t)(CIN / 8) * TC_PLANE;
 }
 
+// Roles (192 threads): warp 0 lane 0 issues the MMAs, warp 1 lane 0 issues
+// the TMA box copies, warps 2..5 run the epilogue (warp w reads accumulator
+// lanes 32 (w mod 4) .. 32 (w mod 4) + 31, the quarter tensor memory lets it
+// access).  Two box buffers and two accumulator sets (2 x QZ x 32 columns)
+// let tile i's MMAs run while tile i-1's epilogue drains its accumulator and
+// tile i+1's box arrives.  Barriers, per buffer b:
+//   full[b]  the box of the tile using b has landed (TMA complete_tx)
+//   mma[b]   that tile's MMAs are done (tcgen05.commit): its accumulator may
+//            be read and its box buffer refilled
+//   free[b]  the epilogue has read that accumulator (one arrival per
+//            epilogue warp)
+// Tile i uses b = i mod 2 and completes phase i / 2 of each barrier; every
+// wait is bounded, and a role that gives up reports in *err and leaves its
+// loop (the others then time out on the phases it no longer completes).
+constexpr int kConvThreads = 192;
+constexpr int kConvWaitPolls = 1 << 24;
 template <int CIN, int COUT, int MODE, bool FLIP>
-__global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUtensorMap tmap, Dims d,
-                                                 const bf16 *__restrict__ wt, const float *__restrict__ bias,
-                                                 void *out, const bf16 *__restrict__ aux, int *err) {
+__global__ void __launch_bounds__(kConvThreads, 1) k_conv_tc(const __grid_constant__ CUtensorMap tmap, Dims d,
+                                                           const bf16 *__restrict__ wt, const float *__restrict__ bias,
+                                                           void *out, const bf16 *__restrict__ aux, int *err) {
     constexpr int KCH = CIN / 8;
     constexpr uint32_t PLANE = TC_PLANE, WTAP = KCH * COUT * 16, WBYTES = 27 * WTAP, XBYTES = KCH * PLANE;
+    constexpr uint32_t ACC_COLS = QZ * 32;  // one accumulator set
     static_assert(CIN % 16 == 0 && (COUT == 16 || COUT == 32), "tile shapes");
     static_assert(WTAP % 128 == 0, "planes stay 128-byte aligned");
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ uint32_t tmem_slot;
-    __shared__ __align__(8) uint64_t mbar_mma[2], mbar_box[2];
+    __shared__ __align__(8) uint64_t bar_full[2], bar_mma[2], bar_free[2];
     unsigned char *ws = smem_raw + ((128 - (smem_addr(smem_raw) & 127)) & 127);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     for (int i = tid; i < 27 * COUT * KCH; i += blockDim.x) {
@@ -372,18 +387,26 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUte
     }
     cp_commit();
     if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;\n" ::"r"(
-            smem_addr(&tmem_slot)));
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                         smem_addr(&tmem_slot)),
+                     "n"(2 * ACC_COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
     }
-    const uint32_t mbars[2] = {smem_addr(&mbar_mma[0]), smem_addr(&mbar_mma[1])},
-                   bbar[2] = {smem_addr(&mbar_box[0]), smem_addr(&mbar_box[1])};
+    // barrier addresses by buffer (selected, not indexed: no local-memory array)
+    const uint32_t full0 = smem_addr(&bar_full[0]), full1 = smem_addr(&bar_full[1]);
+    const uint32_t mma0 = smem_addr(&bar_mma[0]), mma1 = smem_addr(&bar_mma[1]);
+    const uint32_t fre0 = smem_addr(&bar_free[0]), fre1 = smem_addr(&bar_free[1]);
+    auto full = [&](int b) { return b ? full1 : full0; };
+    auto mma = [&](int b) { return b ? mma1 : mma0; };
+    auto fre = [&](int b) { return b ? fre1 : fre0; };
     const uint32_t wbase = smem_addr(ws), xbase0 = wbase + WBYTES;
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mbars[0]));
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mbars[1]));
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bbar[0]));
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bbar[1]));
+#pragma unroll
+        for (int b = 0; b < 2; b++) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(full(b)));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mma(b)));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;\n" ::"r"(fre(b)));
+        }
         asm volatile("fence.mbarrier_init.release.cluster;\n");
     }
     cp_wait<0>();
@@ -391,52 +414,33 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUte
     asm volatile("tcgen05.fence::before_thread_sync;\n");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n");
-    const uint32_t tmem = tmem_slot, taddr = tmem + ((uint32_t)(warp * 32) << 16);
-    const uint32_t idesc = tc_idesc<COUT>();
-    const uint32_t bar = mbars[0];
+    const uint32_t tmem = tmem_slot;
+    const i64 first = blockIdx.x, stride = gridDim.x;
+    const int ntile = first < d.ntiles ? (int)((d.ntiles - 1 - first) / stride + 1) : 0;
+    bool failed = false;
 
-    i64 tile = blockIdx.x;
-    int it = 0;
-    bool box_pending = false, mma_pending = false, failed = false;
-    uint32_t pending_bar = 0, pending_par = 0, cur_bar = 0, cur_par = 0;
-    if (tid == 0 && tile < d.ntiles) {
-        int x0, y0, z0;
-        tc_tile_origin(d, tile, x0, y0, z0);
-        tc_issue_box<CIN>(&tmap, xbase0, bbar[0], x0, y0, z0);
-    }
-    for (; tile < d.ntiles; tile += gridDim.x, it++) {
-        const int buf = it & 1;
-        const uint32_t bpar = (uint32_t)(it >> 1) & 1u, mpar = (uint32_t)it & 1u;
-        bool ok = true;
-        if (tid == 0) {
-            const i64 next = tile + gridDim.x;
-            if (next < d.ntiles) {  // the other buffer's MMAs finished last iteration
-                int x0, y0, z0;
-                tc_tile_origin(d, next, x0, y0, z0);
-                tc_issue_box<CIN>(&tmap, xbase0 + (buf ^ 1) * XBYTES, bbar[buf ^ 1], x0, y0, z0);
-                box_pending = true;
-                pending_bar = bbar[buf ^ 1];
-                pending_par = (uint32_t)((it + 1) >> 1) & 1u;
-            } else {
-                box_pending = false;
-            }
-            ok = mbar_wait(bbar[buf], bpar, 1 << 24);
-            if (!ok) {  // this box too is still in flight
-                cur_bar = bbar[buf];
-                cur_par = bpar;
-            }
-            if (ok) {
+    if (warp == 0) {
+        if (lane == 0) {  // MMA issuer
+            const uint32_t idesc = tc_idesc<COUT>();
+            const uint64_t b0 = smem_desc(wbase, COUT * 16, 128);
+            int committed = 0;
+            for (int it = 0; it < ntile; it++) {
+                const int b = it & 1;
+                if (!mbar_wait(full(b), (uint32_t)(it >> 1) & 1u, kConvWaitPolls) ||
+                    (it >= 2 && !mbar_wait(fre(b), (uint32_t)((it >> 1) - 1) & 1u, kConvWaitPolls))) {
+                    failed = true;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;\n");
                 // descriptors of every (tap, channel group) differ from the
                 // buffer's and the weights' base descriptors only in the
                 // start-address field (shared addresses stay below 2^18, so
                 // adding the offset in 16-byte units never carries out of it):
-                // the unrolled chain adds immediates
-                const uint64_t a0 = smem_desc(xbase0 + buf * XBYTES, PLANE, GX * 16);
-                const uint64_t b0 = smem_desc(wbase, COUT * 16, 128);
-                // the QZ slices' chains are interleaved: consecutive MMAs go
-                // to different accumulators, so one MMA's accumulation does
-                // not wait for the previous one (a single chain of these
-                // small N = COUT products kept the tensor pipe 15 % busy)
+                // the unrolled chain adds immediates.  The QZ slices' chains
+                // are interleaved so that consecutive MMAs go to different
+                // accumulators.
+                const uint64_t a0 = smem_desc(xbase0 + b * XBYTES, PLANE, GX * 16);
+                const uint32_t acc = tmem + (uint32_t)b * ACC_COLS;
 #pragma unroll
                 for (int tap = 0; tap < 27; tap++) {
                     // offset + 1 along each axis (FLIP mirrors the tap: -d + 1 = 2 - (d + 1))
@@ -447,81 +451,151 @@ __global__ void __launch_bounds__(128, 1) k_conv_tc(const __grid_constant__ CUte
                     for (int kk = 0; kk < KCH / 2; kk++)
 #pragma unroll
                         for (int q = 0; q < QZ; q++)
-                            tc_mma(tmem + (uint32_t)(q * 32), a0 + ((shift + q * GY * GX * 16 + kk * 2 * PLANE) >> 4),
+                            tc_mma(acc + (uint32_t)(q * 32), a0 + ((shift + q * GY * GX * 16 + kk * 2 * PLANE) >> 4),
                                    b0 + ((tap * WTAP + kk * 2 * COUT * 16) >> 4), idesc, (tap | kk) != 0);
                 }
                 asm volatile(
-                    "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar));
+                    "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mma(b)));
+                committed = it + 1;
             }
+            if (committed > 0)  // every MMA issued is done before the accumulators are released
+                mbar_wait(mma((committed - 1) & 1), (uint32_t)((committed - 1) >> 1) & 1u, kConvWaitPolls);
         }
-        if (__syncthreads_or(!ok)) {
-            failed = true;
-            break;
+        __syncwarp();
+    } else if (warp == 1) {
+        if (lane == 0) {  // box producer
+            int issued = 0;
+            for (int it = 0; it < ntile; it++) {
+                const int b = it & 1;
+                // buffer b was last read by tile it-2's MMAs
+                if (it >= 2 && !mbar_wait(mma(b), (uint32_t)((it >> 1) - 1) & 1u, kConvWaitPolls)) {
+                    failed = true;
+                    break;
+                }
+                int x0, y0, z0;
+                tc_tile_origin(d, first + it * stride, x0, y0, z0);
+                tc_issue_box<CIN>(&tmap, xbase0 + b * XBYTES, full(b), x0, y0, z0);
+                issued = it + 1;
+            }
+            // the copies still in flight land before the block leaves
+            for (int j = issued - 2; j < issued; j++)
+                if (j >= 0) mbar_wait(full(j & 1), (uint32_t)(j >> 1) & 1u, kConvWaitPolls);
         }
-        mma_pending = true;
-        ok = mbar_wait(bar, mpar, 1 << 24);
-        if (__syncthreads_or(!ok)) {
-            failed = true;
-            break;
-        }
-        mma_pending = false;
-        asm volatile("tcgen05.fence::after_thread_sync;\n");
-        int x0, y0, z0;
-        tc_tile_origin(d, tile, x0, y0, z0);
-#pragma unroll 1
-        for (int zq = 0; zq < QZ; zq++) {  // slice zq of the tile: accumulator columns 32 zq ..
-        float acc[COUT];
-        tmem_rows<COUT>(taddr + (uint32_t)(zq * 32), acc);
-        const int r = warp * 32 + lane, gx = x0 + (r & 7), gy = y0 + (r >> 3), gz = z0 + zq;
-        if (gx < d.W && gy < d.H && gz < d.D) {
-            const i64 v = gx + (i64)gy * d.W + (i64)gz * d.W * d.H;
-            if constexpr (MODE == 1) {
-                reinterpret_cast<float *>(out)[v] = acc[0] + bias[0];
-            } else {
-                uint4 *o = reinterpret_cast<uint4 *>(reinterpret_cast<bf16 *>(out) + v * COUT);
-                const uint4 *ax = MODE == 2 ? reinterpret_cast<const uint4 *>(aux + v * COUT) : nullptr;
+        __syncwarp();
+    } else {  // epilogue: warps 2..5
+        const int quarter = warp & 3;
+        const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16);
+        float bsh[COUT];  // the layer's bias, held in registers (MODE 0 adds all, MODE 1 the first)
 #pragma unroll
-                for (int q = 0; q < COUT / 8; q++) {
-                    uint4 mk = make_uint4(0, 0, 0, 0);
-                    if constexpr (MODE == 2) mk = ax[q];
-                    const bf16 *mb = reinterpret_cast<const bf16 *>(&mk);
-                    uint4 pk;
-                    __nv_bfloat162 *p2 = reinterpret_cast<__nv_bfloat162 *>(&pk);
+        for (int c = 0; c < COUT; c++) bsh[c] = MODE == 2 ? 0.f : (MODE == 1 && c > 0 ? 0.f : bias[c]);
+        for (int it = 0; it < ntile; it++) {
+            const int b = it & 1;
+            if (!mbar_wait(mma(b), (uint32_t)(it >> 1) & 1u, kConvWaitPolls)) {
+                failed = true;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;\n");
+            // every slice's rows at once, one wait, and the accumulator set is
+            // handed back to the MMA issuer before the arithmetic and stores
+            uint32_t raw[QZ][COUT];
 #pragma unroll
-                    for (int h = 0; h < 4; h++) {
-                        const int ch = q * 8 + 2 * h;
-                        float v0 = acc[ch], v1 = acc[ch + 1];
-                        if constexpr (MODE == 0) {
-                            v0 = fmaxf(v0 + bias[ch], 0.f);
-                            v1 = fmaxf(v1 + bias[ch + 1], 0.f);
-                        } else {
-                            if (!(__bfloat162float(mb[2 * h]) > 0.f)) v0 = 0.f;
-                            if (!(__bfloat162float(mb[2 * h + 1]) > 0.f)) v1 = 0.f;
+            for (int zq = 0; zq < QZ; zq++) tmem_ld<COUT>(taddr + (uint32_t)b * ACC_COLS + (uint32_t)(zq * 32), raw[zq]);
+            tmem_wait();
+            asm volatile("tcgen05.fence::before_thread_sync;\n");
+            __syncwarp();
+            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(fre(b)) : "memory");
+            int x0, y0, z0;
+            tc_tile_origin(d, first + it * stride, x0, y0, z0);
+            const int r = quarter * 32 + lane, gx = x0 + (r & 7), gy = y0 + (r >> 3);
+#pragma unroll
+            for (int zq = 0; zq < QZ; zq++) {  // slice zq of the tile
+                const int gz = z0 + zq;
+                if (gx < d.W && gy < d.H && gz < d.D) {
+                    const i64 v = gx + (i64)gy * d.W + (i64)gz * d.W * d.H;
+                    if constexpr (MODE == 1) {
+                        reinterpret_cast<float *>(out)[v] = __uint_as_float(raw[zq][0]) + bsh[0];
+                    } else {
+                        uint4 *o = reinterpret_cast<uint4 *>(reinterpret_cast<bf16 *>(out) + v * COUT);
+                        const uint4 *ax = MODE == 2 ? reinterpret_cast<const uint4 *>(aux + v * COUT) : nullptr;
+#pragma unroll
+                        for (int q = 0; q < COUT / 8; q++) {
+                            uint4 mk = make_uint4(0, 0, 0, 0);
+                            if constexpr (MODE == 2) mk = ax[q];
+                            const bf16 *mb = reinterpret_cast<const bf16 *>(&mk);
+                            uint4 pk;
+                            __nv_bfloat162 *p2 = reinterpret_cast<__nv_bfloat162 *>(&pk);
+#pragma unroll
+                            for (int h = 0; h < 4; h++) {
+                                const int ch = q * 8 + 2 * h;
+                                float v0 = __uint_as_float(raw[zq][ch]), v1 = __uint_as_float(raw[zq][ch + 1]);
+                                if constexpr (MODE == 0) {
+                                    v0 = fmaxf(v0 + bsh[ch], 0.f);
+                                    v1 = fmaxf(v1 + bsh[ch + 1], 0.f);
+                                } else {
+                                    if (!(__bfloat162float(mb[2 * h]) > 0.f)) v0 = 0.f;
+                                    if (!(__bfloat162float(mb[2 * h + 1]) > 0.f)) v1 = 0.f;
+                                }
+                                p2[h] = __floats2bfloat162_rn(v0, v1);
+                            }
+                            o[q] = pk;
                         }
-                        p2[h] = __floats2bfloat162_rn(v0, v1);
                     }
-                    o[q] = pk;
                 }
             }
         }
-        }
-        asm volatile("tcgen05.fence::before_thread_sync;\n");
-        __syncthreads();  // accumulator read before the next tile's MMAs overwrite it
-        asm volatile("tcgen05.fence::after_thread_sync;\n");
     }
-    if (failed) {
-        // report, then give the copies and MMAs in flight one more bounded
-        // wait before the accumulator is released
-        if (tid == 0) {
-            atomicOr(err, 1);
-            if (box_pending) mbar_wait(pending_bar, pending_par, 1 << 24);
-            if (cur_bar) mbar_wait(cur_bar, cur_par, 1 << 24);
-        }
-        if (mma_pending) mbar_wait(bar, (uint32_t)it & 1u, 1 << 24);
+    if (failed) atomicOr(err, 1);
+    asm volatile("tcgen05.fence::before_thread_sync;\n");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n");
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "n"(2 * ACC_COLS));
+}
+
+// The tensor pipe's own ceiling for one instruction shape: one block per SM
+// issues `reps` x 8 back-to-back tcgen05.mma of M = 128, N, K = 16 (bf16,
+// f32 accumulators) on zeroed shared-memory operands, into 256 / N
+// accumulators in turn, and waits for them (bounded).  A convolution made of
+// N = 32 products (32 output channels) cannot run faster than this kernel at
+// N = 32; measured on GB300 the rate grows with N up to N = 128.
+// operands: A (4 KB) at 0, B (N x 32 bytes, <= 8 KB) at 16 KB; the launch asks
+// for more shared memory than two blocks can share, so each SM runs one
+constexpr uint32_t kRateOperands = 24 * 1024, kRateSmem = 120 * 1024;
+template <int N>
+__global__ void __launch_bounds__(128, 1) k_mma_rate(int reps, int *err) {
+    extern __shared__ __align__(128) unsigned char rs[];
+    __shared__ uint32_t tmem_slot;
+    __shared__ __align__(8) uint64_t mbar;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    for (int i = tid; i < (int)(kRateOperands / 4); i += blockDim.x) reinterpret_cast<uint32_t *>(rs)[i] = 0u;
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;\n" ::"r"(smem_addr(&tmem_slot)));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    const uint32_t bar = smem_addr(&mbar);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar));
+        asm volatile("fence.mbarrier_init.release.cluster;\n");
+    }
+    asm volatile("fence.proxy.async.shared::cta;\n");
+    asm volatile("tcgen05.fence::before_thread_sync;\n");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n");
+    const uint32_t tmem = tmem_slot;
+    if (tid == 0) {
+        const uint32_t base = smem_addr(rs);
+        const uint64_t a = smem_desc(base, 2048, 128), b = smem_desc(base + 16384, N * 16, 128);
+        const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | (8u << 24);
+        for (int r = 0; r < reps; r++)
+#pragma unroll
+            for (int q = 0; q < 8; q++) tc_mma(tmem + (uint32_t)((q % (256 / N)) * N), a, b, idesc, (r | q) != 0);
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar));
+        if (!mbar_wait(bar, 0u, 1 << 24)) atomicOr(err, 1);
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n");
     __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;\n" ::"r"(tmem));
+    asm volatile("tcgen05.fence::after_thread_sync;\n");
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;\n" ::"r"(tmem));
 }
 
 // ------------------------------------------------------------ weight gradient
@@ -850,7 +924,7 @@ dmtz_status conv(dmtz_cnn *net, const Dims &d, const bf16 *in, const bf16 *w, co
         if (s != DMTZ_OK) return s;
         int *err = net->tc_err;
         void *args[] = {&tm, &dt, &w, &bias, &out, &aux, &err};
-        return launch_persistent(net, k_conv_tc<CIN, COUT, MODE, FLIP>, 128, tc_smem<CIN, COUT>(), dt.ntiles, 0,
+        return launch_persistent(net, k_conv_tc<CIN, COUT, MODE, FLIP>, kConvThreads, tc_smem<CIN, COUT>(), dt.ntiles, 0,
                                  nullptr, st, args);
     }
     Dims dd = d;
@@ -1094,6 +1168,38 @@ static dmtz_status check_tc(dmtz_cnn *net) {
 dmtz_status dmtz_cnn_set_tensor_path(dmtz_cnn *net, int path) {
     if (!net || (path != 0 && path != 1)) return DMTZ_ERR_ARG;
     net->tensor_path = path;
+    return DMTZ_OK;
+}
+
+dmtz_status dmtz_cnn_mma_ceiling(dmtz_cnn *net, int n, int reps, double *tflops) {
+    if (!net || !tflops || reps < 1 || reps > (1 << 16) || (n != 32 && n != 64 && n != 128 && n != 256))
+        return DMTZ_ERR_ARG;
+    NCK(cudaSetDevice(net->device));
+    cudaStream_t st = net->stream;
+    void (*kern)(int, int *) = n == 32 ? k_mma_rate<32> : n == 64 ? k_mma_rate<64> : n == 128 ? k_mma_rate<128>
+                                                                                             : k_mma_rate<256>;
+    NCK(cudaFuncSetAttribute((const void *)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRateSmem));
+    int *err = nullptr;
+    NCK(cudaMalloc(&err, sizeof(int)));
+    cudaEvent_t e[2];
+    cudaEventCreate(&e[0]);
+    cudaEventCreate(&e[1]);
+    cudaMemsetAsync(err, 0, sizeof(int), st);
+    kern<<<net->nsm, 128, kRateSmem, st>>>(reps, err);  // warm-up
+    cudaEventRecord(e[0], st);
+    kern<<<net->nsm, 128, kRateSmem, st>>>(reps, err);
+    cudaEventRecord(e[1], st);
+    int herr = 0;
+    cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st);
+    const cudaError_t ce = cudaStreamSynchronize(st);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e[0], e[1]);
+    cudaEventDestroy(e[0]);
+    cudaEventDestroy(e[1]);
+    cudaFree(err);
+    if (ce != cudaSuccess) return nfail(net, DMTZ_ERR_CUDA, std::string("k_mma_rate: ") + cudaGetErrorString(ce));
+    if (herr) return nfail(net, DMTZ_ERR_CUDA, "k_mma_rate: the MMAs did not complete in time");
+    *tflops = 2.0 * 128 * n * 16 * 8.0 * reps * net->nsm / (ms * 1e-3) / 1e12;
     return DMTZ_OK;
 }
 

@@ -332,6 +332,12 @@ dmtz_status dmtz_cnn_backward(dmtz_cnn *net, int W, int H, int D, const float *t
  * 0 = the warp-level mma.sync kernels.  Same arithmetic (bf16 products, f32
  * sums); results differ only in the order of the f32 sums. */
 dmtz_status dmtz_cnn_set_tensor_path(dmtz_cnn *net, int path);
+/* Measurement only: the tensor pipe's rate, in TFLOP/s over all SMs, for
+ * back-to-back tcgen05.mma of shape M = 128, N = n (32, 64, 128 or 256),
+ * K = 16 (bf16, f32 accumulators), `reps` x 8 per SM.  The convolutions'
+ * products have N = 32 (the output channels), so the n = 32 rate bounds
+ * them. */
+dmtz_status dmtz_cnn_mma_ceiling(dmtz_cnn *net, int n, int reps, double *tflops);
 /* proposal threshold in units of the bound, 0..2 */
 dmtz_status dmtz_cnn_set_min_drop(dmtz_cnn *net, float min_drop);
 /* one Adam step (beta 0.9 / 0.999, eps 1e-8) with learning rate lr */

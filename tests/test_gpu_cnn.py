@@ -343,3 +343,14 @@ def test_tensor_paths_agree(net):
         outs.append(out.cpu().numpy().astype(np.float64))
     net.set_tensor_path(1)
     assert _rel(outs[0], outs[1]) < 1e-2
+
+
+def test_mma_shape_ceiling(net):
+    """The tensor pipe's rate for back-to-back 128 x N x 16 products: every
+    shape completes, and wider products run at least as fast per FLOP as the
+    convolutions' N = 32 (the rates are the ceilings the profiles cite)."""
+    rates = {n: net.mma_ceiling(n, reps=256) for n in (32, 64, 128, 256)}
+    assert all(r > 0 for r in rates.values()), rates
+    assert rates[256] >= rates[32], rates
+    with pytest.raises(RuntimeError):  # DmtzError: shapes other than 32..256 by powers of 2
+        net.mma_ceiling(48)
