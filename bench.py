@@ -522,6 +522,7 @@ def run_cnn(args):
     V = size ** 3
     ctx = dm.Context(0)
     net = dm.Network(0, seed=0)
+    net.set_tensor_path(args.tensor_path)
     fd, gd = torch.from_numpy(f).cuda(), torch.from_numpy(g).cuda()
     feat = torch.empty((V, 16), dtype=torch.bfloat16, device="cuda")
     active = torch.empty(V, dtype=torch.uint8, device="cuda")
@@ -537,7 +538,9 @@ def run_cnn(args):
     tf_conv = conv_flop / (ms[2] * 1e-3) / 1e12
     # the tensor pipe's own rate for the instruction shape the convolutions
     # use (128 x 32 x 16) and for wider ones, measured here
-    ceil = {n: net.mma_ceiling(n) for n in (32, 64, 128, 256)}
+    ceil = {n: net.mma_ceiling(n) for n in (32, 64, 96, 128, 256)}
+    # path 2's MMAs are 128 x 96 x 16, of whose 128 rows (16 per x-line) 14 are outputs
+    shape_n, row_eff = (96, 14 / 16) if args.tensor_path == 2 else (32, 1.0)
     line = {"metric": "learned-proposal network, forward TFLOP/s (bf16 tensor cores)",
             "value": CNN_FLOP_PER_VOX * V / (ms[0] * 1e-3) / 1e12, "unit": "TFLOP/s", "n_gpus": 1,
             "steps": args.steps, "warmup": 1, "ms_per_step": ms[0], "higher_is_better": True, "dtype": "bf16",
@@ -546,11 +549,13 @@ def run_cnn(args):
                        "flop_per_voxel_forward": CNN_FLOP_PER_VOX, "train_step_ms": ms[1],
                        "train_step_tflops": 3 * CNN_FLOP_PER_VOX * V / (ms[1] * 1e-3) / 1e12,
                        "wgrad32_ms": ms[3], "wgrad32_tflops": conv_flop / (ms[3] * 1e-3) / 1e12},
-            "roofline": {"bound": "tensor", "kernel": "k_conv_tc<32,32> (one 32->32 layer)", "achieved": tf_conv,
+            "roofline": {"bound": "tensor", "kernel": {0: "k_conv", 1: "k_conv_tc", 2: "k_conv_tcx"}[args.tensor_path]
+                         + "<32,32> (one 32->32 layer)", "achieved": tf_conv,
                          "peak": pk, "unit": "TFLOP/s", "frac": tf_conv / pk, "peak_source": pk_src,
                          "traffic": None,
                          "mma_shape_tflops": {f"128x{n}x16": ceil[n] for n in ceil},
-                         "frac_of_shape": tf_conv / ceil[32]}}
+                         "mma_shape": f"128x{shape_n}x16", "output_rows_per_mma": row_eff,
+                         "frac_of_shape": tf_conv / row_eff / ceil[shape_n]}}
     print(json.dumps(line), flush=True)
     net.close()
     ctx.close()
@@ -745,6 +750,8 @@ def main():
     ap.add_argument("--big-kind", choices=["powerlaw", "gauss"], default="powerlaw", help="big workload: field kind")
     ap.add_argument("--max-rounds", type=int, default=2000)
     ap.add_argument("--cnn-size", type=int, default=256, help="cnn workload: grid size")
+    ap.add_argument("--tensor-path", type=int, default=2, choices=[0, 1, 2],
+                    help="cnn workload: 1 tcgen05, 2 tcgen05 with folded x-taps, 0 mma.sync")
     ap.add_argument("--traces", type=int, default=200, help="learned workload and line: training traces")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned warm start's A/B in the default line")
     ap.add_argument("--epochs", type=int, default=10, help="learned workload: epochs")

@@ -496,12 +496,15 @@ class Network:
         return loss.value
 
     def set_tensor_path(self, path: int):
-        """1: convolutions on tcgen05 (default); 0: on mma.sync."""
+        """2: convolutions on tcgen05 with the three x-taps of each offset
+        folded into one wider product (default); 1: on tcgen05, one product
+        per tap; 0: on mma.sync."""
         self._check(self._L.dmtz_cnn_set_tensor_path(self._h, int(path)))
 
     def mma_ceiling(self, n: int = 32, reps: int = 512) -> float:
         """TFLOP/s of back-to-back tcgen05.mma of shape 128 x n x 16 (bf16) on
-        every SM: the tensor pipe's ceiling for the convolutions' n = 32."""
+        every SM: the tensor pipe's ceiling for the convolutions' products
+        (n = 96 on the default tensor path, 32 on path 1)."""
         t = ctypes.c_double()
         self._check(self._L.dmtz_cnn_mma_ceiling(self._h, int(n), int(reps), ctypes.byref(t)))
         return t.value

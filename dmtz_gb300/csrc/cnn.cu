@@ -552,10 +552,244 @@ __global__ void __launch_bounds__(kConvThreads, 1) k_conv_tc(const __grid_consta
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "n"(2 * ACC_COLS));
 }
 
+// ---------------------------------------- convolution on tcgen05, x-taps folded
+// The same convolution with wider products.  For each (dy, dz) offset one
+// MMA multiplies the rows shifted by (-1, dy, dz) with the three x-taps'
+// weight blocks side by side (N = 3 COUT): columns [t COUT, (t+1) COUT) of
+// row r hold the contribution of x-tap t (dx = t - 1) to the output t
+// vertices before row r's along x, so
+//   out[r] = D[r][0, COUT) + D[r+1][COUT, 2 COUT) + D[r+2][2 COUT, 3 COUT),
+// summed in the epilogue with two warp shuffles per channel.  A tile's 128
+// rows are 8 lines of 16 x-neighbours (two core matrices per line, so the
+// 8-row groups are 128 bytes apart throughout), of which the first 14 are
+// outputs; tiles step 14 along x and overlap by two rows.  The box needs no
+// halo along +x (16 x 10 x (QZ2 + 2) vertices).  9 x CIN/16 x QZ2 MMAs per
+// tile of 14 x 8 x QZ2 outputs.  Roles, barriers and bounded waits as in
+// k_conv_tc; FLIP mirrors the taps through the weight layout.
+constexpr int XF_TX = 14, XF_GX = 16, XF_TY = 8, XF_GY = XF_TY + 2, XF_QZ = 2, XF_GZ = XF_QZ + 2;
+constexpr int XF_GVOX = XF_GX * XF_GY * XF_GZ;
+constexpr uint32_t XF_PLANE = XF_GVOX * 16;  // a multiple of 128
+inline Dims make_xf_dims(int W, int H, int D) {
+    Dims d{W, H, D, (W + XF_TX - 1) / XF_TX, (H + XF_TY - 1) / XF_TY, (D + XF_QZ - 1) / XF_QZ, 0};
+    d.ntiles = (i64)d.ntx * d.nty * d.ntz;
+    return d;
+}
+// accumulator columns of one slice: 3 COUT rounded up to a power of two
+template <int COUT>
+__host__ __device__ constexpr uint32_t xf_cols() {
+    return COUT == 32 ? 128u : 64u;
+}
+template <int CIN, int COUT>
+constexpr size_t xf_smem() {
+    return 128 + (size_t)9 * (CIN / 8) * (3 * COUT) * 16 + 2 * (size_t)(CIN / 8) * XF_PLANE;
+}
+template <int CIN, int COUT, int MODE, bool FLIP>
+__global__ void __launch_bounds__(kConvThreads, 1) k_conv_tcx(const __grid_constant__ CUtensorMap tmap, Dims d,
+                                                            const bf16 *__restrict__ wt,
+                                                            const float *__restrict__ bias, void *out,
+                                                            const bf16 *__restrict__ aux, int *err) {
+    constexpr int KCH = CIN / 8, N = 3 * COUT;
+    constexpr uint32_t WGRP = N * 16, WBYTES = 9 * KCH * WGRP, XBYTES = KCH * XF_PLANE;
+    constexpr uint32_t SCOLS = xf_cols<COUT>(), ACC_COLS = XF_QZ * SCOLS, ALLOC = 2 * ACC_COLS;
+    static_assert(CIN % 16 == 0 && (COUT == 16 || COUT == 32), "tile shapes");
+    static_assert(WGRP % 128 == 0 && XF_PLANE % 128 == 0, "operand blocks stay 128-byte aligned");
+    static_assert(ALLOC == 256 || ALLOC == 512, "tensor-memory allocation is a power of two");
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ uint32_t tmem_slot;
+    __shared__ __align__(8) uint64_t bar_full[2], bar_mma[2], bar_free[2];
+    unsigned char *ws = smem_raw + ((128 - (smem_addr(smem_raw) & 127)) & 127);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // weights: per (dy, dz) offset u and channel group kc, rows n = t COUT + c
+    // hold tap (t - 1, dy, dz) of output channel c (mirrored under FLIP)
+    for (int i = tid; i < 9 * KCH * N; i += blockDim.x) {
+        const int u = i / (KCH * N), rem = i - u * (KCH * N), kc = rem / N, n = rem - kc * N;
+        const int t = n / COUT, c = n - t * COUT;
+        const int tap = FLIP ? 26 - (t + 3 * u) : t + 3 * u;
+        cp16(ws + (u * KCH + kc) * WGRP + n * 16, wt + ((i64)tap * COUT + c) * CIN + kc * 8, 16);
+    }
+    cp_commit();
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
+                         smem_addr(&tmem_slot)),
+                     "n"(ALLOC));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    const uint32_t full0 = smem_addr(&bar_full[0]), full1 = smem_addr(&bar_full[1]);
+    const uint32_t mma0 = smem_addr(&bar_mma[0]), mma1 = smem_addr(&bar_mma[1]);
+    const uint32_t fre0 = smem_addr(&bar_free[0]), fre1 = smem_addr(&bar_free[1]);
+    auto full = [&](int b) { return b ? full1 : full0; };
+    auto mma = [&](int b) { return b ? mma1 : mma0; };
+    auto fre = [&](int b) { return b ? fre1 : fre0; };
+    const uint32_t wbase = smem_addr(ws), xbase0 = wbase + WBYTES;
+    if (tid == 0) {
+#pragma unroll
+        for (int b = 0; b < 2; b++) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(full(b)));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mma(b)));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;\n" ::"r"(fre(b)));
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;\n");
+    }
+    cp_wait<0>();
+    asm volatile("fence.proxy.async.shared::cta;\n");
+    asm volatile("tcgen05.fence::before_thread_sync;\n");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n");
+    const uint32_t tmem = tmem_slot;
+    const i64 first = blockIdx.x, stride = gridDim.x;
+    const int ntile = first < d.ntiles ? (int)((d.ntiles - 1 - first) / stride + 1) : 0;
+    auto origin = [&](i64 tile, int &x0, int &y0, int &z0) {
+        x0 = (int)(tile % d.ntx) * XF_TX;
+        y0 = (int)((tile / d.ntx) % d.nty) * XF_TY;
+        z0 = (int)(tile / ((i64)d.ntx * d.nty)) * XF_QZ;
+    };
+    bool failed = false;
+
+    if (warp == 0) {
+        if (lane == 0) {  // MMA issuer
+            const uint32_t idesc =
+                (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+            const uint64_t b0 = smem_desc(wbase, WGRP, 128);
+            int committed = 0;
+            for (int it = 0; it < ntile; it++) {
+                const int b = it & 1;
+                if (!mbar_wait(full(b), (uint32_t)(it >> 1) & 1u, kConvWaitPolls) ||
+                    (it >= 2 && !mbar_wait(fre(b), (uint32_t)((it >> 1) - 1) & 1u, kConvWaitPolls))) {
+                    failed = true;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;\n");
+                const uint64_t a0 = smem_desc(xbase0 + b * XBYTES, XF_PLANE, 128);
+                const uint32_t acc = tmem + (uint32_t)b * ACC_COLS;
+#pragma unroll
+                for (int u = 0; u < 9; u++) {
+                    const int sy = u % 3, sz = u / 3;  // dy + 1, dz + 1
+#pragma unroll
+                    for (int kk = 0; kk < KCH / 2; kk++)
+#pragma unroll
+                        for (int q = 0; q < XF_QZ; q++)
+                            tc_mma(acc + (uint32_t)q * SCOLS,
+                                   a0 + ((((q + sz) * XF_GY + sy) * XF_GX * 16 + kk * 2 * XF_PLANE) >> 4),
+                                   b0 + (((u * KCH + kk * 2) * WGRP) >> 4), idesc, (u | kk) != 0);
+                }
+                asm volatile(
+                    "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mma(b)));
+                committed = it + 1;
+            }
+            if (committed > 0)
+                mbar_wait(mma((committed - 1) & 1), (uint32_t)((committed - 1) >> 1) & 1u, kConvWaitPolls);
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        if (lane == 0) {  // box producer
+            int issued = 0;
+            for (int it = 0; it < ntile; it++) {
+                const int b = it & 1;
+                if (it >= 2 && !mbar_wait(mma(b), (uint32_t)((it >> 1) - 1) & 1u, kConvWaitPolls)) {
+                    failed = true;
+                    break;
+                }
+                int x0, y0, z0;
+                origin(first + it * stride, x0, y0, z0);
+                const uint32_t dst = xbase0 + b * XBYTES, bar = full(b);
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar),
+                             "r"((uint32_t)(KCH * XF_GVOX * 16)));
+#pragma unroll
+                for (int c = 0; c < KCH; c++)
+                    asm volatile(
+                        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, "
+                        "{%2, %3, %4, %5}], [%6];\n" ::"r"(dst + c * XF_PLANE),
+                        "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(c * 8), "r"(x0 - 1), "r"(y0 - 1), "r"(z0 - 1),
+                        "r"(bar)
+                        : "memory");
+                issued = it + 1;
+            }
+            for (int j = issued - 2; j < issued; j++)
+                if (j >= 0) mbar_wait(full(j & 1), (uint32_t)(j >> 1) & 1u, kConvWaitPolls);
+        }
+        __syncwarp();
+    } else {  // epilogue: warps 2..5
+        const int quarter = warp & 3;
+        const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16);
+        float bsh[COUT];
+#pragma unroll
+        for (int c = 0; c < COUT; c++) bsh[c] = MODE == 2 ? 0.f : (MODE == 1 && c > 0 ? 0.f : bias[c]);
+        const int r = quarter * 32 + lane, rx = r & 15, ry = r >> 4;
+        for (int it = 0; it < ntile; it++) {
+            const int b = it & 1;
+            if (!mbar_wait(mma(b), (uint32_t)(it >> 1) & 1u, kConvWaitPolls)) {
+                failed = true;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;\n");
+            int x0, y0, z0;
+            origin(first + it * stride, x0, y0, z0);
+            const int gx = x0 + rx, gy = y0 + ry;
+#pragma unroll 1
+            for (int zq = 0; zq < XF_QZ; zq++) {
+                uint32_t p0[COUT], p1[COUT], p2[COUT];
+                const uint32_t col = taddr + (uint32_t)b * ACC_COLS + (uint32_t)zq * SCOLS;
+                tmem_ld<COUT>(col, p0);
+                tmem_ld<COUT>(col + COUT, p1);
+                tmem_ld<COUT>(col + 2 * COUT, p2);
+                tmem_wait();
+                if (zq == XF_QZ - 1) {  // the accumulator set is read: hand it back
+                    asm volatile("tcgen05.fence::before_thread_sync;\n");
+                    __syncwarp();
+                    if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(fre(b)) : "memory");
+                }
+                float acc[COUT];
+#pragma unroll
+                for (int c = 0; c < COUT; c++)  // rows r+1 and r+2 are lanes lane+1, lane+2 (same x-line)
+                    acc[c] = __uint_as_float(p0[c]) + __shfl_down_sync(0xffffffffu, __uint_as_float(p1[c]), 1) +
+                             __shfl_down_sync(0xffffffffu, __uint_as_float(p2[c]), 2);
+                const int gz = z0 + zq;
+                if (rx < XF_TX && gx < d.W && gy < d.H && gz < d.D) {
+                    const i64 v = gx + (i64)gy * d.W + (i64)gz * d.W * d.H;
+                    if constexpr (MODE == 1) {
+                        reinterpret_cast<float *>(out)[v] = acc[0] + bsh[0];
+                    } else {
+                        uint4 *o = reinterpret_cast<uint4 *>(reinterpret_cast<bf16 *>(out) + v * COUT);
+                        const uint4 *ax = MODE == 2 ? reinterpret_cast<const uint4 *>(aux + v * COUT) : nullptr;
+#pragma unroll
+                        for (int q = 0; q < COUT / 8; q++) {
+                            uint4 mk = make_uint4(0, 0, 0, 0);
+                            if constexpr (MODE == 2) mk = ax[q];
+                            const bf16 *mb = reinterpret_cast<const bf16 *>(&mk);
+                            uint4 pk;
+                            __nv_bfloat162 *p2h = reinterpret_cast<__nv_bfloat162 *>(&pk);
+#pragma unroll
+                            for (int h = 0; h < 4; h++) {
+                                const int ch = q * 8 + 2 * h;
+                                float v0 = acc[ch], v1 = acc[ch + 1];
+                                if constexpr (MODE == 0) {
+                                    v0 = fmaxf(v0 + bsh[ch], 0.f);
+                                    v1 = fmaxf(v1 + bsh[ch + 1], 0.f);
+                                } else {
+                                    if (!(__bfloat162float(mb[2 * h]) > 0.f)) v0 = 0.f;
+                                    if (!(__bfloat162float(mb[2 * h + 1]) > 0.f)) v1 = 0.f;
+                                }
+                                p2h[h] = __floats2bfloat162_rn(v0, v1);
+                            }
+                            o[q] = pk;
+                        }
+                    }
+                }
+            }
+        }
+    }
+    if (failed) atomicOr(err, 1);
+    asm volatile("tcgen05.fence::before_thread_sync;\n");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n");
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "n"(ALLOC));
+}
+
 // The tensor pipe's own ceiling for one instruction shape: one block per SM
-// issues `reps` x 8 back-to-back tcgen05.mma of M = 128, N, K = 16 (bf16,
-// f32 accumulators) on zeroed shared-memory operands, into 256 / N
-// accumulators in turn, and waits for them (bounded).  A convolution made of
+// issues `reps` x 8 back-to-back tcgen05.mma of M = 128, N (32, 48, 64, 96,
+// 128 or 256), K = 16 (bf16, f32 accumulators) on zeroed shared-memory
+// operands, into the accumulators that fit 256 columns in turn, and waits for
+// them (bounded).  A convolution made of
 // N = 32 products (32 output channels) cannot run faster than this kernel at
 // N = 32; measured on GB300 the rate grows with N up to N = 128.
 // operands: A (4 KB) at 0, B (N x 32 bytes, <= 8 KB) at 16 KB; the launch asks
@@ -586,9 +820,12 @@ __global__ void __launch_bounds__(128, 1) k_mma_rate(int reps, int *err) {
         const uint32_t base = smem_addr(rs);
         const uint64_t a = smem_desc(base, 2048, 128), b = smem_desc(base + 16384, N * 16, 128);
         const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | (8u << 24);
+        // accumulators side by side in the 256 columns, each at a multiple of
+        // the power of two >= N (as the convolutions place theirs)
+        constexpr int step = N <= 32 ? 32 : N <= 64 ? 64 : N <= 128 ? 128 : 256, nacc = 256 / step;
         for (int r = 0; r < reps; r++)
 #pragma unroll
-            for (int q = 0; q < 8; q++) tc_mma(tmem + (uint32_t)((q % (256 / N)) * N), a, b, idesc, (r | q) != 0);
+            for (int q = 0; q < 8; q++) tc_mma(tmem + (uint32_t)((q % nacc) * step), a, b, idesc, (r | q) != 0);
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar));
         if (!mbar_wait(bar, 0u, 1 << 24)) atomicOr(err, 1);
     }
@@ -824,7 +1061,7 @@ struct dmtz_cnn {
     const bf16 *last_feat = nullptr;
     const float *last_out = nullptr;
     // convolutions on tcgen05 (1, the default) or on mma.sync (0)
-    int tensor_path = 1;
+    int tensor_path = 2;
     int *tc_err = nullptr;  // set by a tcgen05 convolution whose wait timed out
     // warm-start scratch
     i64 capS = 0;
@@ -893,7 +1130,8 @@ dmtz_status launch_persistent(dmtz_cnn *net, K kernel, int threads, size_t smem,
 
 // tensor map of a channels-last bf16 activation tensor for the TMA box of
 // k_conv_tc (the driver's encoder, looked up once through the runtime)
-dmtz_status box_map(dmtz_cnn *net, CUtensorMap *tm, const bf16 *act, int C, int W, int H, int D) {
+dmtz_status box_map(dmtz_cnn *net, CUtensorMap *tm, const bf16 *act, int C, int W, int H, int D, int bx = GX,
+                    int by = GY, int bz = GZ) {
     static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
     if (!encode) {
         cudaDriverEntryPointQueryResult q;
@@ -906,7 +1144,7 @@ dmtz_status box_map(dmtz_cnn *net, CUtensorMap *tm, const bf16 *act, int C, int 
     }
     const cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)D};
     const cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)C * 2 * W, (cuuint64_t)C * 2 * W * H};
-    const cuuint32_t box[4] = {8, GX, GY, GZ}, estr[4] = {1, 1, 1, 1};
+    const cuuint32_t box[4] = {8, (cuuint32_t)bx, (cuuint32_t)by, (cuuint32_t)bz}, estr[4] = {1, 1, 1, 1};
     const CUresult r = encode(tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16 *>(act), dims, strides, box,
                               estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -917,6 +1155,19 @@ dmtz_status box_map(dmtz_cnn *net, CUtensorMap *tm, const bf16 *act, int C, int 
 template <int CIN, int COUT, int MODE, bool FLIP>
 dmtz_status conv(dmtz_cnn *net, const Dims &d, const bf16 *in, const bf16 *w, const float *bias, void *out,
                  const bf16 *aux, cudaStream_t st) {
+    if (net->tensor_path == 2) {
+        Dims dt = make_xf_dims(d.W, d.H, d.D);
+        CUtensorMap tm;
+        dmtz_status s = box_map(net, &tm, in, CIN, d.W, d.H, d.D, XF_GX, XF_GY, XF_GZ);
+        if (s != DMTZ_OK) return s;
+        int *err = net->tc_err;
+        void *args[] = {&tm, &dt, &w, &bias, &out, &aux, &err};
+        // each block holds 2 x 2 x 64 or 2 x 2 x 128 tensor-memory columns; no more blocks per SM
+        // than the 512 columns hold (a second block's allocation would wait for the first to exit)
+        const int cap = net->nsm * (int)(512 / (4 * xf_cols<COUT>()));
+        return launch_persistent(net, k_conv_tcx<CIN, COUT, MODE, FLIP>, kConvThreads, xf_smem<CIN, COUT>(),
+                                 dt.ntiles, cap, nullptr, st, args);
+    }
     if (net->tensor_path) {
         Dims dt = make_tc_dims(d.W, d.H, d.D);
         CUtensorMap tm;
@@ -1166,18 +1417,19 @@ static dmtz_status check_tc(dmtz_cnn *net) {
 }
 
 dmtz_status dmtz_cnn_set_tensor_path(dmtz_cnn *net, int path) {
-    if (!net || (path != 0 && path != 1)) return DMTZ_ERR_ARG;
+    if (!net || path < 0 || path > 2) return DMTZ_ERR_ARG;
     net->tensor_path = path;
     return DMTZ_OK;
 }
 
 dmtz_status dmtz_cnn_mma_ceiling(dmtz_cnn *net, int n, int reps, double *tflops) {
-    if (!net || !tflops || reps < 1 || reps > (1 << 16) || (n != 32 && n != 64 && n != 128 && n != 256))
-        return DMTZ_ERR_ARG;
+    // the shapes are compile-time constants: the issuing thread does no arithmetic between MMAs
+    void (*kern)(int, int *) = n == 32 ? k_mma_rate<32> : n == 48 ? k_mma_rate<48> : n == 64 ? k_mma_rate<64>
+                             : n == 96 ? k_mma_rate<96> : n == 128 ? k_mma_rate<128> : n == 256 ? k_mma_rate<256>
+                                                                                                 : nullptr;
+    if (!net || !tflops || reps < 1 || reps > (1 << 16) || !kern) return DMTZ_ERR_ARG;
     NCK(cudaSetDevice(net->device));
     cudaStream_t st = net->stream;
-    void (*kern)(int, int *) = n == 32 ? k_mma_rate<32> : n == 64 ? k_mma_rate<64> : n == 128 ? k_mma_rate<128>
-                                                                                             : k_mma_rate<256>;
     NCK(cudaFuncSetAttribute((const void *)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRateSmem));
     int *err = nullptr;
     NCK(cudaMalloc(&err, sizeof(int)));

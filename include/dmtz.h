@@ -328,15 +328,17 @@ dmtz_status dmtz_cnn_forward(dmtz_cnn *net, int W, int H, int D, const void *fea
 dmtz_status dmtz_cnn_backward(dmtz_cnn *net, int W, int H, int D, const float *target, const uint8_t *active,
                               double *loss);
 /* Tensor-core path of the convolutions (no counterpart in the reference):
- * 1 (the default) = tcgen05.mma with the accumulators in tensor memory,
+ * 1 = tcgen05.mma with the accumulators in tensor memory,
+ * 2 (the default) = tcgen05.mma with the three x-taps of each (y, z) offset in one product
+ * of three times the width (partial sums shifted and added in the epilogue),
  * 0 = the warp-level mma.sync kernels.  Same arithmetic (bf16 products, f32
  * sums); results differ only in the order of the f32 sums. */
 dmtz_status dmtz_cnn_set_tensor_path(dmtz_cnn *net, int path);
 /* Measurement only: the tensor pipe's rate, in TFLOP/s over all SMs, for
- * back-to-back tcgen05.mma of shape M = 128, N = n (32, 64, 128 or 256),
- * K = 16 (bf16, f32 accumulators), `reps` x 8 per SM.  The convolutions'
- * products have N = 32 (the output channels), so the n = 32 rate bounds
- * them. */
+ * back-to-back tcgen05.mma of shape M = 128, N = n (32, 48, 64, 96, 128 or
+ * 256), K = 16 (bf16, f32 accumulators), `reps` x 8 per SM.  The
+ * convolutions' products have N = 32 on tensor path 1 and N = 96 (three taps
+ * of 32 output channels) on path 2: those rates bound them. */
 dmtz_status dmtz_cnn_mma_ceiling(dmtz_cnn *net, int n, int reps, double *tflops);
 /* proposal threshold in units of the bound, 0..2 */
 dmtz_status dmtz_cnn_set_min_drop(dmtz_cnn *net, float min_drop);
