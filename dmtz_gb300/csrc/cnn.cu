@@ -1128,8 +1128,9 @@ dmtz_status launch_persistent(dmtz_cnn *net, K kernel, int threads, size_t smem,
     return DMTZ_OK;
 }
 
-// tensor map of a channels-last bf16 activation tensor for the TMA box of
-// k_conv_tc (the driver's encoder, looked up once through the runtime)
+// tensor map of a channels-last bf16 activation tensor for the TMA boxes of
+// k_conv_tc and k_conv_tcx (the CUDA driver's encoder, looked up once through
+// the runtime)
 dmtz_status box_map(dmtz_cnn *net, CUtensorMap *tm, const bf16 *act, int C, int W, int H, int D, int bx = GX,
                     int by = GY, int bz = GZ) {
     static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
