@@ -245,22 +245,20 @@ __global__ void __launch_bounds__(256, 1) k_conv(Dims d, const bf16 *__restrict_
 // The same convolution (same modes, FLIP, epilogues) on the 5th-generation
 // tensor cores: tcgen05.mma with the accumulator in tensor memory.
 //
-// GEMM per tile: D[128 vertices][COUT] = sum over 27 taps of A_tap[128][CIN] x
-// W_tap[CIN][COUT], K = 16 per instruction.  The tile is 8 x 16 x 1 vertices
-// (x, y, z), so its 128 rows are 16 lines of 8 x-neighbours.  Its halo box
-// (10 x 18 x 3 vertices) sits in shared memory as CIN/8 planes, one per
-// 16-byte group of 8 channels, each plane vertex-major (16 bytes per vertex).
-// In that layout the 8 rows of one x-line and one channel group are 128
-// contiguous bytes: one "core matrix" of the no-swizzle K-major operand
-// layout.  A tap's A operand is the box shifted by the tap's offset: its
-// descriptor starts at the shifted vertex, steps 10 x 16 bytes from one line
-// to the next (stride byte offset) and one plane from one channel group to
-// the next (leading byte offset).  Weights are stored per tap as [group][out
-// channel][8 channels], the same layout for B.  One thread issues the MMAs;
-// completion is signalled by tcgen05.commit on an mbarrier (a bounded wait:
-// on timeout the block reports in *err and leaves); each warp then reads its
-// 32 rows of the accumulator (tcgen05.ld, lane = tile row) for the epilogue.
-// The next tile's box streams in by cp.async while the MMAs run.
+// GEMM per z-slice of a tile: D[128 vertices][COUT] = sum over 27 taps of
+// A_tap[128][CIN] x W_tap[CIN][COUT], K = 16 per instruction.  A tile is
+// 8 x 16 x 4 vertices (x, y, z): four slices whose 128 rows are 16 lines of
+// 8 x-neighbours.  Its halo box (10 x 18 x 6 vertices) sits in shared memory
+// as CIN/8 planes, one per 16-byte group of 8 channels, each plane
+// vertex-major (16 bytes per vertex).  In that layout the 8 rows of one
+// x-line and one channel group are 128 contiguous bytes: one "core matrix" of
+// the no-swizzle K-major operand layout.  A tap's A operand is the box
+// shifted by the tap's offset: its descriptor starts at the shifted vertex,
+// steps 10 x 16 bytes from one line to the next (stride byte offset) and one
+// plane from one channel group to the next (leading byte offset).  Weights
+// are stored per tap as [group][out channel][8 channels], the same layout for
+// B.  The boxes arrive by TMA; the roles that issue the MMAs and copies and
+// run the epilogue are described at k_conv_tc.
 constexpr int QX = 8, QY = 16, QZ = 4;  // tile: QZ slices of 128 vertices (one MMA chain each)
 constexpr int GX = QX + 2, GY = QY + 2, GZ = QZ + 2, GVOX = GX * GY * GZ;  // halo box
 inline Dims make_tc_dims(int W, int H, int D) {
